@@ -1,0 +1,319 @@
+// capi.cu -- the extern "C" boundary declared in include/fmmgen_gb300.h.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "../../include/fmmgen_gb300.h"
+#include "internal.h"
+#include "mi_table.cuh"
+
+struct fmmgen_tree {
+  DevTree t;
+  bool built = false;
+  int last_precision = -1;
+};
+
+int fmm_op_batch(int op, int n, const double *d, const double *in, double *out, int order, int so, int potential,
+                 int field, cudaStream_t st);
+void fmm_eval_times(DevTree *t);
+
+namespace {
+thread_local std::string g_err;
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+int ret(int rc) {
+  if (rc == FMM_OK) return rc;
+  if (g_err.empty()) {
+    switch (rc) {
+      case FMM_ERR_ARG: g_err = "invalid argument"; break;
+      case FMM_ERR_DEPTH: g_err = "octree deeper than 21 levels (>= ncrit coincident particles)"; break;
+      case FMM_ERR_RANGE: g_err = "M2L offset range too wide"; break;
+      case FMM_ERR_STATE: g_err = "tree handle not built"; break;
+      default: g_err = "CUDA error"; break;
+    }
+  }
+  return rc;
+}
+}  // namespace
+
+void fmm_set_cuda_error(cudaError_t e, const char *what, const char *file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+  g_err = buf;
+}
+void fmm_set_error_text(const char *msg) { g_err = msg; }
+
+extern "C" {
+
+const char *fmmgen_last_error(void) { return g_err.c_str(); }
+const char *fmmgen_version(void) { return "fmmgen_gb300 0.1 (sm_103a)"; }
+int fmmgen_max_order(void) { return FMM_PMAX; }
+
+long fmmgen_nterms(int p) { return fmm_nterms(p); }
+long fmmgen_msize(int order, int so) { return fmm_nterms(order) - fmm_nterms(so - 1); }
+long fmmgen_lsize(int order, int so) { return fmm_nterms(order - so); }
+int fmmgen_minorder(int so, int field) { return so + (field ? 1 : 0); }
+int fmmgen_sourcesize(int so) { return fmm_nterms(so) - fmm_nterms(so - 1); }
+int fmmgen_outputsize(int potential, int field) { return (potential ? 1 : 0) + (field ? 3 : 0); }
+
+#define OPB(opid, n, d, in, out, order, so, pot, fld, st)                                           \
+  do {                                                                                              \
+    g_err.clear();                                                                                  \
+    return ret(fmm_op_batch(opid, n, d, in, out, order, so, pot, fld, S(st)));                     \
+  } while (0)
+
+int fmmgen_gpu_P2M(int n, const double *d, const double *q, double *M, int order, int so, void *st) {
+  OPB(0, n, d, q, M, order, so, 1, 1, st);
+}
+int fmmgen_gpu_M2M(int n, const double *d, const double *M, double *Ms, int order, int so, void *st) {
+  OPB(1, n, d, M, Ms, order, so, 1, 1, st);
+}
+int fmmgen_gpu_M2L(int n, const double *d, const double *M, double *L, int order, int so, void *st) {
+  OPB(2, n, d, M, L, order, so, 1, 1, st);
+}
+int fmmgen_gpu_L2L(int n, const double *d, const double *L, double *Ls, int order, int so, void *st) {
+  OPB(3, n, d, L, Ls, order, so, 1, 1, st);
+}
+int fmmgen_gpu_L2P(int n, const double *d, const double *L, double *F, int order, int so, int potential, int field,
+                   void *st) {
+  OPB(4, n, d, L, F, order, so, potential, field, st);
+}
+int fmmgen_gpu_P2P(int n, const double *d, const double *Sv, double *F, int so, int potential, int field, void *st) {
+  OPB(5, n, d, Sv, F, 0, so, potential, field, st);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// scalar twins
+// ---------------------------------------------------------------------------
+namespace {
+template <typename T> int d2h(std::vector<T> &v, const T *p, size_t n) {
+  v.resize(n);
+  if (n) FMM_CUDA_TRY(cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+  return FMM_OK;
+}
+struct ScalarCfg {
+  int so = 0, potential = 1, field = 1, maxorder = FMM_PMAX;
+  std::mutex mu;
+  cudaStream_t st = nullptr;
+  double *dbuf = nullptr;  // [3 + NTMAX + NTMAX]
+};
+ScalarCfg g_cfg;
+
+// runs one operator on host arrays through the device path
+void scalar_op(int op, double x, double y, double z, const double *in, int insize, double *out, int outsize,
+               int order) {
+  std::lock_guard<std::mutex> lk(g_cfg.mu);
+  if (!g_cfg.st && cudaStreamCreateWithFlags(&g_cfg.st, cudaStreamNonBlocking) != cudaSuccess) return;
+  if (!g_cfg.dbuf && cudaMalloc((void **)&g_cfg.dbuf, sizeof(double) * (4 + 2 * FMM_NTMAX)) != cudaSuccess) return;
+  double *d = g_cfg.dbuf, *din = d + 4, *dout = din + FMM_NTMAX;
+  double h[3] = {x, y, z};
+  cudaMemcpyAsync(d, h, sizeof(h), cudaMemcpyHostToDevice, g_cfg.st);
+  cudaMemcpyAsync(din, in, sizeof(double) * insize, cudaMemcpyHostToDevice, g_cfg.st);
+  cudaMemcpyAsync(dout, out, sizeof(double) * outsize, cudaMemcpyHostToDevice, g_cfg.st);
+  if (fmm_op_batch(op, 1, d, din, dout, order, g_cfg.so, g_cfg.potential, g_cfg.field, g_cfg.st) != FMM_OK) return;
+  cudaMemcpyAsync(out, dout, sizeof(double) * outsize, cudaMemcpyDeviceToHost, g_cfg.st);
+  cudaStreamSynchronize(g_cfg.st);
+}
+bool order_ok(int order) {
+  return order >= g_cfg.so + (g_cfg.field ? 1 : 0) && order <= g_cfg.maxorder && order <= FMM_PMAX;
+}
+}  // namespace
+
+extern "C" {
+
+int fmmgen_configure(int so, int potential, int field, int maxorder) {
+  if (so < 0 || so > 1 || (!potential && !field) || maxorder < so || maxorder > FMM_PMAX) return ret(FMM_ERR_ARG);
+  std::lock_guard<std::mutex> lk(g_cfg.mu);
+  g_cfg.so = so; g_cfg.potential = potential; g_cfg.field = field; g_cfg.maxorder = maxorder;
+  return FMM_OK;
+}
+void P2M(double x, double y, double z, double q, double *M, int order) {
+  if (!order_ok(order)) return;
+  scalar_op(0, x, y, z, &q, 1, M, (int)fmmgen_msize(order, g_cfg.so), order);
+}
+void M2M(double x, double y, double z, double *M, double *Ms, int order) {
+  if (!order_ok(order)) return;
+  int ms = (int)fmmgen_msize(order, g_cfg.so);
+  scalar_op(1, x, y, z, M, ms, Ms, ms, order);
+}
+void M2L(double x, double y, double z, double *M, double *L, int order) {
+  if (!order_ok(order)) return;
+  scalar_op(2, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), L, (int)fmmgen_lsize(order, g_cfg.so), order);
+}
+void L2L(double x, double y, double z, double *L, double *Ls, int order) {
+  if (!order_ok(order)) return;
+  int ls = (int)fmmgen_lsize(order, g_cfg.so);
+  scalar_op(3, x, y, z, L, ls, Ls, ls, order);
+}
+void L2P(double x, double y, double z, double *L, double *F, int order) {
+  if (!order_ok(order)) return;
+  scalar_op(4, x, y, z, L, (int)fmmgen_lsize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
+            order);
+}
+void P2P(double x, double y, double z, double *Sv, double *F) {
+  scalar_op(5, x, y, z, Sv, fmmgen_sourcesize(g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field), 0);
+}
+
+// ---------------------------------------------------------------------------
+// tree API
+// ---------------------------------------------------------------------------
+int fmmgen_tree_build(const double *pos, long N, long ncrit, int order, double theta, int so, void *stream,
+                      fmmgen_tree **tree) {
+  g_err.clear();
+  if (!tree) return ret(FMM_ERR_ARG);
+  fmmgen_tree *h = *tree;
+  if (!h) h = new fmmgen_tree();
+  h->built = false;
+  int rc = fmm_tree_build(&h->t, pos, N, ncrit, order, theta, so, S(stream));
+  *tree = h;
+  if (rc == FMM_OK) h->built = true;
+  return ret(rc);
+}
+
+int fmmgen_tree_compute_field_fmm(fmmgen_tree *tree, const double *Sv, double *F, int potential, int field,
+                                  int precision, void *stream) {
+  g_err.clear();
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  int rc = fmm_tree_evaluate(&tree->t, Sv, F, potential, field, precision, S(stream));
+  if (rc == FMM_OK) tree->last_precision = precision;
+  return ret(rc);
+}
+
+int fmmgen_gpu_direct(const double *pos, const double *Sv, long N, const long *targets, long ntargets, int so,
+                      int potential, int field, double *F, void *stream) {
+  g_err.clear();
+  return ret(fmm_direct(pos, Sv, N, targets, ntargets, so, potential, field, F, S(stream)));
+}
+
+int fmmgen_tree_free(fmmgen_tree *tree) {
+  if (!tree) return FMM_OK;
+  cudaDeviceSynchronize();
+  fmm_tree_destroy(&tree->t);
+  delete tree;
+  return FMM_OK;
+}
+
+int fmmgen_tree_info(fmmgen_tree *tree, long *info) {
+  g_err.clear();
+  if (!tree || !tree->built || !info) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  info[0] = t.ncells; info[1] = t.nleaves; info[2] = t.nm2l; info[3] = t.np2p;
+  info[4] = t.nlevels; info[5] = t.nclasses; info[6] = t.N; info[7] = t.ncrit;
+  return FMM_OK;
+}
+
+int fmmgen_tree_root(fmmgen_tree *tree, double *root4) {
+  if (!tree || !tree->built || !root4) return ret(FMM_ERR_STATE);
+  root4[0] = tree->t.root.cx; root4[1] = tree->t.root.cy; root4[2] = tree->t.root.cz; root4[3] = tree->t.root.r;
+  return FMM_OK;
+}
+
+int fmmgen_tree_export_cells(fmmgen_tree *tree, unsigned long long *cell_id, long *cell_count, double *centre,
+                             long *leaf_off, long *leaf_idx) {
+  g_err.clear();
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  std::vector<uint64_t> cid;
+  std::vector<int> ps, pc;
+  std::vector<double> x, y, z;
+  std::vector<uint32_t> perm;
+  size_t nc = t.ncells;
+  if (d2h(cid, t.cid.p, nc) || d2h(ps, t.pstart.p, nc) || d2h(pc, t.pcount.p, nc) || d2h(x, t.cx.p, nc) ||
+      d2h(y, t.cy.p, nc) || d2h(z, t.cz.p, nc) || d2h(perm, t.perm.p, t.N))
+    return ret(FMM_ERR_CUDA);
+  long k = 0, o = 0;
+  for (size_t c = 0; c < nc; c++) {
+    if (cell_id) cell_id[c] = cid[c];
+    if (cell_count) cell_count[c] = pc[c];
+    if (centre) { centre[3 * c] = x[c]; centre[3 * c + 1] = y[c]; centre[3 * c + 2] = z[c]; }
+    if (pc[c] < t.ncrit) {
+      if (leaf_off) leaf_off[k] = o;
+      for (int i = 0; i < pc[c]; i++) {
+        if (leaf_idx) leaf_idx[o] = perm[ps[c] + i];
+        o++;
+      }
+      k++;
+    }
+  }
+  if (leaf_off) leaf_off[k] = o;
+  return FMM_OK;
+}
+
+int fmmgen_tree_export_lists(fmmgen_tree *tree, unsigned long long *m2l, unsigned long long *p2p) {
+  g_err.clear();
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  size_t nc = t.ncells;
+  std::vector<uint64_t> cid;
+  std::vector<int> moff, msrc, poff, psrc;
+  if (d2h(cid, t.cid.p, nc) || d2h(moff, t.m2l_off.p, nc + 1) || d2h(msrc, t.m2l_src.p, t.nm2l) ||
+      d2h(poff, t.p2p_off.p, nc + 1) || d2h(psrc, t.p2p_src.p, t.np2p))
+    return ret(FMM_ERR_CUDA);
+  for (size_t c = 0; c < nc; c++) {
+    if (m2l)
+      for (int k = moff[c]; k < moff[c + 1]; k++) { m2l[2 * k] = cid[msrc[k]]; m2l[2 * k + 1] = cid[c]; }
+    if (p2p)
+      for (int k = poff[c]; k < poff[c + 1]; k++) { p2p[2 * k] = cid[c]; p2p[2 * k + 1] = cid[psrc[k]]; }
+  }
+  return FMM_OK;
+}
+
+}  // extern "C"
+
+// M_n = M~_n s^|n|, L_n = L^_n / s^(|n|+1)
+template <typename T>
+__global__ void k_unscale(const T *Ms, const T *Ls, const unsigned char *clevel, const double *lev, int ncells,
+                          int msize, int moff, int lsize, double *Mo, double *Lo) {
+  int c = blockIdx.x;
+  if (c >= ncells) return;
+  double s = lev[2 * clevel[c]];
+  for (int j = threadIdx.x; j < msize; j += blockDim.x) {
+    int d = c_mi[j + moff][3];
+    Mo[(size_t)c * msize + j] = (double)Ms[(size_t)c * msize + j] * pow(s, d);
+  }
+  for (int j = threadIdx.x; j < lsize; j += blockDim.x) {
+    int d = c_mi[j][3];
+    Lo[(size_t)c * lsize + j] = (double)Ls[(size_t)c * lsize + j] / pow(s, d + 1);
+  }
+}
+
+extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, double *L) {
+  g_err.clear();
+  if (!tree || !tree->built || tree->last_precision < 0) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  int ms = (int)fmmgen_msize(t.order, t.so), ls = (int)fmmgen_lsize(t.order, t.so), moff = fmm_nterms(t.so - 1);
+  size_t nc = t.ncells;
+  double *dM = nullptr, *dL = nullptr;
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  FMM_CUDA_TRY(cudaMalloc((void **)&dM, nc * ms * sizeof(double)));
+  FMM_CUDA_TRY(cudaMalloc((void **)&dL, nc * ls * sizeof(double)));
+  if (tree->last_precision == FMMGEN_PREC_FP64)
+    k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
+  else
+    k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(M, dM, nc * ms * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(L, dL, nc * ls * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(dM);
+  cudaFree(dL);
+  if (e != cudaSuccess) {
+    fmm_set_cuda_error(e, "export_expansions", __FILE__, __LINE__);
+    return FMM_ERR_CUDA;
+  }
+  return FMM_OK;
+}
+
+extern "C" int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8) {
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  if (build_ms6) memcpy(build_ms6, tree->t.build_ms, sizeof(float) * 6);
+  if (eval_ms8 && tree->last_precision >= 0) {
+    fmm_eval_times(&tree->t);
+    memcpy(eval_ms8, tree->t.phase_ms, sizeof(float) * 8);
+  }
+  return FMM_OK;
+}

@@ -1,0 +1,81 @@
+// common.cuh -- shared device/host helpers for the GB300 octree FMM library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#define FMM_PMAX 12          // highest expansion order the device code supports
+#define FMM_NTMAX 455        // Nterms(12)
+#define FMM_MAXLEVEL 21      // 3 bits per level in a 64-bit key
+#define FMM_WARPS 4          // warps per block of the warp-per-cell kernels
+
+// Multi-index layout of fmmgen (fmmgen/utils.py:26-35, 65-118): monomials ordered
+// by total degree, then nx descending, then ny descending.
+__host__ __device__ __forceinline__ int fmm_nterms(int p) {
+  return p < 0 ? 0 : (p + 1) * (p + 2) * (p + 3) / 6;
+}
+__host__ __device__ __forceinline__ int fmm_idx3(int nx, int ny, int nz) {
+  int d = nx + ny + nz, j = d - nx;
+  return fmm_nterms(d - 1) + j * (j + 1) / 2 + (j - ny);
+}
+struct MI { unsigned char x, y, z, d; };
+__host__ __device__ __forceinline__ MI fmm_decode(int i) {
+  int d = 0;
+  while (fmm_nterms(d) <= i) d++;
+  int r = i - fmm_nterms(d - 1);
+  int j = 0;
+  while ((j + 1) * (j + 2) / 2 <= r) j++;
+  int ny = j - (r - j * (j + 1) / 2);
+  int nx = d - j;
+  MI m;
+  m.x = (unsigned char)nx; m.y = (unsigned char)ny; m.z = (unsigned char)(d - nx - ny); m.d = (unsigned char)d;
+  return m;
+}
+
+// Error flags raised by kernels (OR-ed into a device word the host reads).
+#define FMM_EFLAG_DEPTH 1u     // a cell at FMM_MAXLEVEL still holds >= ncrit particles
+#define FMM_EFLAG_RANGE 2u     // an M2L offset outside the class table's range
+#define FMM_EFLAG_BOUNDS 4u    // an index check failed (never expected)
+
+// Status codes of the C ABI (mirrored in include/fmmgen_gb300.h).
+#define FMM_OK 0
+#define FMM_ERR_ARG 1
+#define FMM_ERR_CUDA 2
+#define FMM_ERR_DEPTH 3
+#define FMM_ERR_RANGE 4
+#define FMM_ERR_STATE 5
+
+#define FMM_CUDA_TRY(expr)                                  \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) { fmm_set_cuda_error(_e, #expr, __FILE__, __LINE__); return FMM_ERR_CUDA; } \
+  } while (0)
+
+void fmm_set_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+void fmm_set_error_text(const char *msg);
+
+__device__ __forceinline__ unsigned fmm_lane() { return threadIdx.x & 31u; }
+
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t cap = 0;  // elements
+};
+// Grow-only device buffer (contents are not preserved on growth).
+template <typename T> int fmm_reserve(DevBuf<T> &b, size_t n) {
+  if (n <= b.cap && b.p) return FMM_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr; b.cap = 0;
+  size_t want = n < 16 ? 16 : n + n / 8;
+  FMM_CUDA_TRY(cudaMalloc((void **)&b.p, want * sizeof(T)));
+  b.cap = want;
+  return FMM_OK;
+}
+template <typename T> void fmm_release(DevBuf<T> &b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr; b.cap = 0;
+}
+
+static inline unsigned fmm_blocks(size_t n, unsigned bs) {
+  size_t b = (n + bs - 1) / bs;
+  return (unsigned)(b == 0 ? 1 : b);
+}

@@ -1,0 +1,643 @@
+// eval.cu -- the FMM evaluation pass on the device octree
+// (Tree::compute_field_fmm, example/tree.cpp:243-271).
+//
+// Expansions are kept scaled by the cell half-width s so that both FP64 and
+// FP32 see O(1) numbers at any cell size:
+//   M~_n = M_n / s^|n|            L^_n = s^(|n|+1) L_n
+// which turns the operators into
+//   P2M  M~_n  = sum_p q ((c - x)/s)^n / n!                      (dipole: sum_j S_j/s (..)^(n-e_j)/(n-e_j)!)
+//   M2M  M~p_n = sum_k M~c_{n-k} 2^-|n-k| (d/s_p)^k / k!          d = parent - child
+//   M2L  L^A_n = sum_m 2^((lA-lB)|m|) D_{n+m}(d/s_A) M~B_m        d = A - B
+//   L2L  L^c_n = 2^-(|n|+1) sum_k (d/s_p)^k / k! L^p_{n+k}          d = child - parent
+//   L2P  phi   = (1/s) sum_n L^_n (r/s)^n / n!,  E = -grad phi      r = particle - cell
+// (fmmgen/expansions.py:22-207 with D homogeneous of degree -|k|-1).  The
+// displacement conventions are those of example/calculate.cpp:149-151, 182-184,
+// 201-203, 227-229, 243-245.
+#include <algorithm>
+#include "internal.h"
+#include "mi_table.cuh"
+
+#define TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
+
+// ---------------------------------------------------------------------------
+// warp contraction engine (plans.cu)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void engine_run(const Plan &P, const T *A, const T *B, T *slots, int lane) {
+  T acc = T(0);
+  for (int it = 0; it < P.iters; ++it) {
+    uint32_t w = __ldg(&P.task[it * 32 + lane]);
+    if (w == 0xffffffffu) break;
+    acc += A[w & 1023u] * B[(w >> 10) & 1023u];
+    if (w >> 31) {
+      slots[(w >> 20) & 2047u] += acc;
+      acc = T(0);
+    }
+  }
+}
+template <typename T> __device__ __forceinline__ T engine_out(const Plan &P, const T *slots, int n) {
+  T s = T(0);
+  for (int k = __ldg(&P.out_seg[n]); k < __ldg(&P.out_seg[n + 1]); k++) s += slots[k];
+  return s;
+}
+
+__device__ __forceinline__ double pow2i(int e) { return ldexp(1.0, e); }
+
+// per-level half-width s_l and 1/s_l (exact powers of two times the root r)
+struct Levels { const double *lev; };
+
+// ---------------------------------------------------------------------------
+// P2M (example/calculate.cpp:135-161)
+// ---------------------------------------------------------------------------
+#define NPL ((FMM_NTMAX + 31) / 32)
+template <typename T>
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, int nleaves, const int *pstart,
+                                                        const int *pcount, const unsigned char *clevel,
+                                                        const double *cx, const double *cy, const double *cz,
+                                                        const double *px, const double *py, const double *pz,
+                                                        const uint32_t *perm, const double *S, int so, int order,
+                                                        const double *lev, T *M) {
+  __shared__ T tb[FMM_WARPS][3][32][FMM_PMAX + 1];
+  __shared__ T sq[FMM_WARPS][32][3];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int leaf = blockIdx.x * FMM_WARPS + w;
+  if (leaf >= nleaves) return;
+  const int c = leaf_cells[leaf];
+  const int off = fmm_nterms(so - 1), msize = fmm_nterms(order) - off;
+  const double s = lev[2 * clevel[c]];
+  const double inv_s = s > 0 ? 1.0 / s : 0.0;  // a zero-width root (coincident points) has no far field
+  const double ccx = cx[c], ccy = cy[c], ccz = cz[c];
+  const int p0 = pstart[c], np = pcount[c];
+  T acc[NPL];
+#pragma unroll
+  for (int k = 0; k < NPL; k++) acc[k] = T(0);
+  for (int base = 0; base < np; base += 32) {
+    int j = base + lane;
+    if (j < np) {
+      int i = p0 + j;
+      T ux = (T)((ccx - px[i]) * inv_s), uy = (T)((ccy - py[i]) * inv_s), uz = (T)((ccz - pz[i]) * inv_s);
+      T a = 1, b = 1, d = 1;
+      tb[w][0][lane][0] = a; tb[w][1][lane][0] = b; tb[w][2][lane][0] = d;
+      for (int k = 1; k <= order; k++) {
+        a = a * ux / T(k); b = b * uy / T(k); d = d * uz / T(k);
+        tb[w][0][lane][k] = a; tb[w][1][lane][k] = b; tb[w][2][lane][k] = d;
+      }
+      uint32_t o = perm[i];
+      if (so == 0) {
+        sq[w][lane][0] = (T)S[o];
+      } else {
+        sq[w][lane][0] = (T)(S[3 * (size_t)o] * inv_s);
+        sq[w][lane][1] = (T)(S[3 * (size_t)o + 1] * inv_s);
+        sq[w][lane][2] = (T)(S[3 * (size_t)o + 2] * inv_s);
+      }
+    }
+    __syncwarp();
+    int cnt = min(32, np - base);
+#pragma unroll
+    for (int k = 0; k < NPL; k++) {
+      int i = lane + 32 * k;
+      if (i < msize) {
+        int nx = c_mi[i + off][0], ny = c_mi[i + off][1], nz = c_mi[i + off][2];
+        T sum = acc[k];
+        if (so == 0) {
+          for (int jj = 0; jj < cnt; jj++)
+            sum += sq[w][jj][0] * tb[w][0][jj][nx] * tb[w][1][jj][ny] * tb[w][2][jj][nz];
+        } else {
+          for (int jj = 0; jj < cnt; jj++) {
+            if (nx) sum += sq[w][jj][0] * tb[w][0][jj][nx - 1] * tb[w][1][jj][ny] * tb[w][2][jj][nz];
+            if (ny) sum += sq[w][jj][1] * tb[w][0][jj][nx] * tb[w][1][jj][ny - 1] * tb[w][2][jj][nz];
+            if (nz) sum += sq[w][jj][2] * tb[w][0][jj][nx] * tb[w][1][jj][ny] * tb[w][2][jj][nz - 1];
+          }
+        }
+        acc[k] = sum;
+      }
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int k = 0; k < NPL; k++) {
+    int i = lane + 32 * k;
+    if (i < msize) M[(size_t)c * msize + i] = acc[k];
+  }
+}
+
+// shift monomials mon[idx(k)] = v^k / k! for |k| <= pmax (warp-parallel)
+template <typename T>
+__device__ __forceinline__ void warp_monomials(double vx, double vy, double vz, int pmax, T *mon, int lane) {
+  int cnt = fmm_nterms(pmax);
+  for (int i = lane; i < cnt; i += 32) {
+    int kx = c_mi[i][0], ky = c_mi[i][1], kz = c_mi[i][2];
+    double a = 1, b = 1, d = 1;
+    for (int q = 1; q <= kx; q++) a = a * vx / q;
+    for (int q = 1; q <= ky; q++) b = b * vy / q;
+    for (int q = 1; q <= kz; q++) d = d * vz / q;
+    mon[i] = (T)(a * b * d);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// M2M for all parents of one level (example/calculate.cpp:163-187)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, int so, int order,
+                                                        const unsigned char *child_mask, const int *child_first,
+                                                        const unsigned char *clevel, const double *cx,
+                                                        const double *cy, const double *cz, const double *lev,
+                                                        T *M) {
+  __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = lo + blockIdx.x * FMM_WARPS + w;
+  if (c >= hi) return;
+  unsigned mask = child_mask[c];
+  if (!mask) return;
+  const int off = fmm_nterms(so - 1), msize = fmm_nterms(order) - off;
+  const double inv_s = 1.0 / lev[2 * clevel[c]];
+  for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
+  int ch = child_first[c];
+  int nch = __popc(mask);
+  for (int q = 0; q < nch; q++, ch++) {
+    __syncwarp();
+    warp_monomials<T>((cx[c] - cx[ch]) * inv_s, (cy[c] - cy[ch]) * inv_s, (cz[c] - cz[ch]) * inv_s, order - so,
+                      sA[w], lane);
+    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)ch * msize + j] * (T)pow2i(-(int)c_mi[j + off][3]);
+    __syncwarp();
+    engine_run<T>(P, sA[w], sB[w], sS[w], lane);
+  }
+  __syncwarp();
+  for (int n = lane; n < msize; n += 32) M[(size_t)c * msize + n] = engine_out<T>(P, sS[w], n);
+}
+
+// ---------------------------------------------------------------------------
+// M2L, one warp per target cell (example/calculate.cpp:190-206)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l(Plan P, int ncells, int so, int order, const int *off_,
+                                                        const int *src, const int *cls, const T *clsD,
+                                                        const unsigned char *clevel, const T *M, T *L) {
+  __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int A = blockIdx.x * FMM_WARPS + w;
+  if (A >= ncells) return;
+  const int moff = fmm_nterms(so - 1), msize = fmm_nterms(order) - moff, lsize = fmm_nterms(order - so);
+  const int nt = fmm_nterms(order);
+  const int k0 = off_[A], k1 = off_[A + 1];
+  if (k0 == k1) {
+    for (int n = lane; n < lsize; n += 32) L[(size_t)A * lsize + n] = T(0);
+    return;
+  }
+  for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
+  const int la = clevel[A];
+  for (int k = k0; k < k1; k++) {
+    const int B = src[k];
+    const T *D = clsD + (size_t)cls[k] * nt;
+    const int dl = la - (int)clevel[B];  // rho = s_B / s_A = 2^(lA - lB)
+    __syncwarp();
+    for (int i = lane; i < nt; i += 32) sA[w][i] = D[i];
+    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)B * msize + j] * (T)pow2i(dl * (int)c_mi[j + moff][3]);
+    __syncwarp();
+    engine_run<T>(P, sA[w], sB[w], sS[w], lane);
+  }
+  __syncwarp();
+  for (int n = lane; n < lsize; n += 32) L[(size_t)A * lsize + n] = engine_out<T>(P, sS[w], n);
+}
+
+// ---------------------------------------------------------------------------
+// L2L for all cells of one level (example/calculate.cpp:219-234)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_l2l(Plan P, int lo, int hi, int so, int order,
+                                                        const int *parent, const unsigned char *clevel,
+                                                        const double *cx, const double *cy, const double *cz,
+                                                        const double *lev, T *L) {
+  __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = lo + blockIdx.x * FMM_WARPS + w;
+  if (c >= hi) return;
+  const int p = parent[c];
+  const int lsize = fmm_nterms(order - so);
+  const double inv_s = 1.0 / lev[2 * clevel[p]];
+  for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
+  warp_monomials<T>((cx[c] - cx[p]) * inv_s, (cy[c] - cy[p]) * inv_s, (cz[c] - cz[p]) * inv_s, order - so, sA[w],
+                    lane);
+  for (int j = lane; j < lsize; j += 32) sB[w][j] = L[(size_t)p * lsize + j];
+  __syncwarp();
+  engine_run<T>(P, sA[w], sB[w], sS[w], lane);
+  __syncwarp();
+  for (int n = lane; n < lsize; n += 32)
+    L[(size_t)c * lsize + n] += engine_out<T>(P, sS[w], n) * (T)pow2i(-((int)c_mi[n][3] + 1));
+}
+
+// ---------------------------------------------------------------------------
+// L2P, one warp per leaf, one lane per particle (example/calculate.cpp:236-250)
+// ---------------------------------------------------------------------------
+#define L2P_WARPS 2
+template <typename T>
+__global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, int nleaves, const int *pstart,
+                                                        const int *pcount, const unsigned char *clevel,
+                                                        const double *cx, const double *cy, const double *cz,
+                                                        const double *px, const double *py, const double *pz,
+                                                        int so, int order, const double *lev, const T *L,
+                                                        double *Ffar) {
+  __shared__ T sL[L2P_WARPS][FMM_NTMAX];
+  __shared__ T tb[L2P_WARPS][3][FMM_PMAX + 1][33];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int leaf = blockIdx.x * L2P_WARPS + w;
+  if (leaf >= nleaves) return;
+  const int c = leaf_cells[leaf];
+  const int pl = order - so, lsize = fmm_nterms(pl);
+  const double s = lev[2 * clevel[c]], inv_s = s > 0 ? 1.0 / s : 0.0;
+  for (int j = lane; j < lsize; j += 32) sL[w][j] = s > 0 ? L[(size_t)c * lsize + j] : T(0);
+  __syncwarp();
+  const int p0 = pstart[c], np = pcount[c];
+  for (int base = 0; base < np; base += 32) {
+    int i = p0 + base + lane;
+    bool ok = base + lane < np;
+    if (ok) {
+      T ux = (T)((px[i] - cx[c]) * inv_s), uy = (T)((py[i] - cy[c]) * inv_s), uz = (T)((pz[i] - cz[c]) * inv_s);
+      T a = 1, b = 1, d = 1;
+      tb[w][0][0][lane] = a; tb[w][1][0][lane] = b; tb[w][2][0][lane] = d;
+      for (int k = 1; k <= pl; k++) {
+        a = a * ux / T(k); b = b * uy / T(k); d = d * uz / T(k);
+        tb[w][0][k][lane] = a; tb[w][1][k][lane] = b; tb[w][2][k][lane] = d;
+      }
+      T phi = 0, ex = 0, ey = 0, ez = 0;
+      for (int n = 0; n < lsize; n++) {
+        int nx = c_mi[n][0], ny = c_mi[n][1], nz = c_mi[n][2];
+        T l = sL[w][n];
+        T yz = tb[w][1][ny][lane] * tb[w][2][nz][lane];
+        phi += l * tb[w][0][nx][lane] * yz;
+        if (nx) ex += l * tb[w][0][nx - 1][lane] * yz;
+        if (ny) ey += l * tb[w][0][nx][lane] * tb[w][1][ny - 1][lane] * tb[w][2][nz][lane];
+        if (nz) ez += l * tb[w][0][nx][lane] * tb[w][1][ny][lane] * tb[w][2][nz - 1][lane];
+      }
+      double is2 = inv_s * inv_s;
+      Ffar[4 * (size_t)i] = (double)phi * inv_s;
+      Ffar[4 * (size_t)i + 1] = -(double)ex * is2;
+      Ffar[4 * (size_t)i + 2] = -(double)ey * is2;
+      Ffar[4 * (size_t)i + 3] = -(double)ez * is2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// P2P in FP64, one warp per target leaf (example/calculate.cpp:24-40, 208-216)
+// ---------------------------------------------------------------------------
+#define P2P_WARPS 4
+__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p64(const int *leaf_cells, int nleaves, const int *pstart,
+                                                          const int *pcount, const int *off_, const int *src,
+                                                          const double *px, const double *py, const double *pz,
+                                                          const uint32_t *perm, const double *S, int so,
+                                                          double *Fnear) {
+  __shared__ double sx[P2P_WARPS][32], sy[P2P_WARPS][32], sz[P2P_WARPS][32], sq[P2P_WARPS][32][3];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int leaf = blockIdx.x * P2P_WARPS + w;
+  if (leaf >= nleaves) return;
+  const int A = leaf_cells[leaf];
+  const int a0 = pstart[A], na = pcount[A];
+  const int k0 = off_[A], k1 = off_[A + 1];
+  for (int tb = 0; tb < na; tb += 32) {
+    const int i = a0 + tb + lane;
+    const bool ok = tb + lane < na;
+    double xi = 0, yi = 0, zi = 0;
+    if (ok) { xi = px[i]; yi = py[i]; zi = pz[i]; }
+    double phi = 0, ex = 0, ey = 0, ez = 0;
+    for (int k = k0; k < k1; k++) {
+      const int B = src[k];
+      const int b0 = pstart[B], nb = pcount[B];
+      for (int sb = 0; sb < nb; sb += 32) {
+        __syncwarp();
+        int j = b0 + sb + lane;
+        if (sb + lane < nb) {
+          sx[w][lane] = px[j]; sy[w][lane] = py[j]; sz[w][lane] = pz[j];
+          uint32_t o = perm[j];
+          if (so == 0) sq[w][lane][0] = S[o];
+          else { sq[w][lane][0] = S[3 * (size_t)o]; sq[w][lane][1] = S[3 * (size_t)o + 1]; sq[w][lane][2] = S[3 * (size_t)o + 2]; }
+        }
+        __syncwarp();
+        const int cnt = min(32, nb - sb);
+        if (ok) {
+          for (int jj = 0; jj < cnt; jj++) {
+            if (b0 + sb + jj == i) continue;  // l2 != l1
+            double dx = xi - sx[w][jj], dy = yi - sy[w][jj], dz = zi - sz[w][jj];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            double rinv = rsqrt(r2);
+            double r3 = rinv * rinv * rinv;
+            if (so == 0) {
+              double q = sq[w][jj][0];
+              phi += q * rinv;
+              double qr3 = q * r3;
+              ex += qr3 * dx; ey += qr3 * dy; ez += qr3 * dz;
+            } else {
+              double sxj = sq[w][jj][0], syj = sq[w][jj][1], szj = sq[w][jj][2];
+              double sr = sxj * dx + syj * dy + szj * dz;
+              double r5 = 3.0 * sr * r3 * rinv * rinv;
+              phi -= sr * r3;
+              ex += sxj * r3 - r5 * dx; ey += syj * r3 - r5 * dy; ez += szj * r3 - r5 * dz;
+            }
+          }
+        }
+      }
+    }
+    if (ok) {
+      Fnear[4 * (size_t)i] = phi; Fnear[4 * (size_t)i + 1] = ex;
+      Fnear[4 * (size_t)i + 2] = ey; Fnear[4 * (size_t)i + 3] = ez;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// P2P in FP32 with compensated accumulation (mixed precision)
+// ---------------------------------------------------------------------------
+// Positions are FP32 offsets from the particle's own leaf centre; the offset
+// between the two leaf centres is formed in FP64 once per leaf pair.  Each
+// source leaf's contribution is summed in FP32 (<= ncrit terms) and folded into
+// a Kahan-compensated FP32 total.  rsqrt is the hardware approximation plus
+// one Newton step.
+__device__ __forceinline__ float rsqrt_nr(float r2) {
+  float y = rsqrtf(r2);
+  return y * fmaf(-0.5f * r2 * y, y, 1.5f);
+}
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
+  float y = v - c;
+  float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
+                                                          const int *pcount, const int *off_, const int *src,
+                                                          const double *cx, const double *cy, const double *cz,
+                                                          const float *lx, const float *ly, const float *lz,
+                                                          const uint32_t *perm, const double *S, int so,
+                                                          double *Fnear) {
+  __shared__ float4 sp[P2P_WARPS][32];
+  __shared__ float4 sd[P2P_WARPS][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int leaf = blockIdx.x * P2P_WARPS + w;
+  if (leaf >= nleaves) return;
+  const int A = leaf_cells[leaf];
+  const int a0 = pstart[A], na = pcount[A];
+  const int k0 = off_[A], k1 = off_[A + 1];
+  const double cax = cx[A], cay = cy[A], caz = cz[A];
+  for (int tb = 0; tb < na; tb += 32) {
+    const int i = a0 + tb + lane;
+    const bool ok = tb + lane < na;
+    float xi = 0, yi = 0, zi = 0;
+    if (ok) { xi = lx[i]; yi = ly[i]; zi = lz[i]; }
+    float s0 = 0, s1 = 0, s2 = 0, s3 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    for (int k = k0; k < k1; k++) {
+      const int B = src[k];
+      const int b0 = pstart[B], nb = pcount[B];
+      const float ox = (float)(cax - cx[B]), oy = (float)(cay - cy[B]), oz = (float)(caz - cz[B]);
+      const float tx = xi + ox, ty = yi + oy, tz = zi + oz;
+      float phi = 0, ex = 0, ey = 0, ez = 0;
+      for (int sb = 0; sb < nb; sb += 32) {
+        __syncwarp();
+        int j = b0 + sb + lane;
+        if (sb + lane < nb) {
+          uint32_t o = perm[j];
+          if (so == 0) {
+            sp[w][lane] = make_float4(lx[j], ly[j], lz[j], (float)S[o]);
+          } else {
+            sp[w][lane] = make_float4(lx[j], ly[j], lz[j], 0.f);
+            sd[w][lane] = make_float4((float)S[3 * (size_t)o], (float)S[3 * (size_t)o + 1], (float)S[3 * (size_t)o + 2], 0.f);
+          }
+        }
+        __syncwarp();
+        const int cnt = min(32, nb - sb);
+        const int self = (B == A) ? (i - (b0 + sb)) : -1;  // skip l2 == l1
+        if (so == 0) {
+#pragma unroll 4
+          for (int jj = 0; jj < cnt; jj++) {
+            float4 q = sp[w][jj];
+            float dx = tx - q.x, dy = ty - q.y, dz = tz - q.z;
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float rinv = (jj == self) ? 0.f : rsqrt_nr(r2);
+            float qr = q.w * rinv;
+            float qr3 = qr * rinv * rinv;
+            phi += qr;
+            ex = fmaf(qr3, dx, ex); ey = fmaf(qr3, dy, ey); ez = fmaf(qr3, dz, ez);
+          }
+        } else {
+          for (int jj = 0; jj < cnt; jj++) {
+            float4 q = sp[w][jj];
+            float4 d = sd[w][jj];
+            float dx = tx - q.x, dy = ty - q.y, dz = tz - q.z;
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float rinv = (jj == self) ? 0.f : rsqrt_nr(r2);
+            float r3 = rinv * rinv * rinv;
+            float sr = fmaf(d.x, dx, fmaf(d.y, dy, d.z * dz));
+            float r5 = 3.f * sr * r3 * rinv * rinv;
+            phi -= sr * r3;
+            ex += d.x * r3 - r5 * dx; ey += d.y * r3 - r5 * dy; ez += d.z * r3 - r5 * dz;
+          }
+        }
+      }
+      kahan_add(s0, c0, phi); kahan_add(s1, c1, ex); kahan_add(s2, c2, ey); kahan_add(s3, c3, ez);
+    }
+    if (ok) {
+      Fnear[4 * (size_t)i] = (double)s0 - (double)c0;
+      Fnear[4 * (size_t)i + 1] = (double)s1 - (double)c1;
+      Fnear[4 * (size_t)i + 2] = (double)s2 - (double)c2;
+      Fnear[4 * (size_t)i + 3] = (double)s3 - (double)c3;
+    }
+  }
+}
+
+// local FP32 coordinates: particle - its leaf centre
+__global__ void k_local_coords(const int *leaf_cells, int nleaves, const int *pstart, const int *pcount,
+                               const double *cx, const double *cy, const double *cz, const double *px,
+                               const double *py, const double *pz, float *lx, float *ly, float *lz) {
+  int leaf = blockIdx.x;
+  if (leaf >= nleaves) return;
+  int c = leaf_cells[leaf];
+  for (int j = threadIdx.x; j < pcount[c]; j += blockDim.x) {
+    int i = pstart[c] + j;
+    lx[i] = (float)(px[i] - cx[c]);
+    ly[i] = (float)(py[i] - cy[c]);
+    lz[i] = (float)(pz[i] - cz[c]);
+  }
+}
+
+// F[caller index][outsize] = near + far, in FP64
+__global__ void k_finalize(const double *Fnear, const double *Ffar, const uint32_t *perm, long N, int potential,
+                           int field, double *F) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int outsize = (potential ? 1 : 0) + (field ? 3 : 0);
+  size_t o = (size_t)perm[i] * outsize;
+  const double *a = Fnear + 4 * (size_t)i, *b = Ffar + 4 * (size_t)i;
+  int k = 0;
+  if (potential) F[o + k++] = a[0] + b[0];
+  if (field) {
+    F[o + k] = a[1] + b[1];
+    F[o + k + 1] = a[2] + b[2];
+    F[o + k + 2] = a[3] + b[3];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+static int rec(DevTree *t, int i, cudaStream_t st) {
+  FMM_CUDA_TRY(cudaEventRecord(t->ev[6 + i], st));
+  return FMM_OK;
+}
+
+template <typename T>
+static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, cudaStream_t st) {
+  const int p = t->order, so = t->so;
+  const double *lev = t->d_root.p + 16;
+  const int nl = t->nleaves, nc = t->ncells;
+  // P2M
+  k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+      t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
+      t->pz.p, t->perm.p, S, so, p, lev, M);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 1, st));
+  // M2M, deepest parents first
+  for (int l = t->nlevels - 2; l >= 0; l--) {
+    int lo = t->level_off[l], hi = t->level_off[l + 1];
+    k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, M);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 2, st));
+  // M2L
+  k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+      ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
+      mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 3, st));
+  // P2P
+  if (mixed)
+    k_p2p32<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
+        t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->cx.p, t->cy.p, t->cz.p,
+        t->lx.p, t->ly.p, t->lz.p, t->perm.p, S, so, t->Fnear.p);
+  else
+    k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
+        t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->px.p, t->py.p, t->pz.p,
+        t->perm.p, S, so, t->Fnear.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 4, st));
+  // L2L, top-down
+  for (int l = 1; l < t->nlevels; l++) {
+    int lo = t->level_off[l], hi = t->level_off[l + 1];
+    k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(ps->l2l, lo, hi, so, p, t->parent.p,
+                                                                         t->clevel.p, t->cx.p, t->cy.p, t->cz.p,
+                                                                         lev, L);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 5, st));
+  // L2P
+  k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(t->leaf_cells.p, nl, t->pstart.p, t->pcount.p,
+                                                                  t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p,
+                                                                  t->py.p, t->pz.p, so, p, lev, L, t->Ffar.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 6, st));
+  return FMM_OK;
+}
+
+int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
+                      cudaStream_t st) {
+  if (!t || t->ncells == 0) return FMM_ERR_STATE;
+  if (!S || !F || (!potential && !field) || precision < 0 || precision > 1) return FMM_ERR_ARG;
+  const PlanSet *ps = fmm_get_plans(t->order, t->so);
+  if (!ps) return FMM_ERR_CUDA;
+  const bool mixed = precision == 1;
+  const int p = t->order, so = t->so;
+  const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
+  const size_t nc = t->ncells;
+  TRY(fmm_reserve(t->Fnear, 4 * (size_t)t->N));
+  TRY(fmm_reserve(t->Ffar, 4 * (size_t)t->N));
+  TRY(rec(t, 0, st));
+  if (mixed) {
+    TRY(fmm_reserve(t->Mf, nc * msize));
+    TRY(fmm_reserve(t->Lf, nc * lsize));
+    TRY(fmm_reserve(t->lx, t->N)); TRY(fmm_reserve(t->ly, t->N)); TRY(fmm_reserve(t->lz, t->N));
+    k_local_coords<<<t->nleaves, 128, 0, st>>>(t->leaf_cells.p, t->nleaves, t->pstart.p, t->pcount.p, t->cx.p,
+                                               t->cy.p, t->cz.p, t->px.p, t->py.p, t->pz.p, t->lx.p, t->ly.p,
+                                               t->lz.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, st));
+  } else {
+    TRY(fmm_reserve(t->M, nc * msize));
+    TRY(fmm_reserve(t->L, nc * lsize));
+    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, st));
+  }
+  k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N, potential, field, F);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 7, st));
+  return FMM_OK;
+}
+
+// Per-phase times of the last evaluate (needs the stream to have completed).
+void fmm_eval_times(DevTree *t) {
+  float ms;
+  for (int i = 0; i < 7; i++) {
+    cudaEventElapsedTime(&ms, t->ev[6 + i], t->ev[6 + i + 1]);
+    t->phase_ms[i] = ms;
+  }
+  cudaEventElapsedTime(&ms, t->ev[6], t->ev[13]);
+  t->phase_ms[7] = ms;
+}
+
+// ---------------------------------------------------------------------------
+// direct O(N^2) sum in FP64 (example/calculate.cpp:252-264)
+// ---------------------------------------------------------------------------
+#define DIR_BS 128
+__global__ void __launch_bounds__(DIR_BS) k_direct(const double *pos, const double *S, long N, const long *targets,
+                                                   long nt, int so, int potential, int field, double *F) {
+  __shared__ double sx[DIR_BS], sy[DIR_BS], sz[DIR_BS], sq[DIR_BS][3];
+  long t = blockIdx.x * (long)DIR_BS + threadIdx.x;
+  long i = t < nt ? (targets ? targets[t] : t) : -1;
+  double xi = 0, yi = 0, zi = 0;
+  if (i >= 0) { xi = pos[3 * i]; yi = pos[3 * i + 1]; zi = pos[3 * i + 2]; }
+  double phi = 0, ex = 0, ey = 0, ez = 0;
+  for (long b = 0; b < N; b += DIR_BS) {
+    __syncthreads();
+    long j = b + threadIdx.x;
+    if (j < N) {
+      sx[threadIdx.x] = pos[3 * j]; sy[threadIdx.x] = pos[3 * j + 1]; sz[threadIdx.x] = pos[3 * j + 2];
+      if (so == 0) sq[threadIdx.x][0] = S[j];
+      else { sq[threadIdx.x][0] = S[3 * j]; sq[threadIdx.x][1] = S[3 * j + 1]; sq[threadIdx.x][2] = S[3 * j + 2]; }
+    }
+    __syncthreads();
+    int cnt = (int)min((long)DIR_BS, N - b);
+    if (i < 0) continue;
+    for (int jj = 0; jj < cnt; jj++) {
+      if (b + jj == i) continue;
+      double dx = xi - sx[jj], dy = yi - sy[jj], dz = zi - sz[jj];
+      double R = sqrt(dx * dx + dy * dy + dz * dz);
+      double rinv = 1.0 / R;
+      double r3 = rinv * rinv * rinv;
+      if (so == 0) {
+        double q = sq[jj][0];
+        phi += q * rinv;
+        ex += q * dx * r3; ey += q * dy * r3; ez += q * dz * r3;
+      } else {
+        double a = sq[jj][0], bb = sq[jj][1], c = sq[jj][2];
+        double sr = a * dx + bb * dy + c * dz;
+        double r5 = r3 * rinv * rinv;
+        phi -= sr * r3;
+        ex += a * r3 - 3.0 * sr * dx * r5; ey += bb * r3 - 3.0 * sr * dy * r5; ez += c * r3 - 3.0 * sr * dz * r5;
+      }
+    }
+  }
+  if (i >= 0) {
+    int outsize = (potential ? 1 : 0) + (field ? 3 : 0);
+    size_t o = (size_t)t * outsize;
+    int k = 0;
+    if (potential) F[o + k++] = phi;
+    if (field) { F[o + k] = ex; F[o + k + 1] = ey; F[o + k + 2] = ez; }
+  }
+}
+
+int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
+               int potential, int field, double *F, cudaStream_t st) {
+  if (!pos || !S || !F || N < 1 || (!potential && !field) || so < 0 || so > 1) return FMM_ERR_ARG;
+  long nt = targets ? ntargets : N;
+  if (nt < 1) return FMM_OK;
+  k_direct<<<fmm_blocks(nt, DIR_BS), DIR_BS, 0, st>>>(pos, S, N, targets, nt, so, potential, field, F);
+  FMM_CUDA_TRY(cudaGetLastError());
+  return FMM_OK;
+}

@@ -1,0 +1,87 @@
+// internal.h -- the device octree handle and the host-side entry points that
+// tree.cu / eval.cu / plans.cu export to capi.cu.
+#pragma once
+#include <vector>
+#include "common.cuh"
+
+// Root cube of build_tree (example/tree.cpp:139-187): mean-centred, half-width
+// 1.001 * max |x - mean|.
+struct RootBox {
+  double cx, cy, cz, r;
+};
+
+// Task plan of the warp contraction engine (see plans.cu): one warp applies
+//   out[n] (+)= scale(n) * sum_t A[a_t] * B[b_t]
+// with the tasks of each output split into per-lane segments.
+struct Plan {
+  const uint32_t *task = nullptr;  // [iters][32]: a(10) | b(10)<<10 | slot(11)<<20 | end(1)<<31; 0xffffffff = pad
+  const int *out_seg = nullptr;    // [nout+1] segment range of each output (segments of one output are consecutive)
+  int iters = 0, nout = 0, nseg = 0;
+};
+struct PlanSet {
+  int order = -1, so = -1;
+  Plan m2l, m2m, l2l;
+  void *dmem = nullptr;  // one allocation holding every table
+};
+const PlanSet *fmm_get_plans(int order, int so);  // cached per device
+
+struct DevTree {
+  // configuration
+  long N = 0, ncrit = 0;
+  int order = 0, so = 0;
+  double theta = 0;
+  int dev = 0;
+  RootBox root;
+  // levels: cells of level l are [level_off[l], level_off[l+1])
+  int nlevels = 0;
+  std::vector<int> level_off;
+  int ncells = 0, nleaves = 0;
+  long nm2l = 0, np2p = 0;
+  int nclasses = 0;
+  uint32_t eflags = 0;
+
+  // particles in sorted (leaf-contiguous) order
+  DevBuf<uint64_t> keys, keys2;
+  DevBuf<uint32_t> perm, perm2;           // sorted position -> caller's particle index
+  DevBuf<double> px, py, pz;              // sorted positions (FP64)
+  DevBuf<float> lx, ly, lz;               // sorted positions relative to their leaf centre / leaf half-width (FP32)
+  // cells, level-major, Morton order within a level
+  DevBuf<double> cx, cy, cz;
+  DevBuf<uint64_t> cid;                   // (1 << 3*level) | octant path
+  DevBuf<int> ix, iy, iz;                 // integer cell coordinates at the cell's level
+  DevBuf<int> pstart, pcount, parent, child_first;
+  DevBuf<unsigned char> child_mask, clevel;
+  DevBuf<int> leaf_cells;                 // leaf cell indices
+  DevBuf<int> cell_leaf;                  // cell -> leaf ordinal or -1
+  // interaction lists, grouped by target cell (CSR over cells)
+  DevBuf<int> m2l_off, m2l_src, m2l_cls;
+  DevBuf<int> p2p_off, p2p_src;
+  // M2L translation classes: operator vectors D^(k)(d/s_target), |k| <= order
+  DevBuf<int> cls_key4;                   // [nclasses][4]: dlev, dx, dy, dz
+  DevBuf<double> cls_D;                   // [nclasses][Nterms(order)]
+  DevBuf<float> cls_Df;
+  DevBuf<int> cls_table;                  // dense table key -> class id
+  int cls_range = 0, cls_dlmin = 0, cls_dlmax = 0;
+  // expansions (scaled: M~_n = M_n / s^|n|, L^_n = s^(|n|+1) L_n)
+  DevBuf<double> M, L;
+  DevBuf<float> Mf, Lf;
+  DevBuf<double> Fnear, Ffar;             // [N][4] sorted order
+  // scratch
+  DevBuf<int> fa, fb, fa2, fb2;           // traversal frontiers
+  DevBuf<char> tmp;                       // scan / sort / misc scratch
+  DevBuf<uint32_t> d_eflags;
+  DevBuf<double> d_root;                  // sums / maxima for the root box
+  // last evaluate() phase times (ms): P2M, M2M, M2L, P2P, L2L, L2P, finalize, total
+  float phase_ms[8] = {0};
+  float build_ms[6] = {0};                // root, keys+sort, levels, lists, classes, total
+  cudaEvent_t ev[16];
+  bool ev_ready = false;
+};
+
+int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
+                   cudaStream_t st);
+int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
+                      cudaStream_t st);
+void fmm_tree_destroy(DevTree *t);
+int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
+               int potential, int field, double *F, cudaStream_t st);

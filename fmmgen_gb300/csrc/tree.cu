@@ -1,0 +1,761 @@
+// tree.cu -- device octree build and interaction lists.
+//
+// Reproduces build_tree (example/tree.cpp:130-233) and interact_dehnen_lazy
+// (example/calculate.cpp:81-133) bit-exactly, without the sequential insertion:
+//  * build_tree's final partition does not depend on insertion order: a cell
+//    is split iff it holds >= ncrit particles, a child exists iff a particle
+//    falls in its octant, and each particle's octant path is fixed by FP64
+//    comparisons against centres that depend only on the path.  So every
+//    particle gets a 63-bit key of its 21 octant digits, computed with exactly
+//    the reference's FP64 centre arithmetic (example/tree.cpp:94-98, 193), the
+//    keys are radix-sorted, and the cells are cut level by level from the
+//    sorted keys with the count rule.
+//  * the dual-tree walk is run breadth-first over a frontier of cell pairs;
+//    each pair's decision (MAC, P2P, split A, split B) depends only on the
+//    pair, so the visited pairs -- and the M2L/P2P lists as multisets -- are
+//    those of the recursive walk.
+// All FP64 arithmetic that decides structure uses __d*_rn intrinsics so that no
+// FMA contraction changes a rounding relative to the reference source.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include "internal.h"
+#include "prims.cuh"
+#include "deriv.cuh"
+
+// ---------------------------------------------------------------------------
+// root box (example/tree.cpp:139-187)
+// ---------------------------------------------------------------------------
+// Sequential FP64 sums in particle order, one chain per axis, exactly as the
+// reference accumulates the mean; warps 1.. stream the next chunk into shared
+// memory while warp 0 adds the current one.
+#define ROOT_CHUNK 512
+__global__ void k_root_sum(const double *__restrict__ pos, long N, double *out) {
+  __shared__ double buf[2][3 * ROOT_CHUNK];
+  const int t = threadIdx.x;
+  long nchunks = (N + ROOT_CHUNK - 1) / ROOT_CHUNK;
+  double s = 0.0;
+  {
+    long n0 = N < ROOT_CHUNK ? N : ROOT_CHUNK;
+    for (long i = t; i < 3 * n0; i += blockDim.x) buf[0][i] = pos[i];
+  }
+  __syncthreads();
+  for (long k = 0; k < nchunks; k++) {
+    if (t >= 32 && k + 1 < nchunks) {
+      long b = (k + 1) * ROOT_CHUNK;
+      long n = N - b < ROOT_CHUNK ? N - b : ROOT_CHUNK;
+      for (long i = t - 32; i < 3 * n; i += blockDim.x - 32) buf[(k + 1) & 1][i] = pos[3 * b + i];
+    }
+    if (t < 3) {
+      long b = k * ROOT_CHUNK;
+      long n = N - b < ROOT_CHUNK ? N - b : ROOT_CHUNK;
+      const double *c = buf[k & 1];
+      for (long j = 0; j < n; j++) s = __dadd_rn(s, c[3 * j + t]);
+    }
+    __syncthreads();
+  }
+  if (t < 3) out[t] = s;
+}
+
+__global__ void k_root_absmax(const double *__restrict__ pos, long N, const double *sums,
+                              unsigned long long *mx) {
+  double inv_n = (double)N;
+  double ax = __ddiv_rn(sums[0], inv_n), ay = __ddiv_rn(sums[1], inv_n), az = __ddiv_rn(sums[2], inv_n);
+  double mxx = 0, mxy = 0, mxz = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    mxx = fmax(mxx, fabs(__dsub_rn(pos[3 * i], ax)));
+    mxy = fmax(mxy, fabs(__dsub_rn(pos[3 * i + 1], ay)));
+    mxz = fmax(mxz, fabs(__dsub_rn(pos[3 * i + 2], az)));
+  }
+  for (int d = 16; d; d >>= 1) {
+    mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, d));
+    mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, d));
+    mxz = fmax(mxz, __shfl_xor_sync(0xffffffffu, mxz, d));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(&mx[0], (unsigned long long)__double_as_longlong(mxx));
+    atomicMax(&mx[1], (unsigned long long)__double_as_longlong(mxy));
+    atomicMax(&mx[2], (unsigned long long)__double_as_longlong(mxz));
+  }
+}
+
+// root[0..3] = centre, r; lev[2l] = r_l, lev[2l+1] = rmax_l = sqrt(3*r_l*r_l)
+__global__ void k_root_final(const double *sums, const unsigned long long *mx, long N, double *root,
+                             double *lev) {
+  double n = (double)N;
+  double ax = __ddiv_rn(sums[0], n), ay = __ddiv_rn(sums[1], n), az = __ddiv_rn(sums[2], n);
+  double xm = __longlong_as_double((long long)mx[0]);
+  double ym = __longlong_as_double((long long)mx[1]);
+  double zm = __longlong_as_double((long long)mx[2]);
+  double r = __dmul_rn((xm > ym ? (xm > zm ? xm : zm) : (ym > zm ? ym : zm)), 1.001);
+  root[0] = ax; root[1] = ay; root[2] = az; root[3] = r;
+  double rl = r;
+  for (int l = 0; l <= FMM_MAXLEVEL; l++) {
+    lev[2 * l] = rl;
+    lev[2 * l + 1] = __dsqrt_rn(__dmul_rn(__dmul_rn(3.0, rl), rl));  // example/tree.cpp:15
+    rl = __ddiv_rn(rl, 2.0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-particle octant keys (example/tree.cpp:94-98, 189-204)
+// ---------------------------------------------------------------------------
+__global__ void k_keys(const double *__restrict__ pos, long N, const double *root, uint64_t *keys,
+                       uint32_t *idx) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+  double cx = root[0], cy = root[1], cz = root[2], r = root[3];
+  uint64_t key = 0;
+#pragma unroll 3
+  for (int l = 0; l < FMM_MAXLEVEL; l++) {
+    int oct = (x > cx) + ((y > cy) << 1) + ((z > cz) << 2);
+    key = (key << 3) | (uint64_t)oct;
+    r = __ddiv_rn(r, 2.0);
+    cx = __dadd_rn(cx, __dmul_rn(r, (double)((oct & 1) * 2 - 1)));
+    cy = __dadd_rn(cy, __dmul_rn(r, (double)((oct & 2) - 1)));
+    cz = __dadd_rn(cz, __dmul_rn(r, (double)((oct & 4) / 2 - 1)));
+  }
+  keys[i] = key;
+  idx[i] = (uint32_t)i;
+}
+
+__global__ void k_gather_pos(const double *__restrict__ pos, const uint32_t *perm, long N, double *px,
+                             double *py, double *pz) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  uint32_t j = perm[i];
+  px[i] = pos[3 * (size_t)j];
+  py[i] = pos[3 * (size_t)j + 1];
+  pz[i] = pos[3 * (size_t)j + 2];
+}
+
+// ---------------------------------------------------------------------------
+// level-by-level cell construction
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int digit_at(uint64_t key, int level /*1..21*/) {
+  return (int)((key >> (3 * (FMM_MAXLEVEL - level))) & 7u);
+}
+// first index in [lo, hi) whose level-`level` digit is >= d (digits are sorted there)
+__device__ __forceinline__ int lower_digit(const uint64_t *keys, int lo, int hi, int level, int d) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (digit_at(keys[mid], level) < d) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_init_root_cell(const double *root, long N, double *cx, double *cy, double *cz, uint64_t *cid,
+                                 int *ix, int *iy, int *iz, int *pstart, int *pcount, int *parent,
+                                 int *child_first, unsigned char *child_mask, unsigned char *clevel) {
+  cx[0] = root[0]; cy[0] = root[1]; cz[0] = root[2];
+  cid[0] = 1; ix[0] = iy[0] = iz[0] = 0;
+  pstart[0] = 0; pcount[0] = (int)N; parent[0] = -1; child_first[0] = -1; child_mask[0] = 0; clevel[0] = 0;
+}
+
+__global__ void k_count_children(int lo, int hi, int level, long ncrit, const uint64_t *keys, const int *pstart,
+                                 const int *pcount, unsigned char *child_mask, uint32_t *cnt,
+                                 uint32_t *eflags) {
+  int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= hi) return;
+  uint32_t n = 0;
+  unsigned mask = 0;
+  if (pcount[c] >= ncrit) {
+    if (level >= FMM_MAXLEVEL) {
+      atomicOr(eflags, FMM_EFLAG_DEPTH);
+    } else {
+      int s = pstart[c], e = s + pcount[c];
+      int b = s;
+      for (int o = 0; o < 8; o++) {
+        int nb = lower_digit(keys, b, e, level + 1, o + 1);
+        if (nb > b) mask |= 1u << o;
+        b = nb;
+      }
+      n = __popc(mask);
+    }
+  }
+  child_mask[c] = (unsigned char)mask;
+  cnt[c - lo] = n;
+}
+
+__global__ void k_write_children(int lo, int hi, int level, const double *lev, const uint64_t *keys,
+                                 const uint32_t *off, double *cx, double *cy, double *cz, uint64_t *cid,
+                                 int *ix, int *iy, int *iz, int *pstart, int *pcount, int *parent,
+                                 int *child_first, const unsigned char *child_mask_in,
+                                 unsigned char *child_mask, unsigned char *clevel) {
+  int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= hi) return;
+  unsigned mask = child_mask_in[c];
+  if (!mask) { child_first[c] = -1; return; }
+  int first = hi + (int)off[c - lo];
+  child_first[c] = first;
+  double r = lev[2 * (level + 1)];  // child half-width = parent r / 2.0
+  double px = cx[c], py = cy[c], pz = cz[c];
+  int s = pstart[c], e = s + pcount[c];
+  int b = s, j = first;
+  for (int o = 0; o < 8; o++) {
+    int nb = lower_digit(keys, b, e, level + 1, o + 1);
+    if (nb > b) {
+      // add_child (example/tree.cpp:95-98)
+      cx[j] = __dadd_rn(px, __dmul_rn(r, (double)((o & 1) * 2 - 1)));
+      cy[j] = __dadd_rn(py, __dmul_rn(r, (double)((o & 2) - 1)));
+      cz[j] = __dadd_rn(pz, __dmul_rn(r, (double)((o & 4) / 2 - 1)));
+      cid[j] = (cid[c] << 3) | (uint64_t)o;
+      ix[j] = 2 * ix[c] + (o & 1);
+      iy[j] = 2 * iy[c] + ((o >> 1) & 1);
+      iz[j] = 2 * iz[c] + (o >> 2);
+      pstart[j] = b;
+      pcount[j] = nb - b;
+      parent[j] = c;
+      child_first[j] = -1;
+      child_mask[j] = 0;
+      clevel[j] = (unsigned char)(level + 1);
+      j++;
+    }
+    b = nb;
+  }
+}
+
+__global__ void k_leaf_flags(int ncells, long ncrit, const int *pcount, uint32_t *flag) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncells) flag[c] = pcount[c] < ncrit ? 1u : 0u;
+}
+__global__ void k_leaf_compact(int ncells, long ncrit, const int *pcount, const uint32_t *off, int *leaf_cells,
+                               int *cell_leaf) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  if (pcount[c] < ncrit) { leaf_cells[off[c]] = c; cell_leaf[c] = (int)off[c]; }
+  else cell_leaf[c] = -1;
+}
+
+// ---------------------------------------------------------------------------
+// dual-tree walk (example/calculate.cpp:81-133), breadth-first
+// ---------------------------------------------------------------------------
+struct WalkCells {
+  const double *cx, *cy, *cz, *lev;
+  const unsigned char *mask, *clevel;
+  const int *child_first;
+};
+
+// 0 = M2L, 1 = P2P, 2 = split A, 3 = split B
+__device__ __forceinline__ int walk_decide(const WalkCells &W, int A, int B, double theta) {
+  double dx = __dsub_rn(W.cx[A], W.cx[B]);
+  double dy = __dsub_rn(W.cy[A], W.cy[B]);
+  double dz = __dsub_rn(W.cz[A], W.cz[B]);
+  double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+  double ra = W.lev[2 * W.clevel[A] + 1], rb = W.lev[2 * W.clevel[B] + 1];
+  if (__dmul_rn(R, theta) > __dadd_rn(ra, rb)) return 0;
+  bool la = W.mask[A] == 0, lb = W.mask[B] == 0;
+  if (la && lb) return 1;  // the nleaf >= ncrit leaf-leaf branch is unreachable
+  if (lb || (ra >= rb && !la)) return 2;
+  return 3;
+}
+
+__global__ void k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, U3 *cnt) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  int A = fa[i], B = fb[i];
+  int d = walk_decide(W, A, B, theta);
+  U3 c{0u, 0u, 0u};
+  if (d == 0) c.x = 1;
+  else if (d == 1) c.y = 1;
+  else if (d == 2) c.z = __popc((unsigned)W.mask[A]);
+  else c.z = __popc((unsigned)W.mask[B]);
+  cnt[i] = c;
+}
+
+__global__ void k_walk_write(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, const U3 *off,
+                             U3 base, int *m2l_src, int *m2l_tgt, int *p2p_tgt, int *p2p_src, int *na,
+                             int *nb) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  int A = fa[i], B = fb[i];
+  int d = walk_decide(W, A, B, theta);
+  U3 o = off[i];
+  if (d == 0) {
+    m2l_src[base.x + o.x] = B;
+    m2l_tgt[base.x + o.x] = A;
+  } else if (d == 1) {
+    p2p_tgt[base.y + o.y] = A;
+    p2p_src[base.y + o.y] = B;
+  } else {
+    int P = d == 2 ? A : B;
+    unsigned m = W.mask[P];
+    int ch = W.child_first[P];
+    uint32_t k = o.z;
+    for (int oc = 0; oc < 8; oc++) {
+      if (!(m & (1u << oc))) continue;
+      if (d == 2) { na[k] = ch; nb[k] = B; }
+      else { na[k] = A; nb[k] = ch; }
+      ch++; k++;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// grouping pairs by target cell
+// ---------------------------------------------------------------------------
+__global__ void k_pair_keys(const int *tgt, long n, uint64_t *keys, uint32_t *idx) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keys[i] = (uint64_t)(uint32_t)tgt[i];
+  idx[i] = (uint32_t)i;
+}
+__global__ void k_pair_gather(const uint32_t *idx, const int *src_in, long n, int *src_out) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) src_out[i] = src_in[idx[i]];
+}
+__global__ void k_target_count(const int *tgt, long n, int *cnt) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&cnt[tgt[i]], 1);
+}
+
+// ---------------------------------------------------------------------------
+// M2L translation classes
+// ---------------------------------------------------------------------------
+// A pair (B -> A) with levels lA, lB is, up to the scale of A, fixed by
+// (dlev = lB - lA, integer offset of the centres in half-widths of the finer
+// level).  Classes are shared across levels.
+__device__ __forceinline__ void pair_class(const int *ix, const int *iy, const int *iz, const unsigned char *clevel,
+                                           int A, int B, int &dl, int &dx, int &dy, int &dz) {
+  int la = clevel[A], lb = clevel[B];
+  int L = la > lb ? la : lb;
+  int sa = L - la, sb = L - lb;
+  dl = lb - la;
+  dx = ((2 * ix[A] + 1) << sa) - ((2 * ix[B] + 1) << sb);
+  dy = ((2 * iy[A] + 1) << sa) - ((2 * iy[B] + 1) << sb);
+  dz = ((2 * iz[A] + 1) << sa) - ((2 * iz[B] + 1) << sb);
+}
+
+__global__ void k_class_range(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
+                              const unsigned char *clevel, int *rng /*[3]: max|d|, max dl, max -dl*/) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int m = 0, dlp = 0, dlm = 0;
+  if (i < n) {
+    int dl, dx, dy, dz;
+    pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
+    m = max(abs(dx), max(abs(dy), abs(dz)));
+    dlp = max(dl, 0);
+    dlm = max(-dl, 0);
+  }
+  for (int d = 16; d; d >>= 1) {
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, d));
+    dlp = max(dlp, __shfl_xor_sync(0xffffffffu, dlp, d));
+    dlm = max(dlm, __shfl_xor_sync(0xffffffffu, dlm, d));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&rng[0], m);
+    atomicMax(&rng[1], dlp);
+    atomicMax(&rng[2], dlm);
+  }
+}
+
+__device__ __forceinline__ long class_slot(int dl, int dx, int dy, int dz, int R, int dlmin) {
+  long w = 2 * R + 1;
+  return ((((long)(dl - dlmin) * w + (dx + R)) * w + (dy + R)) * w + (dz + R));
+}
+
+__global__ void k_class_mark(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
+                             const unsigned char *clevel, int R, int dlmin, uint32_t *mark) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int dl, dx, dy, dz;
+  pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
+  long s = class_slot(dl, dx, dy, dz, R, dlmin);
+  if (mark[s] == 0) mark[s] = 1;
+}
+
+__global__ void k_class_list(const uint32_t *mark, const uint32_t *id, long nslots, int R, int dlmin,
+                             int *table, int *key4) {
+  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= nslots) return;
+  if (!mark[s]) { table[s] = -1; return; }
+  int c = (int)id[s];
+  table[s] = c;
+  long w = 2 * R + 1;
+  long t = s;
+  int dz = (int)(t % w) - R; t /= w;
+  int dy = (int)(t % w) - R; t /= w;
+  int dx = (int)(t % w) - R; t /= w;
+  int dl = (int)t + dlmin;
+  key4[4 * c] = dl; key4[4 * c + 1] = dx; key4[4 * c + 2] = dy; key4[4 * c + 3] = dz;
+}
+
+__global__ void k_class_assign(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
+                               const unsigned char *clevel, int R, int dlmin, const int *table, int *cls) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int dl, dx, dy, dz;
+  pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
+  cls[i] = table[class_slot(dl, dx, dy, dz, R, dlmin)];
+}
+
+// Operator vector of a class: D_k(d / s_A), |k| <= p, in FP64 (one warp per class).
+__global__ void k_class_derivs(const int *key4, int ncls, int p, double *D64, float *D32) {
+  __shared__ double sD[FMM_WARPS][FMM_NTMAX], sT[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_PMAX + 1];
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int c = blockIdx.x * FMM_WARPS + w;
+  if (c >= ncls) return;
+  int dl = key4[4 * c];
+  double sc = dl > 0 ? ldexp(1.0, -dl) : 1.0;  // finer-level half-widths -> half-widths of A
+  double x = key4[4 * c + 1] * sc, y = key4[4 * c + 2] * sc, z = key4[4 * c + 3] * sc;
+  warp_derivs<double>(x, y, z, p, sD[w], sT[w], sB[w]);
+  int nt = fmm_nterms(p);
+  for (int i = lane; i < nt; i += 32) {
+    D64[(size_t)c * nt + i] = sD[w][i];
+    D32[(size_t)c * nt + i] = (float)sD[w][i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+template <typename T> static int grow_keep(DevBuf<T> &b, size_t need, size_t used, cudaStream_t st) {
+  if (need <= b.cap && b.p) return FMM_OK;
+  size_t want = need + need / 2 + 64;
+  T *p = nullptr;
+  FMM_CUDA_TRY(cudaMalloc((void **)&p, want * sizeof(T)));
+  if (b.p && used) FMM_CUDA_TRY(cudaMemcpyAsync(p, b.p, used * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  if (b.p) {
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(b.p);
+  }
+  b.p = p;
+  b.cap = want;
+  return FMM_OK;
+}
+
+static int tmp_reserve(DevTree *t, size_t bytes) { return fmm_reserve(t->tmp, bytes); }
+
+#define TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
+
+static int rec(DevTree *t, int i, cudaStream_t st) {
+  if (!t->ev_ready) return FMM_OK;
+  FMM_CUDA_TRY(cudaEventRecord(t->ev[i], st));
+  return FMM_OK;
+}
+
+static int build_cells(DevTree *t, cudaStream_t st);
+static int build_lists(DevTree *t, cudaStream_t st);
+static int build_classes(DevTree *t, cudaStream_t st);
+
+int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
+                   cudaStream_t st) {
+  if (N < 1 || N >= (1L << 31) - 1 || ncrit < 1 || order < so + 1 || order > FMM_PMAX || so < 0 || so > 1 ||
+      !(theta > 0) || !pos)
+    return FMM_ERR_ARG;
+  t->N = N; t->ncrit = ncrit; t->order = order; t->so = so; t->theta = theta;
+  FMM_CUDA_TRY(cudaGetDevice(&t->dev));
+  if (!t->ev_ready) {
+    for (int i = 0; i < 16; i++) FMM_CUDA_TRY(cudaEventCreate(&t->ev[i]));
+    t->ev_ready = true;
+  }
+  TRY(rec(t, 0, st));
+  TRY(fmm_reserve(t->d_eflags, 4));
+  FMM_CUDA_TRY(cudaMemsetAsync(t->d_eflags.p, 0, sizeof(uint32_t), st));
+  // d_root: [0..2] sums, [3..5] maxima (u64 bits), [6..9] root box, [10..] level r/rmax
+  TRY(fmm_reserve(t->d_root, 16 + 2 * (FMM_MAXLEVEL + 1)));
+  double *dr = t->d_root.p;
+  FMM_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * 16, st));
+  k_root_sum<<<1, 256, 0, st>>>(pos, N, dr);
+  unsigned nbm = std::min<unsigned>(fmm_blocks(N, 256), 152 * 8);
+  k_root_absmax<<<nbm, 256, 0, st>>>(pos, N, dr, (unsigned long long *)(dr + 3));
+  k_root_final<<<1, 1, 0, st>>>(dr, (const unsigned long long *)(dr + 3), N, dr + 6, dr + 16);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 1, st));
+
+  // keys + stable sort
+  TRY(fmm_reserve(t->keys, N)); TRY(fmm_reserve(t->keys2, N));
+  TRY(fmm_reserve(t->perm, N)); TRY(fmm_reserve(t->perm2, N));
+  k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, dr + 6, t->keys.p, t->perm.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  size_t nbh = fmm_rs_nblocks(N);
+  size_t hist_n = 256 * nbh;
+  size_t tmp_bytes = hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 1024;
+  TRY(tmp_reserve(t, tmp_bytes));
+  uint32_t *hist = (uint32_t *)t->tmp.p;
+  uint32_t *scantmp = hist + hist_n;
+  TRY(fmm_radix_sort(t->keys.p, t->perm.p, t->keys2.p, t->perm2.p, N, 0, 3 * FMM_MAXLEVEL, hist, scantmp, st));
+  TRY(fmm_reserve(t->px, N)); TRY(fmm_reserve(t->py, N)); TRY(fmm_reserve(t->pz, N));
+  k_gather_pos<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, t->perm.p, N, t->px.p, t->py.p, t->pz.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  FMM_CUDA_TRY(cudaMemcpyAsync(&t->root, dr + 6, sizeof(RootBox), cudaMemcpyDeviceToHost, st));
+  TRY(rec(t, 2, st));
+
+  TRY(build_cells(t, st));
+  TRY(rec(t, 3, st));
+  TRY(build_lists(t, st));
+  TRY(rec(t, 4, st));
+  TRY(build_classes(t, st));
+  TRY(rec(t, 5, st));
+  FMM_CUDA_TRY(cudaMemcpyAsync(&t->eflags, t->d_eflags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  if (t->ev_ready) {
+    float ms;
+    for (int i = 0; i < 5; i++) {
+      cudaEventElapsedTime(&ms, t->ev[i], t->ev[i + 1]);
+      t->build_ms[i] = ms;
+    }
+    cudaEventElapsedTime(&ms, t->ev[0], t->ev[5]);
+    t->build_ms[5] = ms;
+  }
+  if (t->eflags & FMM_EFLAG_DEPTH) return FMM_ERR_DEPTH;
+  if (t->eflags & FMM_EFLAG_RANGE) return FMM_ERR_RANGE;
+  return FMM_OK;
+}
+
+static int build_cells(DevTree *t, cudaStream_t st) {
+  long N = t->N;
+  size_t cap = (size_t)(4 * N / std::max<long>(t->ncrit, 1)) + 1024;
+  TRY(fmm_reserve(t->cx, cap)); TRY(fmm_reserve(t->cy, cap)); TRY(fmm_reserve(t->cz, cap));
+  TRY(fmm_reserve(t->cid, cap)); TRY(fmm_reserve(t->ix, cap)); TRY(fmm_reserve(t->iy, cap));
+  TRY(fmm_reserve(t->iz, cap)); TRY(fmm_reserve(t->pstart, cap)); TRY(fmm_reserve(t->pcount, cap));
+  TRY(fmm_reserve(t->parent, cap)); TRY(fmm_reserve(t->child_first, cap));
+  TRY(fmm_reserve(t->child_mask, cap)); TRY(fmm_reserve(t->clevel, cap));
+  double *dr = t->d_root.p;
+  k_init_root_cell<<<1, 1, 0, st>>>(dr + 6, N, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
+                                    t->pstart.p, t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p,
+                                    t->clevel.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  t->level_off.assign(1, 0);
+  t->level_off.push_back(1);
+  int lo = 0, hi = 1, level = 0;
+  uint32_t *h_total = nullptr;
+  FMM_CUDA_TRY(cudaMallocHost((void **)&h_total, sizeof(uint32_t)));
+  int rc = FMM_OK;
+  while (true) {
+    int n = hi - lo;
+    size_t need = (size_t)n * 4 + fmm_scan_tmp_elems<uint32_t>(n) * 4 + 64;
+    if ((rc = tmp_reserve(t, need))) break;
+    uint32_t *cnt = (uint32_t *)t->tmp.p;
+    uint32_t *total = cnt + n;
+    uint32_t *stmp = total + 1;
+    k_count_children<<<fmm_blocks(n, 128), 128, 0, st>>>(lo, hi, level, t->ncrit, t->keys.p, t->pstart.p,
+                                                         t->pcount.p, t->child_mask.p, cnt, t->d_eflags.p);
+    if ((rc = fmm_scan<uint32_t>(cnt, cnt, n, total, stmp, st))) break;
+    cudaMemcpyAsync(h_total, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
+    uint32_t nnew = *h_total;
+    if (nnew == 0) break;
+    size_t need_cells = (size_t)hi + nnew;
+    size_t used = hi;
+    if ((rc = grow_keep(t->cx, need_cells, used, st)) || (rc = grow_keep(t->cy, need_cells, used, st)) ||
+        (rc = grow_keep(t->cz, need_cells, used, st)) || (rc = grow_keep(t->cid, need_cells, used, st)) ||
+        (rc = grow_keep(t->ix, need_cells, used, st)) || (rc = grow_keep(t->iy, need_cells, used, st)) ||
+        (rc = grow_keep(t->iz, need_cells, used, st)) || (rc = grow_keep(t->pstart, need_cells, used, st)) ||
+        (rc = grow_keep(t->pcount, need_cells, used, st)) || (rc = grow_keep(t->parent, need_cells, used, st)) ||
+        (rc = grow_keep(t->child_first, need_cells, used, st)) ||
+        (rc = grow_keep(t->child_mask, need_cells, used, st)) || (rc = grow_keep(t->clevel, need_cells, used, st)))
+      break;
+    k_write_children<<<fmm_blocks(n, 128), 128, 0, st>>>(
+        lo, hi, level, dr + 16, t->keys.p, cnt, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
+        t->pstart.p, t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p, t->child_mask.p, t->clevel.p);
+    if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
+    lo = hi;
+    hi = hi + (int)nnew;
+    level++;
+    t->level_off.push_back(hi);
+  }
+  cudaFreeHost(h_total);
+  if (rc) return rc;
+  t->ncells = hi;
+  t->nlevels = level + 1;
+  // leaves
+  int nc = t->ncells;
+  TRY(fmm_reserve(t->leaf_cells, nc));
+  TRY(fmm_reserve(t->cell_leaf, nc));
+  TRY(tmp_reserve(t, (size_t)nc * 4 + fmm_scan_tmp_elems<uint32_t>(nc) * 4 + 64));
+  uint32_t *flag = (uint32_t *)t->tmp.p;
+  uint32_t *total = flag + nc;
+  uint32_t *stmp = total + 1;
+  k_leaf_flags<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag);
+  TRY(fmm_scan<uint32_t>(flag, flag, nc, total, stmp, st));
+  k_leaf_compact<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag, t->leaf_cells.p,
+                                                      t->cell_leaf.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  uint32_t nl = 0;
+  FMM_CUDA_TRY(cudaMemcpyAsync(&nl, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  t->nleaves = (int)nl;
+  return FMM_OK;
+}
+
+// Sort (tgt, src) pairs by target, stably, and build the CSR offsets.
+static int group_by_target(DevTree *t, int *tgt, int *src, long n, DevBuf<int> &off, DevBuf<int> &src_out,
+                           cudaStream_t st) {
+  int nc = t->ncells;
+  TRY(fmm_reserve(off, (size_t)nc + 1));
+  TRY(fmm_reserve(src_out, n > 0 ? n : 1));
+  if (n == 0) {
+    FMM_CUDA_TRY(cudaMemsetAsync(off.p, 0, sizeof(int) * (nc + 1), st));
+    return FMM_OK;
+  }
+  int bits = 1;
+  while ((1L << bits) < nc) bits++;
+  int end_bit = ((bits + 7) / 8) * 8;
+  size_t nbh = fmm_rs_nblocks(n);
+  size_t hist_n = 256 * nbh;
+  size_t bytes = (size_t)n * (8 + 4 + 8 + 4) + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 +
+                 ((size_t)nc + 1) * 4 + fmm_scan_tmp_elems<int>(nc + 1) * 4 + 256;
+  TRY(tmp_reserve(t, bytes));
+  char *p = t->tmp.p;
+  uint64_t *k1 = (uint64_t *)p; p += (size_t)n * 8;
+  uint64_t *k2 = (uint64_t *)p; p += (size_t)n * 8;
+  uint32_t *v1 = (uint32_t *)p; p += (size_t)n * 4;
+  uint32_t *v2 = (uint32_t *)p; p += (size_t)n * 4;
+  uint32_t *hist = (uint32_t *)p; p += hist_n * 4;
+  uint32_t *stmp = (uint32_t *)p; p += fmm_scan_tmp_elems<uint32_t>(hist_n) * 4;
+  int *cnt = (int *)p; p += ((size_t)nc + 1) * 4;
+  int *stmp2 = (int *)p;
+  k_pair_keys<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, k1, v1);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(fmm_radix_sort(k1, v1, k2, v2, n, 0, end_bit, hist, stmp, st));
+  k_pair_gather<<<fmm_blocks(n, 256), 256, 0, st>>>(v1, src, n, src_out.p);
+  // the sorted tgt order is implied by the offsets
+  FMM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nc + 1), st));
+  k_target_count<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, cnt);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(fmm_scan<int>(cnt, off.p, nc + 1, nullptr, stmp2, st));
+  return FMM_OK;
+}
+
+static int build_lists(DevTree *t, cudaStream_t st) {
+  int nc = t->ncells;
+  WalkCells W{t->cx.p, t->cy.p, t->cz.p, t->d_root.p + 16, t->child_mask.p, t->clevel.p, t->child_first.p};
+  // raw (ungrouped) lists live in the frontier buffers' companions
+  DevBuf<int> m2l_src_raw, m2l_tgt_raw, p2p_tgt_raw, p2p_src_raw;
+  size_t cap_pairs = (size_t)nc * 64 + 1024;
+  TRY(fmm_reserve(t->fa, cap_pairs)); TRY(fmm_reserve(t->fb, cap_pairs));
+  TRY(fmm_reserve(t->fa2, cap_pairs)); TRY(fmm_reserve(t->fb2, cap_pairs));
+  int rc = FMM_OK;
+  long nm2l = 0, np2p = 0;
+  uint32_t nf = 1;
+  U3 *h_tot = nullptr;
+  cudaMallocHost((void **)&h_tot, sizeof(U3));
+  int zero = 0;
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->fa.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->fb.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+  if ((rc = fmm_reserve(m2l_src_raw, cap_pairs)) || (rc = fmm_reserve(m2l_tgt_raw, cap_pairs)) ||
+      (rc = fmm_reserve(p2p_tgt_raw, cap_pairs)) || (rc = fmm_reserve(p2p_src_raw, cap_pairs))) {
+    cudaFreeHost(h_tot);
+    return rc;
+  }
+  while (nf > 0) {
+    size_t need = (size_t)nf * sizeof(U3) + fmm_scan_tmp_elems<U3>(nf) * sizeof(U3) + 2 * sizeof(U3);
+    if ((rc = tmp_reserve(t, need))) break;
+    U3 *cnt = (U3 *)t->tmp.p;
+    U3 *tot = cnt + nf;
+    U3 *stmp = tot + 1;
+    k_walk_count<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt);
+    if ((rc = fmm_scan<U3>(cnt, cnt, nf, tot, stmp, st))) break;
+    cudaMemcpyAsync(h_tot, tot, sizeof(U3), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
+    U3 T = *h_tot;
+    if ((rc = grow_keep(m2l_src_raw, nm2l + T.x, nm2l, st)) || (rc = grow_keep(m2l_tgt_raw, nm2l + T.x, nm2l, st)) ||
+        (rc = grow_keep(p2p_tgt_raw, np2p + T.y, np2p, st)) || (rc = grow_keep(p2p_src_raw, np2p + T.y, np2p, st)) ||
+        (rc = fmm_reserve(t->fa2, T.z + 1)) || (rc = fmm_reserve(t->fb2, T.z + 1)))
+      break;
+    U3 base{(uint32_t)nm2l, (uint32_t)np2p, 0u};
+    k_walk_write<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt, base,
+                                                     m2l_src_raw.p, m2l_tgt_raw.p, p2p_tgt_raw.p, p2p_src_raw.p,
+                                                     t->fa2.p, t->fb2.p);
+    if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
+    nm2l += T.x;
+    np2p += T.y;
+    nf = T.z;
+    std::swap(t->fa, t->fa2);
+    std::swap(t->fb, t->fb2);
+  }
+  cudaFreeHost(h_tot);
+  if (!rc) {
+    t->nm2l = nm2l;
+    t->np2p = np2p;
+    rc = group_by_target(t, m2l_tgt_raw.p, m2l_src_raw.p, nm2l, t->m2l_off, t->m2l_src, st);
+    if (!rc) rc = group_by_target(t, p2p_tgt_raw.p, p2p_src_raw.p, np2p, t->p2p_off, t->p2p_src, st);
+  }
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  fmm_release(m2l_src_raw); fmm_release(m2l_tgt_raw); fmm_release(p2p_tgt_raw); fmm_release(p2p_src_raw);
+  return rc;
+}
+
+__global__ void k_expand_targets(const int *off, int nc, int *tgt) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int k = off[c]; k < off[c + 1]; k++) tgt[k] = c;
+}
+
+static int build_classes(DevTree *t, cudaStream_t st) {
+  long n = t->nm2l;
+  int nc = t->ncells;
+  int p = t->order;
+  TRY(fmm_reserve(t->m2l_cls, n > 0 ? n : 1));
+  if (n == 0) { t->nclasses = 0; return FMM_OK; }
+  TRY(fmm_reserve(t->fa, n));
+  k_expand_targets<<<fmm_blocks(nc, 128), 128, 0, st>>>(t->m2l_off.p, nc, t->fa.p);
+  const int *tgt = t->fa.p, *src = t->m2l_src.p;
+  TRY(tmp_reserve(t, 64));
+  int *rng = (int *)t->tmp.p;
+  FMM_CUDA_TRY(cudaMemsetAsync(rng, 0, 3 * sizeof(int), st));
+  k_class_range<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, rng);
+  FMM_CUDA_TRY(cudaGetLastError());
+  int h[3];
+  FMM_CUDA_TRY(cudaMemcpyAsync(h, rng, sizeof(h), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  int R = h[0], dlmin = -h[2], dlmax = h[1];
+  long w = 2L * R + 1;
+  long nslots = (long)(dlmax - dlmin + 1) * w * w * w;
+  if (nslots > (1L << 28)) {
+    fmm_set_error_text("M2L offsets span a range too wide for the class table");
+    return FMM_ERR_RANGE;
+  }
+  t->cls_range = R; t->cls_dlmin = dlmin; t->cls_dlmax = dlmax;
+  TRY(fmm_reserve(t->cls_table, nslots));
+  size_t bytes = (size_t)nslots * 8 + fmm_scan_tmp_elems<uint32_t>(nslots) * 4 + 64;
+  TRY(tmp_reserve(t, bytes));
+  uint32_t *mark = (uint32_t *)t->tmp.p;
+  uint32_t *id = mark + nslots;
+  uint32_t *total = id + nslots;
+  uint32_t *stmp = total + 1;
+  FMM_CUDA_TRY(cudaMemsetAsync(mark, 0, sizeof(uint32_t) * nslots, st));
+  k_class_mark<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R, dlmin,
+                                                   mark);
+  TRY(fmm_scan<uint32_t>(mark, id, nslots, total, stmp, st));
+  uint32_t ncls = 0;
+  FMM_CUDA_TRY(cudaMemcpyAsync(&ncls, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  t->nclasses = (int)ncls;
+  TRY(fmm_reserve(t->cls_key4, 4 * (size_t)ncls));
+  k_class_list<<<fmm_blocks(nslots, 256), 256, 0, st>>>(mark, id, nslots, R, dlmin, t->cls_table.p, t->cls_key4.p);
+  k_class_assign<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R,
+                                                     dlmin, t->cls_table.p, t->m2l_cls.p);
+  int nt = fmm_nterms(p);
+  TRY(fmm_reserve(t->cls_D, (size_t)ncls * nt));
+  TRY(fmm_reserve(t->cls_Df, (size_t)ncls * nt));
+  k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
+                                                                         t->cls_Df.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  return FMM_OK;
+}
+
+void fmm_tree_destroy(DevTree *t) {
+  if (!t) return;
+  fmm_release(t->keys); fmm_release(t->keys2); fmm_release(t->perm); fmm_release(t->perm2);
+  fmm_release(t->px); fmm_release(t->py); fmm_release(t->pz);
+  fmm_release(t->lx); fmm_release(t->ly); fmm_release(t->lz);
+  fmm_release(t->cx); fmm_release(t->cy); fmm_release(t->cz); fmm_release(t->cid);
+  fmm_release(t->ix); fmm_release(t->iy); fmm_release(t->iz);
+  fmm_release(t->pstart); fmm_release(t->pcount); fmm_release(t->parent); fmm_release(t->child_first);
+  fmm_release(t->child_mask); fmm_release(t->clevel); fmm_release(t->leaf_cells); fmm_release(t->cell_leaf);
+  fmm_release(t->m2l_off); fmm_release(t->m2l_src); fmm_release(t->m2l_cls);
+  fmm_release(t->p2p_off); fmm_release(t->p2p_src);
+  fmm_release(t->cls_key4); fmm_release(t->cls_D); fmm_release(t->cls_Df); fmm_release(t->cls_table);
+  fmm_release(t->M); fmm_release(t->L); fmm_release(t->Mf); fmm_release(t->Lf);
+  fmm_release(t->Fnear); fmm_release(t->Ffar);
+  fmm_release(t->fa); fmm_release(t->fb); fmm_release(t->fa2); fmm_release(t->fb2);
+  fmm_release(t->tmp); fmm_release(t->d_eflags); fmm_release(t->d_root);
+  if (t->ev_ready)
+    for (int i = 0; i < 16; i++) cudaEventDestroy(t->ev[i]);
+  t->ev_ready = false;
+}

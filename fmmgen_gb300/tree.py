@@ -1,0 +1,177 @@
+"""Host-side mirror of the reference example's tree API (example/tree.hpp:78-103).
+
+    tree = build_tree(pos, S, N, ncrit, order, theta, source_order=0)
+    tree.compute_field_fmm(F)      # Tree::compute_field_fmm (example/tree.cpp:243-271)
+    tree.compute_field_exact(F)    # Tree::compute_field_exact (example/tree.cpp:295-297)
+
+pos is [N][3], S is [N][SOURCESIZE] and F is [N][OUTPUTSIZE], FP64, in the
+caller's particle order, as in the reference.  Device tensors (torch, cuda,
+float64) are used in place; host arrays (numpy or CPU tensors) are copied to the
+device and F is copied back.  All work runs in libfmmgen_gb300.so on the GPU:
+torch supplies device memory and the stream.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+
+PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+
+
+def _stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _as_device(a, shape_tail):
+    if isinstance(a, torch.Tensor) and a.is_cuda:
+        t = a
+    else:
+        t = torch.as_tensor(np.asarray(a) if not isinstance(a, torch.Tensor) else a)
+        t = t.to(device="cuda")
+    t = t.to(torch.float64).reshape(-1, *shape_tail).contiguous()
+    return t
+
+
+def sourcesize(source_order):
+    return 1 if source_order == 0 else 3
+
+
+def outputsize(potential=True, field=True):
+    return (1 if potential else 0) + (3 if field else 0)
+
+
+class Tree:
+    """Device octree + interaction lists for fixed particle positions."""
+
+    def __init__(self, pos, S, ncrit, order, theta, source_order=0, stream=None):
+        if source_order not in (0, 1):
+            raise ValueError("source_order must be 0 (charges) or 1 (dipoles)")
+        self.pos = _as_device(pos, (3,))
+        self.N = self.pos.shape[0]
+        self.S = _as_device(S, (sourcesize(source_order),)) if S is not None else None
+        if self.S is not None and self.S.shape[0] != self.N:
+            raise ValueError("S must hold one source per particle")
+        self.ncrit, self.order, self.theta, self.source_order = int(ncrit), int(order), float(theta), source_order
+        self._h = C.c_void_p(None)
+        self.rebuild(stream=stream)
+
+    def rebuild(self, pos=None, stream=None):
+        """Rebuild for new positions, reusing the handle's device buffers."""
+        if pos is not None:
+            self.pos = _as_device(pos, (3,))
+            self.N = self.pos.shape[0]
+        check(lib().fmmgen_tree_build(C.c_void_p(self.pos.data_ptr()), self.N, self.ncrit, self.order, self.theta,
+                                      self.source_order, _stream_ptr(stream), C.byref(self._h)))
+        info = np.zeros(8, dtype=np.int64)
+        check(lib().fmmgen_tree_info(self._h, info.ctypes.data))
+        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _) = (int(v) for v in info)
+        return self
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fmmgen_tree_free(h)
+            except Exception:
+                pass
+            self._h = C.c_void_p(None)
+
+    # -- evaluation ---------------------------------------------------------
+    def compute_field_fmm(self, F=None, S=None, potential=True, field=True, precision="fp64", stream=None):
+        """Fill F with phi/E of the FMM; returns F (device tensor unless F is a host array)."""
+        if S is not None:
+            self.S = _as_device(S, (sourcesize(self.source_order),))
+        if self.S is None:
+            raise ValueError("no sources")
+        os_ = outputsize(potential, field)
+        host_out = F is not None and not (isinstance(F, torch.Tensor) and F.is_cuda)
+        Fd = F if (F is not None and not host_out) else torch.empty((self.N, os_), dtype=torch.float64,
+                                                                     device=self.pos.device)
+        if Fd.dtype != torch.float64 or not Fd.is_contiguous() or Fd.numel() != self.N * os_:
+            raise ValueError("F must be a contiguous float64 [N][OUTPUTSIZE] array")
+        check(lib().fmmgen_tree_compute_field_fmm(self._h, C.c_void_p(self.S.data_ptr()), C.c_void_p(Fd.data_ptr()),
+                                                  int(potential), int(field), PRECISIONS[precision],
+                                                  _stream_ptr(stream)))
+        if host_out:
+            F[...] = Fd.reshape(np.shape(F)).cpu().numpy() if isinstance(F, np.ndarray) else Fd.cpu()
+            return F
+        return Fd
+
+    def compute_field_exact(self, F=None, targets=None, potential=True, field=True, stream=None):
+        return direct(self.pos, self.S, targets=targets, source_order=self.source_order, potential=potential,
+                      field=field, F=F, stream=stream)
+
+    # -- introspection (host arrays) ------------------------------------------
+    def root(self):
+        r = np.zeros(4)
+        check(lib().fmmgen_tree_root(self._h, r.ctypes.data))
+        return r
+
+    def cells(self):
+        nc, nl = self.ncells, self.nleaves
+        cid = np.zeros(nc, np.uint64)
+        cnt = np.zeros(nc, np.int64)
+        cen = np.zeros((nc, 3))
+        loff = np.zeros(nl + 1, np.int64)
+        lidx = np.zeros(self.N, np.int64)
+        check(lib().fmmgen_tree_export_cells(self._h, cid.ctypes.data, cnt.ctypes.data, cen.ctypes.data,
+                                             loff.ctypes.data, lidx.ctypes.data))
+        return dict(id=cid, count=cnt, centre=cen, leaf_off=loff, leaf_idx=lidx)
+
+    def lists(self):
+        m2l = np.zeros((max(self.nm2l, 1), 2), np.uint64)
+        p2p = np.zeros((max(self.np2p, 1), 2), np.uint64)
+        check(lib().fmmgen_tree_export_lists(self._h, m2l.ctypes.data, p2p.ctypes.data))
+        return m2l[: self.nm2l], p2p[: self.np2p]
+
+    def expansions(self):
+        ms = int(lib().fmmgen_msize(self.order, self.source_order))
+        ls = int(lib().fmmgen_lsize(self.order, self.source_order))
+        M = np.zeros((self.ncells, ms))
+        L = np.zeros((self.ncells, ls))
+        check(lib().fmmgen_tree_export_expansions(self._h, M.ctypes.data, L.ctypes.data))
+        return M, L
+
+    def times(self):
+        b = np.zeros(6, np.float32)
+        e = np.zeros(8, np.float32)
+        check(lib().fmmgen_tree_times(self._h, b.ctypes.data, e.ctypes.data))
+        return (dict(zip(["root", "keys_sort", "cells", "lists", "classes", "total"], b.tolist())),
+                dict(zip(["P2M", "M2M", "M2L", "P2P", "L2L", "L2P", "finalize", "total"], e.tolist())))
+
+
+def build_tree(pos, S, N=None, ncrit=64, order=4, theta=0.5, source_order=0, stream=None):
+    """build_tree(pos, S, N, ncrit, order, theta) of example/tree.cpp:130-233."""
+    pos_t = _as_device(pos, (3,))
+    if N is not None and int(N) != pos_t.shape[0]:
+        pos_t = pos_t[: int(N)]
+    return Tree(pos_t, S, ncrit, order, theta, source_order=source_order, stream=stream)
+
+
+def direct(pos, S, targets=None, source_order=0, potential=True, field=True, F=None, stream=None):
+    """FP64 O(N^2) sum (example/calculate.cpp:252-264) for a target subset."""
+    pos = _as_device(pos, (3,))
+    S = _as_device(S, (sourcesize(source_order),))
+    N = pos.shape[0]
+    tgt = None
+    nt = N
+    if targets is not None:
+        tgt = torch.as_tensor(np.asarray(targets) if not isinstance(targets, torch.Tensor) else targets)
+        tgt = tgt.to(device=pos.device, dtype=torch.int64).contiguous()
+        nt = tgt.numel()
+    os_ = outputsize(potential, field)
+    Fd = torch.empty((nt, os_), dtype=torch.float64, device=pos.device)
+    check(lib().fmmgen_gpu_direct(C.c_void_p(pos.data_ptr()), C.c_void_p(S.data_ptr()), N,
+                                  C.c_void_p(tgt.data_ptr() if tgt is not None else None), nt, source_order,
+                                  int(potential), int(field), C.c_void_p(Fd.data_ptr()), _stream_ptr(stream)))
+    if F is not None:
+        if isinstance(F, torch.Tensor):
+            F.copy_(Fd)
+        else:
+            F[...] = Fd.cpu().numpy().reshape(np.shape(F))
+        return F
+    return Fd

@@ -1,0 +1,138 @@
+/*
+ * fmmgen_gb300.h -- C ABI of the GB300 (sm_103a) octree FMM library
+ * (libfmmgen_gb300.so).
+ *
+ * It replaces two interfaces of rpep/fmmgen:
+ *   1. the operator ABI that fmmgen.generate_code emits (fmmgen/writer.py:266-330,
+ *      signatures from fmmgen/printers.py:296-313; example instance
+ *      example/operators.cpp:1376-1489): P2M / M2M / M2L / L2L / L2P / P2P with
+ *      "+=" semantics and the FMMGEN_* header macros;
+ *   2. the example tree code's API (example/tree.hpp:78-103):
+ *      build_tree(pos, S, N, ncrit, order, theta) and
+ *      Tree::compute_field_fmm(F) / Tree::compute_field_exact(F).
+ *
+ * Layouts are fmmgen's: positions [N][3], sources [N][SOURCESIZE]
+ * (SOURCESIZE = 1 for charges, 3 for dipoles), outputs [N][OUTPUTSIZE]
+ * (phi, Ex, Ey, Ez as selected by potential/field), multipole/local arrays in
+ * the Nterms multi-index order of fmmgen/utils.py:65-118.  All arrays are
+ * FP64.  Unless a function says "host", pointers are device pointers and work
+ * is stream-ordered on `stream` (a cudaStream_t, NULL = legacy default).
+ * Every function returns a status code (0 = OK) and never aborts; the text of
+ * the last error is available from fmmgen_last_error().
+ */
+#ifndef FMMGEN_GB300_H
+#define FMMGEN_GB300_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FMMGEN_OK 0
+#define FMMGEN_ERR_ARG 1     /* invalid argument (order out of range, N < 1, ...) */
+#define FMMGEN_ERR_CUDA 2    /* CUDA runtime error; see fmmgen_last_error() */
+#define FMMGEN_ERR_DEPTH 3   /* tree would be deeper than 21 levels (>= ncrit coincident points) */
+#define FMMGEN_ERR_RANGE 4   /* interaction offsets beyond the M2L class table */
+#define FMMGEN_ERR_STATE 5   /* handle not built */
+
+/* precision modes of fmmgen_tree_compute_field_fmm */
+#define FMMGEN_PREC_FP64 0   /* every phase in FP64 */
+#define FMMGEN_PREC_MIXED 1  /* FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation */
+
+const char *fmmgen_last_error(void);
+const char *fmmgen_version(void);
+int fmmgen_max_order(void); /* highest expansion order supported (12) */
+
+/* ---- layout constants (the FMMGEN_* macros of fmmgen/writer.py:317-328 and
+ *      Nterms/Msize/Lsize of fmmgen/utils.py:26-35, example/utils.cpp:3-27) ---- */
+long fmmgen_nterms(int p);
+long fmmgen_msize(int order, int source_order);
+long fmmgen_lsize(int order, int source_order);
+int fmmgen_minorder(int source_order, int field);   /* FMMGEN_MINORDER = source_order + field */
+int fmmgen_sourcesize(int source_order);            /* FMMGEN_SOURCESIZE */
+int fmmgen_outputsize(int potential, int field);    /* FMMGEN_OUTPUTSIZE */
+
+/* ---- batched operators: n independent applications, device pointers ----
+ * Each replaces n calls of the generated scalar operator with the same name
+ * (fmmgen/writer.py:147-254): application i reads d[3i..3i+2] and the i-th
+ * input block and adds into the i-th output block.
+ *   P2M: in = q[n],          out = M[n][Msize]     (fmmgen/expansions.py:22-39)
+ *   M2M: in = M[n][Msize],   out = Ms[n][Msize]    (fmmgen/expansions.py:42-78)
+ *   M2L: in = M[n][Msize],   out = L[n][Lsize]     (fmmgen/expansions.py:108-172)
+ *   L2L: in = L[n][Lsize],   out = Ls[n][Lsize]    (fmmgen/expansions.py:175-194)
+ *   L2P: in = L[n][Lsize],   out = F[n][OUTPUTSIZE](fmmgen/expansions.py:197-207)
+ *   P2P: in = S[n][SOURCESIZE], out = F[n][OUTPUTSIZE] (example/operators.cpp:54-66) */
+int fmmgen_gpu_P2M(int n, const double *d, const double *q, double *M, int order, int source_order, void *stream);
+int fmmgen_gpu_M2M(int n, const double *d, const double *M, double *Ms, int order, int source_order, void *stream);
+int fmmgen_gpu_M2L(int n, const double *d, const double *M, double *L, int order, int source_order, void *stream);
+int fmmgen_gpu_L2L(int n, const double *d, const double *L, double *Ls, int order, int source_order, void *stream);
+int fmmgen_gpu_L2P(int n, const double *d, const double *L, double *F, int order, int source_order, int potential,
+                   int field, void *stream);
+int fmmgen_gpu_P2P(int n, const double *d, const double *S, double *F, int source_order, int potential, int field,
+                   void *stream);
+
+/* ---- scalar twins of the generated dispatchers (host pointers, run on the
+ *      GPU synchronously).  Signatures of example/operators.cpp:1376-1489;
+ *      source_order / potential / field are those set by fmmgen_configure
+ *      (the generator fixes them at generation time, fmmgen/writer.py:33-50).
+ *      An order outside [minorder, maxorder] is a silent no-op, as the
+ *      generated switch has no default case (fmmgen/writer.py:296-309). ---- */
+int fmmgen_configure(int source_order, int potential, int field, int maxorder);
+void P2M(double x, double y, double z, double q, double *M, int order);
+void M2M(double x, double y, double z, double *M, double *Ms, int order);
+void M2L(double x, double y, double z, double *M, double *L, int order);
+void L2L(double x, double y, double z, double *L, double *Ls, int order);
+void L2P(double x, double y, double z, double *L, double *F, int order);
+void P2P(double x, double y, double z, double *S, double *F);
+
+/* ---- tree-level API (example/tree.hpp:78-103) ---- */
+typedef struct fmmgen_tree fmmgen_tree;
+
+/* build_tree (example/tree.cpp:130-233) on the device: adaptive octree with the
+ * reference's root cube, ncrit split rule and FP64 centre arithmetic, and the
+ * M2L/P2P interaction lists of interact_dehnen_lazy (example/calculate.cpp:81-133).
+ * pos: device [N][3].  *tree may be NULL (a new handle is made) or an existing
+ * handle whose device buffers are reused.  Synchronises `stream`. */
+int fmmgen_tree_build(const double *pos, long N, long ncrit, int order, double theta, int source_order,
+                      void *stream, fmmgen_tree **tree);
+
+/* Tree::compute_field_fmm (example/tree.cpp:243-271): F (device
+ * [N][OUTPUTSIZE], caller's particle order) is overwritten with phi / E from
+ * the sources S (device [N][SOURCESIZE], caller's particle order).  Does not
+ * synchronise. */
+int fmmgen_tree_compute_field_fmm(fmmgen_tree *tree, const double *S, double *F, int potential, int field,
+                                  int precision, void *stream);
+
+/* Tree::compute_field_exact / evaluate_direct (example/calculate.cpp:252-264):
+ * FP64 O(N^2) sum for the targets listed in `targets` (device, NULL = all N);
+ * F is [ntargets][OUTPUTSIZE] in the order of `targets`. */
+int fmmgen_gpu_direct(const double *pos, const double *S, long N, const long *targets, long ntargets,
+                      int source_order, int potential, int field, double *F, void *stream);
+
+int fmmgen_tree_free(fmmgen_tree *tree);
+
+/* Introspection (host outputs; synchronises).
+ * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit]. */
+int fmmgen_tree_info(fmmgen_tree *tree, long *info);
+/* Root cube [cx, cy, cz, r]. */
+int fmmgen_tree_root(fmmgen_tree *tree, double *root4);
+/* Per cell (level-major order): canonical id (1 << 3*level | octant path),
+ * particle count (the reference's nleaf), centre [3]; leaf particle lists as
+ * CSR over leaves in cell order (caller's particle indices). */
+int fmmgen_tree_export_cells(fmmgen_tree *tree, unsigned long long *cell_id, long *cell_count, double *centre,
+                             long *leaf_off, long *leaf_idx);
+/* Interaction lists as canonical-id pairs, grouped by target:
+ * m2l [nm2l][2] = (source, target), p2p [np2p][2] = (target, source). */
+int fmmgen_tree_export_lists(fmmgen_tree *tree, unsigned long long *m2l, unsigned long long *p2p);
+/* Scaled expansions of the last FP64 evaluate, unscaled back to fmmgen's
+ * convention: M [ncells][Msize], L [ncells][Lsize], cells in level-major order. */
+int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, double *L);
+/* Phase times of the last build ([root, keys+sort, cells, lists, classes, total])
+ * and evaluate ([P2M, M2M, M2L, P2P, L2L, L2P, finalize, total]) in ms. */
+int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FMMGEN_GB300_H */

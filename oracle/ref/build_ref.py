@@ -1,0 +1,134 @@
+"""Build the reference's own FMM path into oracle/_ref/ (checker only).
+
+Recipe, run in the development container where the reference checkout exists:
+  1. fmmgen.generate_code (the reference generator, imported read-only from the
+     checkout) emits operators.{cpp,h} for Coulomb (source_order=0, orders
+     1..PMAX0) and dipole (source_order=1, orders 2..PMAX1) sources, with the
+     settings of the reference's example/example.py (CSE, harmonic derivatives,
+     minpow=11, atomic, C++).
+  2. g++ compiles the reference's example/tree.cpp, calculate.cpp, utils.cpp
+     where they lie in the checkout, plus the generated operators and
+     oracle/ref/ref_harness.cpp, into oracle/_ref/libref_so{0,1}.so.
+     -ffp-contract=off keeps every FP64 expression as written (no FMA
+     contraction), which the bit-exact tree/list comparisons rely on.
+
+Outputs are cached: a step is skipped when its output is newer than its inputs.
+Nothing here is shipped; the GPU machine never runs it.
+
+Usage: python oracle/ref/build_ref.py [--reference DIR] [--pmax0 8] [--pmax1 6]
+"""
+import argparse
+import contextlib
+import io
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(os.path.dirname(HERE), "_ref")
+DEFAULT_REF = "/root/reference"
+
+
+def _generate(args):
+    ref, so, pmax, outdir = args
+    sys.path.insert(0, ref)
+    import fmmgen  # the reference generator
+
+    os.makedirs(outdir, exist_ok=True)
+    cwd = os.getcwd()
+    os.chdir(outdir)
+    try:
+        with contextlib.redirect_stdout(io.StringIO()):
+            fmmgen.generate_code(
+                pmax + 1,  # the generator's upper order bound is exclusive
+                "operators",
+                precision="double",
+                CSE=True,
+                cython=False,
+                potential=True,
+                field=True,
+                source_order=so,
+                atomic=True,
+                minpow=11,
+                harmonic_derivs=True,
+                language="c++",
+                include_dir=outdir,
+                src_dir=outdir,
+            )
+    finally:
+        os.chdir(cwd)
+    return outdir
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build(ref=DEFAULT_REF, pmax0=8, pmax1=6, jobs=4, verbose=True):
+    """Generate + compile; returns {source_order: path to .so}.  Raises if the
+    reference checkout is absent."""
+    ex = os.path.join(ref, "example")
+    if not os.path.isdir(ex):
+        raise FileNotFoundError(f"reference checkout not found at {ref}")
+    specs = [(0, pmax0), (1, pmax1)]
+    gen_jobs = []
+    for so, pmax in specs:
+        outdir = os.path.join(OUT, f"so{so}_p{pmax}")
+        if _stale(os.path.join(outdir, "operators.cpp"), [os.path.join(ref, "fmmgen", "generator.py")]):
+            gen_jobs.append((ref, so, pmax, outdir))
+    if gen_jobs:
+        if verbose:
+            print(f"[build_ref] generating operators with fmmgen: {[(j[1], j[2]) for j in gen_jobs]}", flush=True)
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(len(gen_jobs)) as pool:
+            pool.map(_generate, gen_jobs)
+    libs = {}
+    procs = []
+    for so, pmax in specs:
+        gdir = os.path.join(OUT, f"so{so}_p{pmax}")
+        lib = os.path.join(OUT, f"libref_so{so}.so")
+        srcs = [os.path.join(ex, f) for f in ("tree.cpp", "calculate.cpp", "utils.cpp")]
+        deps = srcs + [os.path.join(gdir, "operators.cpp"), os.path.join(HERE, "ref_harness.cpp"), __file__]
+        libs[so] = lib
+        if not _stale(lib, deps):
+            continue
+        objs = []
+        flags = ["-O2", "-std=c++14", "-fopenmp", "-fPIC", "-ffp-contract=off", "-I", gdir, "-I", ex]
+        cmds = []
+        for s in srcs:
+            o = os.path.join(gdir, os.path.basename(s).replace(".cpp", ".o"))
+            cmds.append(["g++", *flags, "-c", s, "-o", o])
+            objs.append(o)
+        o = os.path.join(gdir, "operators.o")
+        cmds.append(["g++", *flags, "-DP2P=fmmgen_generated_P2P", "-c", os.path.join(gdir, "operators.cpp"), "-o", o])
+        objs.append(o)
+        o = os.path.join(gdir, "ref_harness.o")
+        cmds.append(["g++", *flags, "-c", os.path.join(HERE, "ref_harness.cpp"), "-o", o])
+        objs.append(o)
+        procs.append((cmds, objs, lib, flags))
+    for cmds, objs, lib, flags in procs:
+        if verbose:
+            print(f"[build_ref] compiling {lib}", flush=True)
+        running = [subprocess.Popen(c) for c in cmds]
+        rcs = [p.wait() for p in running]
+        if any(rcs):
+            raise RuntimeError(f"reference compile failed: {rcs}")
+        subprocess.check_call(["g++", "-shared", "-fopenmp", "-o", lib, *objs])
+    return libs
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=DEFAULT_REF)
+    ap.add_argument("--pmax0", type=int, default=8)
+    ap.add_argument("--pmax1", type=int, default=6)
+    a = ap.parse_args()
+    print(build(a.reference, a.pmax0, a.pmax1))
+
+
+if __name__ == "__main__":
+    main()

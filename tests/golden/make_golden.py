@@ -1,0 +1,136 @@
+"""Write the golden fixtures in tests/golden/ from the reference itself.
+
+Run in the development container after `python oracle/ref/build_ref.py`:
+    python tests/golden/make_golden.py
+The values come from the reference's own code: fmmgen's generated operators
+(P2M/M2M/M2L/L2L/L2P at every order) and the example's build_tree /
+interact_dehnen_lazy / compute_field_fmm, linked by oracle/ref/ref_harness.cpp.
+The one restated piece is P2P (the generated field is zero at HEAD); its
+potential is checked against the generated P2P here before anything is saved.
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle import oracle as O  # noqa: E402
+
+
+def list_digest(pairs):
+    """SHA-256 of the sorted pair multiset (rows of uint64)."""
+    a = np.ascontiguousarray(pairs, dtype=np.uint64).reshape(-1, 2)
+    order = np.lexsort((a[:, 1], a[:, 0]))
+    return hashlib.sha256(a[order].tobytes()).hexdigest()
+
+
+def make_ops():
+    rng = np.random.default_rng(2024)
+    for so, (pmin, pmax) in ((0, (1, 8)), (1, (2, 6))):
+        R = O.ref(so)
+        out = {}
+        K = 6
+        for p in range(pmin, pmax + 1):
+            ms, ls = O.msize(p, so), O.lsize(p, so)
+            d = rng.uniform(-1, 1, (K, 3))
+            d *= rng.uniform(1.0, 3.0, (K, 1)) / np.linalg.norm(d, axis=1, keepdims=True)
+            q = rng.uniform(-1, 1, K)
+            Min = rng.standard_normal((K, ms))
+            Lin = rng.standard_normal((K, ls))
+            res = {k: [] for k in ("P2M", "M2M", "M2L", "L2L", "L2P")}
+            for i in range(K):
+                a = np.zeros(ms); R.ref_P2M(*d[i], q[i], a, p); res["P2M"].append(a)
+                a = np.zeros(ms); R.ref_M2M(*d[i], Min[i].copy(), a, p); res["M2M"].append(a)
+                a = np.zeros(ls); R.ref_M2L(*d[i], Min[i].copy(), a, p); res["M2L"].append(a)
+                a = np.zeros(ls); R.ref_L2L(*d[i], Lin[i].copy(), a, p); res["L2L"].append(a)
+                a = np.zeros(4); R.ref_L2P(*d[i], Lin[i].copy(), a, p); res["L2P"].append(a)
+            out[f"p{p}_d"] = d
+            out[f"p{p}_q"] = q
+            out[f"p{p}_M"] = Min
+            out[f"p{p}_L"] = Lin
+            for k, v in res.items():
+                out[f"p{p}_{k}"] = np.array(v)
+        # P2P: restated physics; its potential must equal the generated P2P's
+        ss = 1 if so == 0 else 3
+        d = rng.uniform(-1, 1, (16, 3))
+        S = rng.standard_normal((16, ss))
+        Fr = np.zeros((16, 4))
+        Fg = np.zeros((16, 4))
+        for i in range(16):
+            R.ref_P2P_restated(*d[i], S[i].copy(), Fr[i])
+            R.ref_P2P_generated(*d[i], S[i].copy(), Fg[i])
+        assert np.allclose(Fr[:, 0], Fg[:, 0], rtol=1e-13, atol=0), "restated P2P potential != generated"
+        out["p2p_d"], out["p2p_S"], out["p2p_F"], out["p2p_F_generated"] = d, S, Fr, Fg
+        out["pmin"], out["pmax"] = np.int64(pmin), np.int64(pmax)
+        np.savez_compressed(os.path.join(HERE, f"ops_so{so}.npz"), **out)
+        print(f"ops_so{so}.npz: orders {pmin}..{pmax}")
+
+
+def plummer(rng, n, a=0.1, rmax=1.0):
+    pts = []
+    while sum(len(p) for p in pts) < n:
+        u = rng.uniform(0, 1, 2 * n)
+        r = a / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        r = r[r <= rmax]
+        v = rng.standard_normal((len(r), 3))
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        pts.append(v * r[:, None])
+    return np.concatenate(pts)[:n]
+
+
+def clusters(rng, n, k=4, sigma=0.02):
+    m = n // 2
+    cen = rng.uniform(0, 1, (k, 3))
+    lab = rng.integers(0, k, n - m)
+    return np.concatenate([rng.uniform(0, 1, (m, 3)), cen[lab] + sigma * rng.standard_normal((n - m, 3))])
+
+
+CASES = {
+    # name: (N, ncrit, order, theta, source_order, generator)
+    "uniform10k": (10000, 64, 4, 0.5, 0, "uniform"),
+    "deep": (3000, 8, 3, 0.7, 0, "uniform"),
+    "dipole_plummer": (4000, 32, 4, 0.5, 1, "plummer"),
+    "clustered": (5000, 16, 5, 0.4, 0, "clusters"),
+    "tiny": (50, 64, 3, 0.5, 0, "uniform"),
+    "example_scaled": (2000, 64, 4, 0.5, 0, "example"),
+}
+
+
+def make_trees():
+    for seed, (name, (N, ncrit, p, theta, so, gen)) in enumerate(CASES.items()):
+        rng = np.random.default_rng(seed)
+        if gen == "uniform":
+            pos = rng.uniform(0, 1, (N, 3))
+        elif gen == "plummer":
+            pos = plummer(rng, N)
+        elif gen == "clusters":
+            pos = clusters(rng, N)
+        else:  # the example driver's data: U(-1,1) scaled by 1e-9 (example/main.cpp:86-110)
+            pos = rng.uniform(-1, 1, (N, 3)) * 1e-9
+        S = rng.uniform(-1, 1, (N, 1)) if so == 0 else rng.standard_normal((N, 3))
+        rt = O.RefTree(pos, S, ncrit, p, theta, so)
+        cells = rt.cells()
+        m2l, p2p = rt.lists()
+        F, _ = rt.evaluate()
+        leaf_cell_ids = cells["id"][cells["nleaf"] < ncrit]
+        order = np.argsort(cells["id"])
+        out = dict(N=np.int64(N), ncrit=np.int64(ncrit), order=np.int64(p), theta=np.float64(theta),
+                   source_order=np.int64(so), pos=pos, S=S, F=F,
+                   cell_id=cells["id"][order], cell_nleaf=cells["nleaf"][order], cell_centre=cells["centre"][order],
+                   leaf_id=leaf_cell_ids, leaf_off=cells["leaf_off"], leaf_idx=cells["leaf_idx"],
+                   nm2l=np.int64(len(m2l)), np2p=np.int64(len(p2p)),
+                   m2l_sha256=np.array(list_digest(m2l)), p2p_sha256=np.array(list_digest(p2p)))
+        if len(m2l) + len(p2p) < 20000:
+            o = np.lexsort((m2l[:, 1], m2l[:, 0]))
+            out["m2l"] = m2l[o]
+            o = np.lexsort((p2p[:, 1], p2p[:, 0]))
+            out["p2p"] = p2p[o]
+        np.savez_compressed(os.path.join(HERE, f"tree_{name}.npz"), **out)
+        print(f"tree_{name}.npz: cells {rt.ncells} leaves {rt.nleaves} m2l {len(m2l)} p2p {len(p2p)}")
+
+
+if __name__ == "__main__":
+    make_ops()
+    make_trees()
