@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the octree FMM evaluation path on GB300.
+
+Workload (one "step"): the full FMM -- device octree + interaction lists +
+P2M/M2M/M2L/P2P/L2L/L2P -- of N = 1,000,000 Coulomb charges, positions i.i.d.
+uniform in [0,1]^3 and charges uniform in [-1,1] (seeded synthetic data),
+expansion order p = 8, ncrit = 128, theta = 0.5, field output, mixed precision.
+`value` is particles/s with inputs resident in HBM; `e2e` is the same step
+through the public API from pinned host buffers, copies included.  The plain
+FP64 GPU FMM is timed beside it, and the field error of both against an FP64
+direct sum on a 10,000-particle subset is reported.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Multi-GPU: the path is replicated (independent systems per rank, no collective
+on the data path); `value` is the job total.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particles/s full FMM, N=1M p=8 at 1e-6 rel field err: mixed/learned vs FP64"
+UNIT = "particles/s"
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--order", type=int, default=8)
+    ap.add_argument("--ncrit", type=int, default=128)
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(n, seed):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0.0, 1.0, (n, 3))
+    q = rng.uniform(-1.0, 1.0, (n, 1))
+    return pos, q
+
+
+def config(a, world):
+    return {"workload": f"octree FMM, {a.n} uniform Coulomb charges in the unit cube, p={a.order}, "
+                        f"ncrit={a.ncrit}, theta={a.theta}, field output, tree+lists+evaluation per step",
+            "N": a.n, "order": a.order, "ncrit": a.ncrit, "theta": a.theta, "source_order": 0,
+            "precision": "mixed (FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation)",
+            "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"}
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the checker's restatement of the reference path on host cores
+# ---------------------------------------------------------------------------
+def cpu_sample(pos, q, a, stride):
+    from oracle import oracle as orc
+
+    t0 = time.perf_counter()
+    ot = orc.OracleTree(pos, q, a.ncrit, a.order, a.theta, 0)
+    t_build = time.perf_counter() - t0
+    _, ph = ot.evaluate(potential=False, field=True, sample_stride=stride)
+    p2m, m2m, m2l, p2p, l2l, l2p = ph.tolist()
+    t_full = t_build + p2m + m2m + l2l + stride * (m2l + p2p + l2p)
+    sample = (f"oracle port (C, OpenMP) on this host: full tree build, P2M, M2M, L2L; M2L, P2P, L2P on every "
+              f"{stride}-th target cell, scaled by {stride}; N={a.n}")
+    return a.n / t_full, t_full, sample, orc.num_threads()
+
+
+def run_reference(a, rank, world):
+    """--impl reference: the reference path's CPU implementation on host cores."""
+    if rank != 0:
+        return
+    import subprocess as sp
+
+    sp.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    pos, q = workload(a.n, a.seed)
+    stride = max(a.cpu_stride, 64)
+    for _ in range(a.warmup):
+        cpu_sample(pos, q, a, stride)
+    t0 = time.perf_counter()
+    est = 0.0
+    for _ in range(a.steps):
+        v, t_full, sample, cores = cpu_sample(pos, q, a, stride)
+        est += t_full
+    wall = time.perf_counter() - t0
+    value = a.n * a.steps / est
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * est / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform)", "config": config(a, world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def main():
+    a = args_parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    import torch
+
+    import fmmgen_gb300 as fg
+    from fmmgen_gb300 import build as fbuild
+
+    if not os.path.exists(fbuild.LIB) and rank == 0:
+        fbuild.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+        dist.barrier()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    pos_np, q_np = workload(a.n, a.seed + rank)
+    pos = torch.tensor(pos_np, device=dev)
+    q = torch.tensor(q_np, device=dev)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    F = torch.empty((a.n, 3), dtype=torch.float64, device=dev)
+    L = fg.lib()
+
+    tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta)
+
+    def step(precision="mixed"):
+        tree.rebuild(pos)
+        tree.compute_field_fmm(F, potential=False, field=True, precision=precision)
+
+    phase_sum = {}
+
+    def timed(nsteps, fn, collect_phases=False):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(nsteps):
+            flush.fill_(float(i))
+            evs[i][0].record(st)
+            fn()
+            evs[i][1].record(st)
+            if collect_phases:
+                torch.cuda.synchronize()
+                b, e = tree.times()
+                for k, v in list(b.items()) + list(e.items()):
+                    key = ("build_" if k in b and k not in e else "") + k
+                    phase_sum[key] = phase_sum.get(key, 0.0) + v
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+        dev_ms = sum(s.elapsed_time(e) for s, e in evs)
+        return dev_ms, wall
+
+    # ---- device-resident value (mixed) ----
+    for _ in range(a.warmup):
+        step()
+    n0 = L.fmmgen_launch_count()
+    with ClockSampler(local) as clk:
+        dev_ms, wall = timed(a.steps, step, collect_phases=True)
+    launches = L.fmmgen_launch_count() - n0
+    t_max = dev_ms
+    if pg:
+        t = torch.tensor([dev_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_max = t.item()
+    value = a.n * a.steps * world / (t_max / 1e3)
+    ms_per_step = t_max / a.steps
+
+    # ---- e2e through the public API from pinned host memory ----
+    pos_h = torch.tensor(pos_np).pin_memory()
+    q_h = torch.tensor(q_np).pin_memory()
+    F_h = torch.empty((a.n, 3), dtype=torch.float64).pin_memory()
+    pos_d = torch.empty_like(pos)
+    q_d = torch.empty_like(q)
+
+    def e2e_step():
+        pos_d.copy_(pos_h, non_blocking=True)
+        q_d.copy_(q_h, non_blocking=True)
+        tree.rebuild(pos_d)
+        tree.compute_field_fmm(F, S=q_d, potential=False, field=True, precision="mixed")
+        F_h.copy_(F, non_blocking=True)
+
+    e2e_step()
+    k_e2e = max(3, a.steps // 2)
+    e2e_ms, _ = timed(k_e2e, e2e_step)
+    e2e_max = e2e_ms
+    if pg:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_max = t.item()
+    e2e_value = a.n * k_e2e * world / (e2e_max / 1e3)
+    h2d = pos_h.numel() * 8 + q_h.numel() * 8
+    d2h = F_h.numel() * 8
+    tree.rebuild(pos)
+    tree.S = q
+
+    # ---- accuracy vs FP64 direct sum, and the plain FP64 GPU FMM ----
+    tg = torch.arange(0, a.n, max(1, a.n // 10000), device=dev)[:10000]
+    Fd = fg.direct(pos, q, targets=tg, potential=False, field=True)
+
+    def err(Fx):
+        return (torch.linalg.norm(Fx[tg] - Fd) / torch.linalg.norm(Fd)).item()
+
+    step("mixed")
+    err_mixed = err(F)
+    fp64 = {}
+    if not a.no_fp64:
+        step("fp64")
+        err_fp64 = err(F)
+        k64 = 2
+        ms64, _ = timed(k64, lambda: step("fp64"))
+        fp64 = {"value": a.n * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "rel_field_err": err_fp64}
+        _, e64 = tree.times()
+        fp64["phases_ms"] = {k: round(v, 3) for k, v in e64.items()}
+
+    # ---- roofline of the dominant kernel (live CUDA-event phase times) ----
+    ph = {k: v / a.steps for k, v in phase_sum.items()}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal at the max SM clock
+    p2p_flops = 20.0 * tree.p2p_interactions
+    m2l_flops = 2.0 * math.comb(a.order + 6, 6) * tree.nm2l
+    cand = {"P2P": (ph.get("P2P", 0.0), p2p_flops), "M2L": (ph.get("M2L", 0.0), m2l_flops)}
+    dom = max(cand, key=lambda k: cand[k][0])
+    dom_ms, dom_flops = cand[dom]
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(dom, {}).get("bytes_per_launch")
+    except Exception:
+        pass
+    achieved = dom_flops / (dom_ms / 1e3) / 1e12 if dom_ms > 0 else 0.0
+    roofline = {"kernel": dom, "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "traffic": traffic,
+                "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json "
+                               "(no measured FP32 figure exists)",
+                "work": f"{'20 flop x P2P interactions' if dom == 'P2P' else '2*C(p+6,6) flop x M2L pairs'} "
+                        f"per launch = {dom_flops:.3e} flop"}
+    m2l_ms, _ = cand["M2L"]
+    roofline_m2l = {"kernel": "M2L", "bound": "tensor", "algorithmic_tflops": m2l_flops / (m2l_ms / 1e3) / 1e12
+                    if m2l_ms > 0 else 0.0, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                    "frac": (m2l_flops / (m2l_ms / 1e3) / 1e12) / peaks["bf16_tflops"]
+                    if m2l_ms > 0 and peaks.get("bf16_tflops") else None,
+                    "note": "M2L runs on the FP32 pipe in this build; fraction is of the measured bf16 tensor peak"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic (seeded uniform positions and charges)",
+            "config": config(a, world), "rel_field_err": err_mixed,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "roofline": roofline, "roofline_m2l": roofline_m2l,
+            "fp64_plain": fp64, "speedup_vs_fp64": (value / world) / fp64["value"] if fp64 else None,
+            "phases_ms": {k: round(v, 3) for k, v in ph.items()},
+            "tree": {"cells": tree.ncells, "leaves": tree.nleaves, "m2l_pairs": tree.nm2l, "p2p_pairs": tree.np2p,
+                     "p2p_interactions": tree.p2p_interactions, "m2l_classes": tree.nclasses},
+            "clocks": clk.summary(), "wall_s": wall}
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        v, t_full, sample, cores = cpu_sample(pos_np, q_np, a, a.cpu_stride)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

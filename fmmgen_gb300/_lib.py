@@ -27,6 +27,7 @@ _SIGS = {
     "fmmgen_last_error": (C.c_char_p, []),
     "fmmgen_version": (C.c_char_p, []),
     "fmmgen_max_order": (C.c_int, []),
+    "fmmgen_launch_count": (C.c_longlong, []),
     "fmmgen_nterms": (C.c_long, [C.c_int]),
     "fmmgen_msize": (C.c_long, [C.c_int, C.c_int]),
     "fmmgen_lsize": (C.c_long, [C.c_int, C.c_int]),

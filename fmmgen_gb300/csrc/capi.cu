@@ -1,4 +1,5 @@
 // capi.cu -- the extern "C" boundary declared in include/fmmgen_gb300.h.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -43,8 +44,12 @@ void fmm_set_cuda_error(cudaError_t e, const char *what, const char *file, int l
 }
 void fmm_set_error_text(const char *msg) { g_err = msg; }
 
+static std::atomic<long long> g_launches{0};
+void fmm_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 extern "C" {
 
+long long fmmgen_launch_count(void) { return g_launches.load(); }
 const char *fmmgen_last_error(void) { return g_err.c_str(); }
 const char *fmmgen_version(void) { return "fmmgen_gb300 0.1 (sm_103a)"; }
 int fmmgen_max_order(void) { return FMM_PMAX; }
@@ -201,6 +206,7 @@ int fmmgen_tree_info(fmmgen_tree *tree, long *info) {
   DevTree &t = tree->t;
   info[0] = t.ncells; info[1] = t.nleaves; info[2] = t.nm2l; info[3] = t.np2p;
   info[4] = t.nlevels; info[5] = t.nclasses; info[6] = t.N; info[7] = t.ncrit;
+  info[8] = (long)t.p2p_interactions;
   return FMM_OK;
 }
 
@@ -292,9 +298,9 @@ extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, doubl
   FMM_CUDA_TRY(cudaMalloc((void **)&dM, nc * ms * sizeof(double)));
   FMM_CUDA_TRY(cudaMalloc((void **)&dL, nc * ls * sizeof(double)));
   if (tree->last_precision == FMMGEN_PREC_FP64)
-    k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
+    fmm_note_launch(), k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
   else
-    k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
+    fmm_note_launch(), k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(M, dM, nc * ms * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(L, dL, nc * ls * sizeof(double), cudaMemcpyDeviceToHost);

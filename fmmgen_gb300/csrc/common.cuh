@@ -53,6 +53,8 @@ __host__ __device__ __forceinline__ MI fmm_decode(int i) {
 
 void fmm_set_cuda_error(cudaError_t e, const char *what, const char *file, int line);
 void fmm_set_error_text(const char *msg);
+// Counts kernel launches made by this library (every launch site calls it).
+void fmm_note_launch();
 
 __device__ __forceinline__ unsigned fmm_lane() { return threadIdx.x & 31u; }
 

@@ -41,10 +41,22 @@ template <typename T> __device__ __forceinline__ T engine_out(const Plan &P, con
   return s;
 }
 
-__device__ __forceinline__ double pow2i(int e) { return ldexp(1.0, e); }
+// 2^e built from the exponent bits (|e| well inside the normal range here);
+// avoids FP64 ldexp, which runs on GB300's narrow FP64 pipe.
+template <typename T> __device__ __forceinline__ T exp2i(int e);
+template <> __device__ __forceinline__ float exp2i<float>(int e) { return __int_as_float((e + 127) << 23); }
+template <> __device__ __forceinline__ double exp2i<double>(int e) {
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
 
-// per-level half-width s_l and 1/s_l (exact powers of two times the root r)
-struct Levels { const double *lev; };
+// 1/q for the factorials, in each precision (no divisions in the loops)
+static __constant__ float c_rcpf[FMM_PMAX + 1] = {0.f, 1.f, 1.f / 2, 1.f / 3, 1.f / 4, 1.f / 5, 1.f / 6,
+                                                  1.f / 7, 1.f / 8, 1.f / 9, 1.f / 10, 1.f / 11, 1.f / 12};
+static __constant__ double c_rcpd[FMM_PMAX + 1] = {0., 1., 1. / 2, 1. / 3, 1. / 4, 1. / 5, 1. / 6,
+                                                   1. / 7, 1. / 8, 1. / 9, 1. / 10, 1. / 11, 1. / 12};
+template <typename T> __device__ __forceinline__ T rcp_int(int q);
+template <> __device__ __forceinline__ float rcp_int<float>(int q) { return c_rcpf[q]; }
+template <> __device__ __forceinline__ double rcp_int<double>(int q) { return c_rcpd[q]; }
 
 // ---------------------------------------------------------------------------
 // P2M (example/calculate.cpp:135-161)
@@ -79,7 +91,8 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
       T a = 1, b = 1, d = 1;
       tb[w][0][lane][0] = a; tb[w][1][lane][0] = b; tb[w][2][lane][0] = d;
       for (int k = 1; k <= order; k++) {
-        a = a * ux / T(k); b = b * uy / T(k); d = d * uz / T(k);
+        const T rk = rcp_int<T>(k);
+        a = a * ux * rk; b = b * uy * rk; d = d * uz * rk;
         tb[w][0][lane][k] = a; tb[w][1][lane][k] = b; tb[w][2][lane][k] = d;
       }
       uint32_t o = perm[i];
@@ -121,17 +134,18 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
   }
 }
 
-// shift monomials mon[idx(k)] = v^k / k! for |k| <= pmax (warp-parallel)
+// shift monomials mon[idx(k)] = v^k / k! for |k| <= pmax (warp-parallel, in T)
 template <typename T>
 __device__ __forceinline__ void warp_monomials(double vx, double vy, double vz, int pmax, T *mon, int lane) {
   int cnt = fmm_nterms(pmax);
+  const T x = (T)vx, y = (T)vy, z = (T)vz;
   for (int i = lane; i < cnt; i += 32) {
     int kx = c_mi[i][0], ky = c_mi[i][1], kz = c_mi[i][2];
-    double a = 1, b = 1, d = 1;
-    for (int q = 1; q <= kx; q++) a = a * vx / q;
-    for (int q = 1; q <= ky; q++) b = b * vy / q;
-    for (int q = 1; q <= kz; q++) d = d * vz / q;
-    mon[i] = (T)(a * b * d);
+    T a = 1, b = 1, d = 1;
+    for (int q = 1; q <= kx; q++) a = a * x * rcp_int<T>(q);
+    for (int q = 1; q <= ky; q++) b = b * y * rcp_int<T>(q);
+    for (int q = 1; q <= kz; q++) d = d * z * rcp_int<T>(q);
+    mon[i] = a * b * d;
   }
 }
 
@@ -159,7 +173,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, 
     __syncwarp();
     warp_monomials<T>((cx[c] - cx[ch]) * inv_s, (cy[c] - cy[ch]) * inv_s, (cz[c] - cz[ch]) * inv_s, order - so,
                       sA[w], lane);
-    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)ch * msize + j] * (T)pow2i(-(int)c_mi[j + off][3]);
+    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)ch * msize + j] * exp2i<T>(-(int)c_mi[j + off][3]);
     __syncwarp();
     engine_run<T>(P, sA[w], sB[w], sS[w], lane);
   }
@@ -193,7 +207,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l(Plan P, int ncells, int 
     const int dl = la - (int)clevel[B];  // rho = s_B / s_A = 2^(lA - lB)
     __syncwarp();
     for (int i = lane; i < nt; i += 32) sA[w][i] = D[i];
-    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)B * msize + j] * (T)pow2i(dl * (int)c_mi[j + moff][3]);
+    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)B * msize + j] * exp2i<T>(dl * (int)c_mi[j + moff][3]);
     __syncwarp();
     engine_run<T>(P, sA[w], sB[w], sS[w], lane);
   }
@@ -224,7 +238,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_l2l(Plan P, int lo, int hi, 
   engine_run<T>(P, sA[w], sB[w], sS[w], lane);
   __syncwarp();
   for (int n = lane; n < lsize; n += 32)
-    L[(size_t)c * lsize + n] += engine_out<T>(P, sS[w], n) * (T)pow2i(-((int)c_mi[n][3] + 1));
+    L[(size_t)c * lsize + n] += engine_out<T>(P, sS[w], n) * exp2i<T>(-((int)c_mi[n][3] + 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -257,7 +271,8 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
       T a = 1, b = 1, d = 1;
       tb[w][0][0][lane] = a; tb[w][1][0][lane] = b; tb[w][2][0][lane] = d;
       for (int k = 1; k <= pl; k++) {
-        a = a * ux / T(k); b = b * uy / T(k); d = d * uz / T(k);
+        const T rk = rcp_int<T>(k);
+        a = a * ux * rk; b = b * uy * rk; d = d * uz * rk;
         tb[w][0][k][lane] = a; tb[w][1][k][lane] = b; tb[w][2][k][lane] = d;
       }
       T phi = 0, ex = 0, ey = 0, ez = 0;
@@ -363,44 +378,61 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
   c = (t - s) - y;
   s = t;
 }
+// Two-float leaf-pair offset: c_A - c_B = d * s_L exactly as (hi, lo), with d
+// the integer offset of the centres in half-widths of the finer level L.
+__device__ __forceinline__ void offset2(int d, float2 sc, float &hi, float &lo) {
+  float df = (float)d;
+  hi = df * sc.x;
+  lo = fmaf(df, sc.x, -hi) + df * sc.y;
+}
+// t = (a_hi + a_lo) + (o_hi + o_lo) as (hi, lo), exact two-sum on the high parts
+__device__ __forceinline__ void add2(float ah, float al, float oh, float ol, float &th, float &tl) {
+  th = ah + oh;
+  float bv = th - ah;
+  tl = ((ah - (th - bv)) + (oh - bv)) + (al + ol);
+}
+
 __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
                                                           const int *pcount, const int *off_, const int *src,
-                                                          const double *cx, const double *cy, const double *cz,
-                                                          const float *lx, const float *ly, const float *lz,
-                                                          const uint32_t *perm, const double *S, int so,
-                                                          double *Fnear) {
-  __shared__ float4 sp[P2P_WARPS][32];
-  __shared__ float4 sd[P2P_WARPS][32];
+                                                          const int *ix, const int *iy, const int *iz,
+                                                          const unsigned char *clevel, const float2 *levf,
+                                                          const float4 *phi4, const float4 *plo4,
+                                                          const float4 *sdip, int so, double *Fnear) {
+  __shared__ float4 sh[P2P_WARPS][32], sl[P2P_WARPS][32], sd[P2P_WARPS][32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int leaf = blockIdx.x * P2P_WARPS + w;
   if (leaf >= nleaves) return;
   const int A = leaf_cells[leaf];
   const int a0 = pstart[A], na = pcount[A];
   const int k0 = off_[A], k1 = off_[A + 1];
-  const double cax = cx[A], cay = cy[A], caz = cz[A];
+  const int la = clevel[A], iax = 2 * ix[A] + 1, iay = 2 * iy[A] + 1, iaz = 2 * iz[A] + 1;
   for (int tb = 0; tb < na; tb += 32) {
     const int i = a0 + tb + lane;
     const bool ok = tb + lane < na;
-    float xi = 0, yi = 0, zi = 0;
-    if (ok) { xi = lx[i]; yi = ly[i]; zi = lz[i]; }
+    float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
+    if (ok) { th = phi4[i]; tl = plo4[i]; }
     float s0 = 0, s1 = 0, s2 = 0, s3 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
     for (int k = k0; k < k1; k++) {
       const int B = src[k];
       const int b0 = pstart[B], nb = pcount[B];
-      const float ox = (float)(cax - cx[B]), oy = (float)(cay - cy[B]), oz = (float)(caz - cz[B]);
-      const float tx = xi + ox, ty = yi + oy, tz = zi + oz;
+      const int lb = clevel[B], L = max(la, lb);
+      const float2 sc = levf[L];
+      float oxh, oxl, oyh, oyl, ozh, ozl;
+      offset2((iax << (L - la)) - ((2 * ix[B] + 1) << (L - lb)), sc, oxh, oxl);
+      offset2((iay << (L - la)) - ((2 * iy[B] + 1) << (L - lb)), sc, oyh, oyl);
+      offset2((iaz << (L - la)) - ((2 * iz[B] + 1) << (L - lb)), sc, ozh, ozl);
+      float txh, txl, tyh, tyl, tzh, tzl;
+      add2(th.x, tl.x, oxh, oxl, txh, txl);
+      add2(th.y, tl.y, oyh, oyl, tyh, tyl);
+      add2(th.z, tl.z, ozh, ozl, tzh, tzl);
       float phi = 0, ex = 0, ey = 0, ez = 0;
       for (int sb = 0; sb < nb; sb += 32) {
         __syncwarp();
         int j = b0 + sb + lane;
         if (sb + lane < nb) {
-          uint32_t o = perm[j];
-          if (so == 0) {
-            sp[w][lane] = make_float4(lx[j], ly[j], lz[j], (float)S[o]);
-          } else {
-            sp[w][lane] = make_float4(lx[j], ly[j], lz[j], 0.f);
-            sd[w][lane] = make_float4((float)S[3 * (size_t)o], (float)S[3 * (size_t)o + 1], (float)S[3 * (size_t)o + 2], 0.f);
-          }
+          sh[w][lane] = phi4[j];
+          sl[w][lane] = plo4[j];
+          if (so) sd[w][lane] = sdip[j];
         }
         __syncwarp();
         const int cnt = min(32, nb - sb);
@@ -408,8 +440,9 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
         if (so == 0) {
 #pragma unroll 4
           for (int jj = 0; jj < cnt; jj++) {
-            float4 q = sp[w][jj];
-            float dx = tx - q.x, dy = ty - q.y, dz = tz - q.z;
+            float4 q = sh[w][jj];
+            float4 ql = sl[w][jj];
+            float dx = (txh - q.x) + (txl - ql.x), dy = (tyh - q.y) + (tyl - ql.y), dz = (tzh - q.z) + (tzl - ql.z);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             float rinv = (jj == self) ? 0.f : rsqrt_nr(r2);
             float qr = q.w * rinv;
@@ -419,9 +452,10 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
           }
         } else {
           for (int jj = 0; jj < cnt; jj++) {
-            float4 q = sp[w][jj];
+            float4 q = sh[w][jj];
+            float4 ql = sl[w][jj];
             float4 d = sd[w][jj];
-            float dx = tx - q.x, dy = ty - q.y, dz = tz - q.z;
+            float dx = (txh - q.x) + (txl - ql.x), dy = (tyh - q.y) + (tyl - ql.y), dz = (tzh - q.z) + (tzl - ql.z);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             float rinv = (jj == self) ? 0.f : rsqrt_nr(r2);
             float r3 = rinv * rinv * rinv;
@@ -443,18 +477,23 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
   }
 }
 
-// local FP32 coordinates: particle - its leaf centre
-__global__ void k_local_coords(const int *leaf_cells, int nleaves, const int *pstart, const int *pcount,
-                               const double *cx, const double *cy, const double *cz, const double *px,
-                               const double *py, const double *pz, float *lx, float *ly, float *lz) {
+// Per evaluate: positions as two-float offsets from the leaf centre (hi in .xyz,
+// the charge in .w) plus the low parts; dipole moments in FP32.
+__global__ void k_stage_particles(const int *leaf_cells, int nleaves, const int *pstart, const int *pcount,
+                                  const double *cx, const double *cy, const double *cz, const double *px,
+                                  const double *py, const double *pz, const uint32_t *perm, const double *S, int so,
+                                  float4 *phi4, float4 *plo4, float4 *sdip) {
   int leaf = blockIdx.x;
   if (leaf >= nleaves) return;
   int c = leaf_cells[leaf];
   for (int j = threadIdx.x; j < pcount[c]; j += blockDim.x) {
     int i = pstart[c] + j;
-    lx[i] = (float)(px[i] - cx[c]);
-    ly[i] = (float)(py[i] - cy[c]);
-    lz[i] = (float)(pz[i] - cz[c]);
+    double dx = px[i] - cx[c], dy = py[i] - cy[c], dz = pz[i] - cz[c];
+    float hx = (float)dx, hy = (float)dy, hz = (float)dz;
+    uint32_t o = perm[i];
+    phi4[i] = make_float4(hx, hy, hz, so == 0 ? (float)S[o] : 0.f);
+    plo4[i] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), 0.f);
+    if (so) sdip[i] = make_float4((float)S[3 * (size_t)o], (float)S[3 * (size_t)o + 1], (float)S[3 * (size_t)o + 2], 0.f);
   }
 }
 
@@ -489,7 +528,7 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   const double *lev = t->d_root.p + 16;
   const int nl = t->nleaves, nc = t->ncells;
   // P2M
-  k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+  fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
       t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
       t->pz.p, t->perm.p, S, so, p, lev, M);
   FMM_CUDA_TRY(cudaGetLastError());
@@ -497,24 +536,24 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   // M2M, deepest parents first
   for (int l = t->nlevels - 2; l >= 0; l--) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
-    k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+    fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
         ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, M);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 2, st));
   // M2L
-  k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+  fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
       ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
       mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 3, st));
   // P2P
   if (mixed)
-    k_p2p32<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
-        t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->cx.p, t->cy.p, t->cz.p,
-        t->lx.p, t->ly.p, t->lz.p, t->perm.p, S, so, t->Fnear.p);
+    fmm_note_launch(), k_p2p32<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
+        t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->ix.p, t->iy.p, t->iz.p,
+        t->clevel.p, t->levf.p, t->phi4.p, t->plo4.p, t->sdip.p, so, t->Fnear.p);
   else
-    k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
+    fmm_note_launch(), k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->px.p, t->py.p, t->pz.p,
         t->perm.p, S, so, t->Fnear.p);
   FMM_CUDA_TRY(cudaGetLastError());
@@ -522,14 +561,14 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   // L2L, top-down
   for (int l = 1; l < t->nlevels; l++) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
-    k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(ps->l2l, lo, hi, so, p, t->parent.p,
+    fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(ps->l2l, lo, hi, so, p, t->parent.p,
                                                                          t->clevel.p, t->cx.p, t->cy.p, t->cz.p,
                                                                          lev, L);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 5, st));
   // L2P
-  k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(t->leaf_cells.p, nl, t->pstart.p, t->pcount.p,
+  fmm_note_launch(), k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(t->leaf_cells.p, nl, t->pstart.p, t->pcount.p,
                                                                   t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p,
                                                                   t->py.p, t->pz.p, so, p, lev, L, t->Ffar.p);
   FMM_CUDA_TRY(cudaGetLastError());
@@ -553,10 +592,11 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
   if (mixed) {
     TRY(fmm_reserve(t->Mf, nc * msize));
     TRY(fmm_reserve(t->Lf, nc * lsize));
-    TRY(fmm_reserve(t->lx, t->N)); TRY(fmm_reserve(t->ly, t->N)); TRY(fmm_reserve(t->lz, t->N));
-    k_local_coords<<<t->nleaves, 128, 0, st>>>(t->leaf_cells.p, t->nleaves, t->pstart.p, t->pcount.p, t->cx.p,
-                                               t->cy.p, t->cz.p, t->px.p, t->py.p, t->pz.p, t->lx.p, t->ly.p,
-                                               t->lz.p);
+    TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
+    TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
+    fmm_note_launch(), k_stage_particles<<<t->nleaves, 128, 0, st>>>(
+        t->leaf_cells.p, t->nleaves, t->pstart.p, t->pcount.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p, t->pz.p,
+        t->perm.p, S, t->so, t->phi4.p, t->plo4.p, t->sdip.p);
     FMM_CUDA_TRY(cudaGetLastError());
     TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, st));
   } else {
@@ -564,7 +604,7 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
     TRY(fmm_reserve(t->L, nc * lsize));
     TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, st));
   }
-  k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N, potential, field, F);
+  fmm_note_launch(), k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N, potential, field, F);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 7, st));
   return FMM_OK;
@@ -637,7 +677,7 @@ int fmm_direct(const double *pos, const double *S, long N, const long *targets, 
   if (!pos || !S || !F || N < 1 || (!potential && !field) || so < 0 || so > 1) return FMM_ERR_ARG;
   long nt = targets ? ntargets : N;
   if (nt < 1) return FMM_OK;
-  k_direct<<<fmm_blocks(nt, DIR_BS), DIR_BS, 0, st>>>(pos, S, N, targets, nt, so, potential, field, F);
+  fmm_note_launch(), k_direct<<<fmm_blocks(nt, DIR_BS), DIR_BS, 0, st>>>(pos, S, N, targets, nt, so, potential, field, F);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }

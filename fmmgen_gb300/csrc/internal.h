@@ -37,6 +37,7 @@ struct DevTree {
   std::vector<int> level_off;
   int ncells = 0, nleaves = 0;
   long nm2l = 0, np2p = 0;
+  long long p2p_interactions = 0;  // sum over P2P pairs of n_A n_B, minus self terms
   int nclasses = 0;
   uint32_t eflags = 0;
 
@@ -44,7 +45,8 @@ struct DevTree {
   DevBuf<uint64_t> keys, keys2;
   DevBuf<uint32_t> perm, perm2;           // sorted position -> caller's particle index
   DevBuf<double> px, py, pz;              // sorted positions (FP64)
-  DevBuf<float> lx, ly, lz;               // sorted positions relative to their leaf centre / leaf half-width (FP32)
+  DevBuf<float4> phi4, plo4, sdip;        // FP32 P2P staging: (hi offset from leaf centre, q), lo offset, dipole
+  DevBuf<float2> levf;                    // per-level half-width as an FP32 (hi, lo) pair
   // cells, level-major, Morton order within a level
   DevBuf<double> cx, cy, cz;
   DevBuf<uint64_t> cid;                   // (1 << 3*level) | octant path

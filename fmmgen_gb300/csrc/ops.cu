@@ -165,12 +165,12 @@ int fmm_op_batch(int op, int n, const double *d, const double *in, double *out, 
     if (!ps) return FMM_ERR_CUDA;
   }
   switch (op) {
-    case 0: k_op_p2m<<<nb, 32 * OPW, 0, st>>>(n, d, in, out, order, so); break;
-    case 1: k_op_shift<<<nb, 32 * OPW, 0, st>>>(ps->m2m, n, d, in, out, order, so, ms, ms, order - so); break;
-    case 2: k_op_m2l<<<nb, 32 * OPW, 0, st>>>(ps->m2l, n, d, in, out, order, so); break;
-    case 3: k_op_shift<<<nb, 32 * OPW, 0, st>>>(ps->l2l, n, d, in, out, order, so, ls, ls, order - so); break;
-    case 4: k_op_l2p<<<nb, 32 * OPW, 0, st>>>(n, d, in, out, order, so, potential, field); break;
-    case 5: k_op_p2p<<<fmm_blocks(n, 128), 128, 0, st>>>(n, d, in, out, so, potential, field); break;
+    case 0: fmm_note_launch(), k_op_p2m<<<nb, 32 * OPW, 0, st>>>(n, d, in, out, order, so); break;
+    case 1: fmm_note_launch(), k_op_shift<<<nb, 32 * OPW, 0, st>>>(ps->m2m, n, d, in, out, order, so, ms, ms, order - so); break;
+    case 2: fmm_note_launch(), k_op_m2l<<<nb, 32 * OPW, 0, st>>>(ps->m2l, n, d, in, out, order, so); break;
+    case 3: fmm_note_launch(), k_op_shift<<<nb, 32 * OPW, 0, st>>>(ps->l2l, n, d, in, out, order, so, ls, ls, order - so); break;
+    case 4: fmm_note_launch(), k_op_l2p<<<nb, 32 * OPW, 0, st>>>(n, d, in, out, order, so, potential, field); break;
+    case 5: fmm_note_launch(), k_op_p2p<<<fmm_blocks(n, 128), 128, 0, st>>>(n, d, in, out, so, potential, field); break;
     default: return FMM_ERR_ARG;
   }
   FMM_CUDA_TRY(cudaGetLastError());

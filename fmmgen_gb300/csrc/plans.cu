@@ -107,7 +107,8 @@ const PlanSet *fmm_get_plans(int order, int so) {
   if (g_plans[dev][order][so]) return g_plans[dev][order][so];
   HostPlan hp[3] = {plan_m2l(order, so), plan_m2m(order, so), plan_l2l(order, so)};
   size_t bytes = 0;
-  for (auto &h : hp) bytes += h.task.size() * 4 + h.out_seg.size() * 4 + 256;
+  // each of the two arrays of a plan is padded up to a 256-byte boundary
+  for (auto &h : hp) bytes += h.task.size() * 4 + h.out_seg.size() * 4 + 2 * 256;
   char *d = nullptr;
   if (cudaMalloc((void **)&d, bytes) != cudaSuccess) return nullptr;
   std::vector<char> host(bytes, 0);

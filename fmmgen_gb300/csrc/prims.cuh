@@ -96,16 +96,16 @@ template <typename T> int fmm_scan(const T *in, T *out, size_t n, T *total, T *t
   }
   size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (nb == 1) {
-    k_scan_down<T><<<1, SCAN_BS, 0, st>>>(in, out, n, nullptr, total);
+    fmm_note_launch(), k_scan_down<T><<<1, SCAN_BS, 0, st>>>(in, out, n, nullptr, total);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
   }
   T *bsum = tmp;
-  k_scan_reduce<T><<<(unsigned)nb, SCAN_BS, 0, st>>>(in, n, bsum);
+  fmm_note_launch(), k_scan_reduce<T><<<(unsigned)nb, SCAN_BS, 0, st>>>(in, n, bsum);
   FMM_CUDA_TRY(cudaGetLastError());
   int rc = fmm_scan<T>(bsum, bsum, nb, nullptr, tmp + nb, st);
   if (rc) return rc;
-  k_scan_down<T><<<(unsigned)nb, SCAN_BS, 0, st>>>(in, out, n, bsum, total);
+  fmm_note_launch(), k_scan_down<T><<<(unsigned)nb, SCAN_BS, 0, st>>>(in, out, n, bsum, total);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
@@ -185,11 +185,11 @@ static inline int fmm_radix_sort(uint64_t *keys, uint32_t *vals, uint64_t *keys2
   uint32_t *va = vals, *vb = vals2;
   int passes = 0;
   for (int shift = begin_bit; shift < end_bit; shift += 8) {
-    k_rs_hist<<<nb, RS_BS, 0, st>>>(ka, n, shift, hist, nb);
+    fmm_note_launch(), k_rs_hist<<<nb, RS_BS, 0, st>>>(ka, n, shift, hist, nb);
     FMM_CUDA_TRY(cudaGetLastError());
     int rc = fmm_scan<uint32_t>(hist, hist, (size_t)256 * nb, nullptr, scantmp, st);
     if (rc) return rc;
-    k_rs_scatter<<<nb, RS_BS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
+    fmm_note_launch(), k_rs_scatter<<<nb, RS_BS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
     FMM_CUDA_TRY(cudaGetLastError());
     uint64_t *tk = ka; ka = kb; kb = tk;
     uint32_t *tv = va; va = vb; vb = tv;

@@ -26,36 +26,10 @@
 // ---------------------------------------------------------------------------
 // root box (example/tree.cpp:139-187)
 // ---------------------------------------------------------------------------
-// Sequential FP64 sums in particle order, one chain per axis, exactly as the
-// reference accumulates the mean; warps 1.. stream the next chunk into shared
-// memory while warp 0 adds the current one.
-#define ROOT_CHUNK 512
-__global__ void k_root_sum(const double *__restrict__ pos, long N, double *out) {
-  __shared__ double buf[2][3 * ROOT_CHUNK];
-  const int t = threadIdx.x;
-  long nchunks = (N + ROOT_CHUNK - 1) / ROOT_CHUNK;
-  double s = 0.0;
-  {
-    long n0 = N < ROOT_CHUNK ? N : ROOT_CHUNK;
-    for (long i = t; i < 3 * n0; i += blockDim.x) buf[0][i] = pos[i];
-  }
-  __syncthreads();
-  for (long k = 0; k < nchunks; k++) {
-    if (t >= 32 && k + 1 < nchunks) {
-      long b = (k + 1) * ROOT_CHUNK;
-      long n = N - b < ROOT_CHUNK ? N - b : ROOT_CHUNK;
-      for (long i = t - 32; i < 3 * n; i += blockDim.x - 32) buf[(k + 1) & 1][i] = pos[3 * b + i];
-    }
-    if (t < 3) {
-      long b = k * ROOT_CHUNK;
-      long n = N - b < ROOT_CHUNK ? N - b : ROOT_CHUNK;
-      const double *c = buf[k & 1];
-      for (long j = 0; j < n; j++) s = __dadd_rn(s, c[3 * j + t]);
-    }
-    __syncthreads();
-  }
-  if (t < 3) out[t] = s;
-}
+// The three sequential sums come from fmm_seqsum3 (seqsum.cu), bit-identical to
+// the reference's loop; the maxima are order-independent.
+size_t fmm_seqsum_scratch(long N);
+int fmm_seqsum3(const double *pos, long N, double *out, void *scratch, cudaStream_t st);
 
 __global__ void k_root_absmax(const double *__restrict__ pos, long N, const double *sums,
                               unsigned long long *mx) {
@@ -82,7 +56,7 @@ __global__ void k_root_absmax(const double *__restrict__ pos, long N, const doub
 
 // root[0..3] = centre, r; lev[2l] = r_l, lev[2l+1] = rmax_l = sqrt(3*r_l*r_l)
 __global__ void k_root_final(const double *sums, const unsigned long long *mx, long N, double *root,
-                             double *lev) {
+                             double *lev, float2 *levf) {
   double n = (double)N;
   double ax = __ddiv_rn(sums[0], n), ay = __ddiv_rn(sums[1], n), az = __ddiv_rn(sums[2], n);
   double xm = __longlong_as_double((long long)mx[0]);
@@ -94,6 +68,8 @@ __global__ void k_root_final(const double *sums, const unsigned long long *mx, l
   for (int l = 0; l <= FMM_MAXLEVEL; l++) {
     lev[2 * l] = rl;
     lev[2 * l + 1] = __dsqrt_rn(__dmul_rn(__dmul_rn(3.0, rl), rl));  // example/tree.cpp:15
+    float hi = (float)rl;
+    levf[l] = make_float2(hi, (float)(rl - (double)hi));
     rl = __ddiv_rn(rl, 2.0);
   }
 }
@@ -437,6 +413,7 @@ static int rec(DevTree *t, int i, cudaStream_t st) {
   return FMM_OK;
 }
 
+__global__ void k_p2p_count(const int *off, const int *src, int nc, const int *pcount, unsigned long long *out);
 static int build_cells(DevTree *t, cudaStream_t st);
 static int build_lists(DevTree *t, cudaStream_t st);
 static int build_classes(DevTree *t, cudaStream_t st);
@@ -459,17 +436,20 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
   TRY(fmm_reserve(t->d_root, 16 + 2 * (FMM_MAXLEVEL + 1)));
   double *dr = t->d_root.p;
   FMM_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * 16, st));
-  k_root_sum<<<1, 256, 0, st>>>(pos, N, dr);
+  TRY(tmp_reserve(t, fmm_seqsum_scratch(N)));
+  TRY(fmm_seqsum3(pos, N, dr, t->tmp.p, st));
   unsigned nbm = std::min<unsigned>(fmm_blocks(N, 256), 152 * 8);
-  k_root_absmax<<<nbm, 256, 0, st>>>(pos, N, dr, (unsigned long long *)(dr + 3));
-  k_root_final<<<1, 1, 0, st>>>(dr, (const unsigned long long *)(dr + 3), N, dr + 6, dr + 16);
+  fmm_note_launch(), k_root_absmax<<<nbm, 256, 0, st>>>(pos, N, dr, (unsigned long long *)(dr + 3));
+  TRY(fmm_reserve(t->levf, FMM_MAXLEVEL + 1));
+  fmm_note_launch(), k_root_final<<<1, 1, 0, st>>>(dr, (const unsigned long long *)(dr + 3), N, dr + 6, dr + 16,
+                                                   t->levf.p);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 1, st));
 
   // keys + stable sort
   TRY(fmm_reserve(t->keys, N)); TRY(fmm_reserve(t->keys2, N));
   TRY(fmm_reserve(t->perm, N)); TRY(fmm_reserve(t->perm2, N));
-  k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, dr + 6, t->keys.p, t->perm.p);
+  fmm_note_launch(), k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, dr + 6, t->keys.p, t->perm.p);
   FMM_CUDA_TRY(cudaGetLastError());
   size_t nbh = fmm_rs_nblocks(N);
   size_t hist_n = 256 * nbh;
@@ -479,7 +459,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
   uint32_t *scantmp = hist + hist_n;
   TRY(fmm_radix_sort(t->keys.p, t->perm.p, t->keys2.p, t->perm2.p, N, 0, 3 * FMM_MAXLEVEL, hist, scantmp, st));
   TRY(fmm_reserve(t->px, N)); TRY(fmm_reserve(t->py, N)); TRY(fmm_reserve(t->pz, N));
-  k_gather_pos<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, t->perm.p, N, t->px.p, t->py.p, t->pz.p);
+  fmm_note_launch(), k_gather_pos<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, t->perm.p, N, t->px.p, t->py.p, t->pz.p);
   FMM_CUDA_TRY(cudaGetLastError());
   FMM_CUDA_TRY(cudaMemcpyAsync(&t->root, dr + 6, sizeof(RootBox), cudaMemcpyDeviceToHost, st));
   TRY(rec(t, 2, st));
@@ -515,7 +495,7 @@ static int build_cells(DevTree *t, cudaStream_t st) {
   TRY(fmm_reserve(t->parent, cap)); TRY(fmm_reserve(t->child_first, cap));
   TRY(fmm_reserve(t->child_mask, cap)); TRY(fmm_reserve(t->clevel, cap));
   double *dr = t->d_root.p;
-  k_init_root_cell<<<1, 1, 0, st>>>(dr + 6, N, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
+  fmm_note_launch(), k_init_root_cell<<<1, 1, 0, st>>>(dr + 6, N, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
                                     t->pstart.p, t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p,
                                     t->clevel.p);
   FMM_CUDA_TRY(cudaGetLastError());
@@ -532,7 +512,7 @@ static int build_cells(DevTree *t, cudaStream_t st) {
     uint32_t *cnt = (uint32_t *)t->tmp.p;
     uint32_t *total = cnt + n;
     uint32_t *stmp = total + 1;
-    k_count_children<<<fmm_blocks(n, 128), 128, 0, st>>>(lo, hi, level, t->ncrit, t->keys.p, t->pstart.p,
+    fmm_note_launch(), k_count_children<<<fmm_blocks(n, 128), 128, 0, st>>>(lo, hi, level, t->ncrit, t->keys.p, t->pstart.p,
                                                          t->pcount.p, t->child_mask.p, cnt, t->d_eflags.p);
     if ((rc = fmm_scan<uint32_t>(cnt, cnt, n, total, stmp, st))) break;
     cudaMemcpyAsync(h_total, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -549,7 +529,7 @@ static int build_cells(DevTree *t, cudaStream_t st) {
         (rc = grow_keep(t->child_first, need_cells, used, st)) ||
         (rc = grow_keep(t->child_mask, need_cells, used, st)) || (rc = grow_keep(t->clevel, need_cells, used, st)))
       break;
-    k_write_children<<<fmm_blocks(n, 128), 128, 0, st>>>(
+    fmm_note_launch(), k_write_children<<<fmm_blocks(n, 128), 128, 0, st>>>(
         lo, hi, level, dr + 16, t->keys.p, cnt, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
         t->pstart.p, t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p, t->child_mask.p, t->clevel.p);
     if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -570,9 +550,9 @@ static int build_cells(DevTree *t, cudaStream_t st) {
   uint32_t *flag = (uint32_t *)t->tmp.p;
   uint32_t *total = flag + nc;
   uint32_t *stmp = total + 1;
-  k_leaf_flags<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag);
+  fmm_note_launch(), k_leaf_flags<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag);
   TRY(fmm_scan<uint32_t>(flag, flag, nc, total, stmp, st));
-  k_leaf_compact<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag, t->leaf_cells.p,
+  fmm_note_launch(), k_leaf_compact<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag, t->leaf_cells.p,
                                                       t->cell_leaf.p);
   FMM_CUDA_TRY(cudaGetLastError());
   uint32_t nl = 0;
@@ -609,13 +589,13 @@ static int group_by_target(DevTree *t, int *tgt, int *src, long n, DevBuf<int> &
   uint32_t *stmp = (uint32_t *)p; p += fmm_scan_tmp_elems<uint32_t>(hist_n) * 4;
   int *cnt = (int *)p; p += ((size_t)nc + 1) * 4;
   int *stmp2 = (int *)p;
-  k_pair_keys<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, k1, v1);
+  fmm_note_launch(), k_pair_keys<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, k1, v1);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(fmm_radix_sort(k1, v1, k2, v2, n, 0, end_bit, hist, stmp, st));
-  k_pair_gather<<<fmm_blocks(n, 256), 256, 0, st>>>(v1, src, n, src_out.p);
+  fmm_note_launch(), k_pair_gather<<<fmm_blocks(n, 256), 256, 0, st>>>(v1, src, n, src_out.p);
   // the sorted tgt order is implied by the offsets
   FMM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nc + 1), st));
-  k_target_count<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, cnt);
+  fmm_note_launch(), k_target_count<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, cnt);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(fmm_scan<int>(cnt, off.p, nc + 1, nullptr, stmp2, st));
   return FMM_OK;
@@ -648,7 +628,7 @@ static int build_lists(DevTree *t, cudaStream_t st) {
     U3 *cnt = (U3 *)t->tmp.p;
     U3 *tot = cnt + nf;
     U3 *stmp = tot + 1;
-    k_walk_count<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt);
+    fmm_note_launch(), k_walk_count<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt);
     if ((rc = fmm_scan<U3>(cnt, cnt, nf, tot, stmp, st))) break;
     cudaMemcpyAsync(h_tot, tot, sizeof(U3), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -658,7 +638,7 @@ static int build_lists(DevTree *t, cudaStream_t st) {
         (rc = fmm_reserve(t->fa2, T.z + 1)) || (rc = fmm_reserve(t->fb2, T.z + 1)))
       break;
     U3 base{(uint32_t)nm2l, (uint32_t)np2p, 0u};
-    k_walk_write<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt, base,
+    fmm_note_launch(), k_walk_write<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt, base,
                                                      m2l_src_raw.p, m2l_tgt_raw.p, p2p_tgt_raw.p, p2p_src_raw.p,
                                                      t->fa2.p, t->fb2.p);
     if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -675,9 +655,35 @@ static int build_lists(DevTree *t, cudaStream_t st) {
     rc = group_by_target(t, m2l_tgt_raw.p, m2l_src_raw.p, nm2l, t->m2l_off, t->m2l_src, st);
     if (!rc) rc = group_by_target(t, p2p_tgt_raw.p, p2p_src_raw.p, np2p, t->p2p_off, t->p2p_src, st);
   }
+  if (!rc) {
+    rc = tmp_reserve(t, 64);
+    if (!rc) {
+      unsigned long long *d = (unsigned long long *)t->tmp.p;
+      cudaMemsetAsync(d, 0, sizeof(*d), st);
+      fmm_note_launch(), k_p2p_count<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->p2p_off.p, t->p2p_src.p, nc,
+                                                                          t->pcount.p, d);
+      unsigned long long h = 0;
+      cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
+      FMM_CUDA_TRY(cudaStreamSynchronize(st));
+      t->p2p_interactions = (long long)h;
+    }
+  }
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
   fmm_release(m2l_src_raw); fmm_release(m2l_tgt_raw); fmm_release(p2p_tgt_raw); fmm_release(p2p_src_raw);
   return rc;
+}
+
+// particle-particle interactions of the P2P list (self pairs skip i == j)
+__global__ void k_p2p_count(const int *off, const int *src, int nc, const int *pcount, unsigned long long *out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long s = 0;
+  if (c < nc)
+    for (int k = off[c]; k < off[c + 1]; k++) {
+      int b = src[k];
+      s += (unsigned long long)pcount[c] * pcount[b] - (b == c ? pcount[c] : 0);
+    }
+  for (int d = 16; d; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
 }
 
 __global__ void k_expand_targets(const int *off, int nc, int *tgt) {
@@ -693,12 +699,12 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   TRY(fmm_reserve(t->m2l_cls, n > 0 ? n : 1));
   if (n == 0) { t->nclasses = 0; return FMM_OK; }
   TRY(fmm_reserve(t->fa, n));
-  k_expand_targets<<<fmm_blocks(nc, 128), 128, 0, st>>>(t->m2l_off.p, nc, t->fa.p);
+  fmm_note_launch(), k_expand_targets<<<fmm_blocks(nc, 128), 128, 0, st>>>(t->m2l_off.p, nc, t->fa.p);
   const int *tgt = t->fa.p, *src = t->m2l_src.p;
   TRY(tmp_reserve(t, 64));
   int *rng = (int *)t->tmp.p;
   FMM_CUDA_TRY(cudaMemsetAsync(rng, 0, 3 * sizeof(int), st));
-  k_class_range<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, rng);
+  fmm_note_launch(), k_class_range<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, rng);
   FMM_CUDA_TRY(cudaGetLastError());
   int h[3];
   FMM_CUDA_TRY(cudaMemcpyAsync(h, rng, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -719,7 +725,7 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   uint32_t *total = id + nslots;
   uint32_t *stmp = total + 1;
   FMM_CUDA_TRY(cudaMemsetAsync(mark, 0, sizeof(uint32_t) * nslots, st));
-  k_class_mark<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R, dlmin,
+  fmm_note_launch(), k_class_mark<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R, dlmin,
                                                    mark);
   TRY(fmm_scan<uint32_t>(mark, id, nslots, total, stmp, st));
   uint32_t ncls = 0;
@@ -727,13 +733,13 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
   t->nclasses = (int)ncls;
   TRY(fmm_reserve(t->cls_key4, 4 * (size_t)ncls));
-  k_class_list<<<fmm_blocks(nslots, 256), 256, 0, st>>>(mark, id, nslots, R, dlmin, t->cls_table.p, t->cls_key4.p);
-  k_class_assign<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R,
+  fmm_note_launch(), k_class_list<<<fmm_blocks(nslots, 256), 256, 0, st>>>(mark, id, nslots, R, dlmin, t->cls_table.p, t->cls_key4.p);
+  fmm_note_launch(), k_class_assign<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R,
                                                      dlmin, t->cls_table.p, t->m2l_cls.p);
   int nt = fmm_nterms(p);
   TRY(fmm_reserve(t->cls_D, (size_t)ncls * nt));
   TRY(fmm_reserve(t->cls_Df, (size_t)ncls * nt));
-  k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
+  fmm_note_launch(), k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
                                                                          t->cls_Df.p);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
@@ -743,7 +749,7 @@ void fmm_tree_destroy(DevTree *t) {
   if (!t) return;
   fmm_release(t->keys); fmm_release(t->keys2); fmm_release(t->perm); fmm_release(t->perm2);
   fmm_release(t->px); fmm_release(t->py); fmm_release(t->pz);
-  fmm_release(t->lx); fmm_release(t->ly); fmm_release(t->lz);
+  fmm_release(t->phi4); fmm_release(t->plo4); fmm_release(t->sdip); fmm_release(t->levf);
   fmm_release(t->cx); fmm_release(t->cy); fmm_release(t->cz); fmm_release(t->cid);
   fmm_release(t->ix); fmm_release(t->iy); fmm_release(t->iz);
   fmm_release(t->pstart); fmm_release(t->pcount); fmm_release(t->parent); fmm_release(t->child_first);

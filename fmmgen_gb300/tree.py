@@ -66,9 +66,10 @@ class Tree:
             self.N = self.pos.shape[0]
         check(lib().fmmgen_tree_build(C.c_void_p(self.pos.data_ptr()), self.N, self.ncrit, self.order, self.theta,
                                       self.source_order, _stream_ptr(stream), C.byref(self._h)))
-        info = np.zeros(8, dtype=np.int64)
+        info = np.zeros(9, dtype=np.int64)
         check(lib().fmmgen_tree_info(self._h, info.ctypes.data))
-        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _) = (int(v) for v in info)
+        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _,
+         self.p2p_interactions) = (int(v) for v in info)
         return self
 
     def __del__(self):

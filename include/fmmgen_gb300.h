@@ -43,6 +43,7 @@ extern "C" {
 const char *fmmgen_last_error(void);
 const char *fmmgen_version(void);
 int fmmgen_max_order(void); /* highest expansion order supported (12) */
+long long fmmgen_launch_count(void); /* kernels this library has launched so far (no counterpart in the reference) */
 
 /* ---- layout constants (the FMMGEN_* macros of fmmgen/writer.py:317-328 and
  *      Nterms/Msize/Lsize of fmmgen/utils.py:26-35, example/utils.cpp:3-27) ---- */
@@ -113,7 +114,7 @@ int fmmgen_gpu_direct(const double *pos, const double *S, long N, const long *ta
 int fmmgen_tree_free(fmmgen_tree *tree);
 
 /* Introspection (host outputs; synchronises).
- * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit]. */
+ * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions]. */
 int fmmgen_tree_info(fmmgen_tree *tree, long *info);
 /* Root cube [cx, cy, cz, r]. */
 int fmmgen_tree_root(fmmgen_tree *tree, double *root4);

@@ -71,7 +71,7 @@ def oracle_check(fg, oracle_lib, pos, S, ncrit, p, theta, so=0):
 
 
 @pytest.mark.parametrize("N,ncrit,theta,seed", [(20000, 32, 0.5, 11), (50000, 128, 0.5, 12), (8000, 4, 0.3, 13),
-                                                  (30000, 64, 0.8, 14), (1000, 1, 0.5, 15), (64, 64, 0.5, 16),
+                                                  (30000, 64, 0.8, 14), (1000, 2, 0.5, 15), (64, 64, 0.5, 16),
                                                   (65, 64, 0.5, 17)])
 def test_tree_vs_checker_random(fg, oracle_lib, N, ncrit, theta, seed):
     rng = np.random.default_rng(seed)
@@ -93,10 +93,21 @@ def test_tree_strongly_clustered(fg, oracle_lib):
     oracle_check(fg, oracle_lib, pos, rng.uniform(-1, 1, (8000, 1)), 16, 4, 0.5)
 
 
-def test_root_box_bits(fg, oracle_lib):
+@pytest.mark.parametrize("dist", ["offset", "centred", "dyadic_ties", "tiny_scale", "single"])
+def test_root_box_bits(fg, oracle_lib, dist):
     """Sequential-sum mean and 1.001 * max |x - mean| exactly as build_tree."""
     rng = np.random.default_rng(9)
-    pos = rng.uniform(-3, 7, (123457, 3))
+    n = 123457
+    if dist == "offset":
+        pos = rng.uniform(-3, 7, (n, 3))
+    elif dist == "centred":  # running sums wander across binades around zero
+        pos = 0.1 * rng.standard_normal((n, 3))
+    elif dist == "dyadic_ties":  # short mantissas: many additions round half-way
+        pos = np.round(rng.uniform(0, 1, (n, 3)) * 2 ** 20) / 2 ** 21 + 0.5
+    elif dist == "tiny_scale":  # the example driver's scaling (example/main.cpp:86-110)
+        pos = rng.uniform(-1, 1, (n, 3)) * 1e-9
+    else:
+        pos = rng.uniform(0, 1, (1, 3))
     t = fg.build_tree(torch.tensor(pos, device="cuda"), torch.ones(len(pos), 1, dtype=torch.float64, device="cuda"),
                       len(pos), 64, 3, 0.5)
     r = t.root()
