@@ -113,6 +113,19 @@ int fmmgen_gpu_direct(const double *pos, const double *S, long N, const long *ta
 
 int fmmgen_tree_free(fmmgen_tree *tree);
 
+/* Root cube of build_tree ([cx, cy, cz, r] into the device array root4),
+ * bit-identical to the one fmmgen_tree_build computes, WITHOUT allocating any
+ * device memory: no counterpart in the reference.  For callers that cannot call
+ * cudaMalloc where they need the cube (another allocator already holds the
+ * GPU's free memory, or cudaMalloc's implicit synchronisation is not
+ * acceptable).  Its scratch is one static device array of ~11 MiB held by
+ * every GPU that loads the library, enough for N <= FMMGEN_NOALLOC_MAX_N;
+ * larger N returns FMMGEN_ERR_ARG.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+#define FMMGEN_NOALLOC_MAX_N 16777216L
+int fmmgen_root_box_noalloc(const double *pos, long N, double *root4, void *stream);
+
 /* Introspection (host outputs; synchronises).
  * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions]. */
 int fmmgen_tree_info(fmmgen_tree *tree, long *info);
