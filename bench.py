@@ -47,6 +47,8 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warmup + timed steps only (no e2e, FP64, direct sum, CPU baseline): for ncu captures")
     return ap.parse_args()
 
 
@@ -254,6 +256,11 @@ def main():
         t_max = t.item()
     value = a.n * a.steps * world / (t_max / 1e3)
     ms_per_step = t_max / a.steps
+    if a.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "value": value, "unit": UNIT, "ms_per_step": ms_per_step,
+                              "gpu_launches": launches}), flush=True)
+        return
 
     # ---- e2e through the public API from pinned host memory ----
     pos_h = torch.tensor(pos_np).pin_memory()

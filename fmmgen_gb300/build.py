@@ -28,8 +28,18 @@ def _headers():
     return hs
 
 
+def _generate():
+    """(Re)write csrc/m2l_gen.cuh when its generator is newer."""
+    from . import gen_m2l
+
+    out, src = gen_m2l.OUT, os.path.abspath(gen_m2l.__file__)
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        gen_m2l.generate()
+
+
 def build(verbose=False, ptxas_verbose=False):
     os.makedirs(BUILD, exist_ok=True)
+    _generate()
     hdr_mtime = max(os.path.getmtime(h) for h in _headers())
     jobs = []
     objs = []
@@ -70,5 +80,8 @@ def build(verbose=False, ptxas_verbose=False):
 
 
 if __name__ == "__main__":
-    build(verbose="-v" in sys.argv, ptxas_verbose="--ptxas" in sys.argv)
+    sys.path.insert(0, os.path.dirname(HERE))
+    from fmmgen_gb300 import build as _b
+
+    _b.build(verbose="-v" in sys.argv, ptxas_verbose="--ptxas" in sys.argv)
     print(LIB)

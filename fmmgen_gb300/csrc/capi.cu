@@ -273,17 +273,17 @@ int fmmgen_tree_export_lists(fmmgen_tree *tree, unsigned long long *m2l, unsigne
 // M_n = M~_n s^|n|, L_n = L^_n / s^(|n|+1)
 template <typename T>
 __global__ void k_unscale(const T *Ms, const T *Ls, const unsigned char *clevel, const double *lev, int ncells,
-                          int msize, int moff, int lsize, double *Mo, double *Lo) {
+                          int msize, int moff, int lsize, int mstr, int lstr, double *Mo, double *Lo) {
   int c = blockIdx.x;
   if (c >= ncells) return;
   double s = lev[2 * clevel[c]];
   for (int j = threadIdx.x; j < msize; j += blockDim.x) {
     int d = c_mi[j + moff][3];
-    Mo[(size_t)c * msize + j] = (double)Ms[(size_t)c * msize + j] * pow(s, d);
+    Mo[(size_t)c * msize + j] = (double)Ms[(size_t)c * mstr + j] * pow(s, d);
   }
   for (int j = threadIdx.x; j < lsize; j += blockDim.x) {
     int d = c_mi[j][3];
-    Lo[(size_t)c * lsize + j] = (double)Ls[(size_t)c * lsize + j] / pow(s, d + 1);
+    Lo[(size_t)c * lsize + j] = (double)Ls[(size_t)c * lstr + j] / pow(s, d + 1);
   }
 }
 
@@ -298,9 +298,10 @@ extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, doubl
   FMM_CUDA_TRY(cudaMalloc((void **)&dM, nc * ms * sizeof(double)));
   FMM_CUDA_TRY(cudaMalloc((void **)&dL, nc * ls * sizeof(double)));
   if (tree->last_precision == FMMGEN_PREC_FP64)
-    fmm_note_launch(), k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
+    fmm_note_launch(), k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, ms, ls, dM, dL);
   else
-    fmm_note_launch(), k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, dM, dL);
+    fmm_note_launch(), k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, fmm_stride4(ms),
+                                                   fmm_stride4(ls), dM, dL);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(M, dM, nc * ms * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(L, dL, nc * ls * sizeof(double), cudaMemcpyDeviceToHost);

@@ -18,6 +18,8 @@ __host__ __device__ __forceinline__ int fmm_idx3(int nx, int ny, int nz) {
   int d = nx + ny + nz, j = d - nx;
   return fmm_nterms(d - 1) + j * (j + 1) / 2 + (j - ny);
 }
+// row length rounded up to a multiple of 4 elements (16-byte rows for FP32 float4 access)
+__host__ __device__ __forceinline__ int fmm_stride4(int n) { return (n + 3) / 4 * 4; }
 struct MI { unsigned char x, y, z, d; };
 __host__ __device__ __forceinline__ MI fmm_decode(int i) {
   int d = 0;

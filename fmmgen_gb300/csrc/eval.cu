@@ -16,6 +16,7 @@
 #include <algorithm>
 #include "internal.h"
 #include "mi_table.cuh"
+#include "m2l_gen.cuh"
 
 #define TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
 
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
                                                         const double *cx, const double *cy, const double *cz,
                                                         const double *px, const double *py, const double *pz,
                                                         const uint32_t *perm, const double *S, int so, int order,
-                                                        const double *lev, T *M) {
+                                                        const double *lev, T *M, int mstr) {
   __shared__ T tb[FMM_WARPS][3][32][FMM_PMAX + 1];
   __shared__ T sq[FMM_WARPS][32][3];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
 #pragma unroll
   for (int k = 0; k < NPL; k++) {
     int i = lane + 32 * k;
-    if (i < msize) M[(size_t)c * msize + i] = acc[k];
+    if (i < msize) M[(size_t)c * mstr + i] = acc[k];
   }
 }
 
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, 
                                                         const unsigned char *child_mask, const int *child_first,
                                                         const unsigned char *clevel, const double *cx,
                                                         const double *cy, const double *cz, const double *lev,
-                                                        T *M) {
+                                                        T *M, int mstr) {
   __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = lo + blockIdx.x * FMM_WARPS + w;
@@ -173,12 +174,12 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, 
     __syncwarp();
     warp_monomials<T>((cx[c] - cx[ch]) * inv_s, (cy[c] - cy[ch]) * inv_s, (cz[c] - cz[ch]) * inv_s, order - so,
                       sA[w], lane);
-    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)ch * msize + j] * exp2i<T>(-(int)c_mi[j + off][3]);
+    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)ch * mstr + j] * exp2i<T>(-(int)c_mi[j + off][3]);
     __syncwarp();
     engine_run<T>(P, sA[w], sB[w], sS[w], lane);
   }
   __syncwarp();
-  for (int n = lane; n < msize; n += 32) M[(size_t)c * msize + n] = engine_out<T>(P, sS[w], n);
+  for (int n = lane; n < msize; n += 32) M[(size_t)c * mstr + n] = engine_out<T>(P, sS[w], n);
 }
 
 // ---------------------------------------------------------------------------
@@ -187,7 +188,8 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, 
 template <typename T>
 __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l(Plan P, int ncells, int so, int order, const int *off_,
                                                         const int *src, const int *cls, const T *clsD,
-                                                        const unsigned char *clevel, const T *M, T *L) {
+                                                        const unsigned char *clevel, const T *M, T *L, int mstr,
+                                                        int lstr, int dstr) {
   __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int A = blockIdx.x * FMM_WARPS + w;
@@ -196,23 +198,23 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l(Plan P, int ncells, int 
   const int nt = fmm_nterms(order);
   const int k0 = off_[A], k1 = off_[A + 1];
   if (k0 == k1) {
-    for (int n = lane; n < lsize; n += 32) L[(size_t)A * lsize + n] = T(0);
+    for (int n = lane; n < lsize; n += 32) L[(size_t)A * lstr + n] = T(0);
     return;
   }
   for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
   const int la = clevel[A];
   for (int k = k0; k < k1; k++) {
     const int B = src[k];
-    const T *D = clsD + (size_t)cls[k] * nt;
+    const T *D = clsD + (size_t)cls[k] * dstr;
     const int dl = la - (int)clevel[B];  // rho = s_B / s_A = 2^(lA - lB)
     __syncwarp();
     for (int i = lane; i < nt; i += 32) sA[w][i] = D[i];
-    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)B * msize + j] * exp2i<T>(dl * (int)c_mi[j + moff][3]);
+    for (int j = lane; j < msize; j += 32) sB[w][j] = M[(size_t)B * mstr + j] * exp2i<T>(dl * (int)c_mi[j + moff][3]);
     __syncwarp();
     engine_run<T>(P, sA[w], sB[w], sS[w], lane);
   }
   __syncwarp();
-  for (int n = lane; n < lsize; n += 32) L[(size_t)A * lsize + n] = engine_out<T>(P, sS[w], n);
+  for (int n = lane; n < lsize; n += 32) L[(size_t)A * lstr + n] = engine_out<T>(P, sS[w], n);
 }
 
 // ---------------------------------------------------------------------------
@@ -222,7 +224,7 @@ template <typename T>
 __global__ void __launch_bounds__(32 * FMM_WARPS) k_l2l(Plan P, int lo, int hi, int so, int order,
                                                         const int *parent, const unsigned char *clevel,
                                                         const double *cx, const double *cy, const double *cz,
-                                                        const double *lev, T *L) {
+                                                        const double *lev, T *L, int lstr) {
   __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = lo + blockIdx.x * FMM_WARPS + w;
@@ -233,12 +235,12 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_l2l(Plan P, int lo, int hi, 
   for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
   warp_monomials<T>((cx[c] - cx[p]) * inv_s, (cy[c] - cy[p]) * inv_s, (cz[c] - cz[p]) * inv_s, order - so, sA[w],
                     lane);
-  for (int j = lane; j < lsize; j += 32) sB[w][j] = L[(size_t)p * lsize + j];
+  for (int j = lane; j < lsize; j += 32) sB[w][j] = L[(size_t)p * lstr + j];
   __syncwarp();
   engine_run<T>(P, sA[w], sB[w], sS[w], lane);
   __syncwarp();
   for (int n = lane; n < lsize; n += 32)
-    L[(size_t)c * lsize + n] += engine_out<T>(P, sS[w], n) * exp2i<T>(-((int)c_mi[n][3] + 1));
+    L[(size_t)c * lstr + n] += engine_out<T>(P, sS[w], n) * exp2i<T>(-((int)c_mi[n][3] + 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
                                                         const double *cx, const double *cy, const double *cz,
                                                         const double *px, const double *py, const double *pz,
                                                         int so, int order, const double *lev, const T *L,
-                                                        double *Ffar) {
+                                                        double *Ffar, int lstr) {
   __shared__ T sL[L2P_WARPS][FMM_NTMAX];
   __shared__ T tb[L2P_WARPS][3][FMM_PMAX + 1][33];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
   const int c = leaf_cells[leaf];
   const int pl = order - so, lsize = fmm_nterms(pl);
   const double s = lev[2 * clevel[c]], inv_s = s > 0 ? 1.0 / s : 0.0;
-  for (int j = lane; j < lsize; j += 32) sL[w][j] = s > 0 ? L[(size_t)c * lsize + j] : T(0);
+  for (int j = lane; j < lsize; j += 32) sL[w][j] = s > 0 ? L[(size_t)c * lstr + j] : T(0);
   __syncwarp();
   const int p0 = pstart[c], np = pcount[c];
   for (int base = 0; base < np; base += 32) {
@@ -294,208 +296,9 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
   }
 }
 
-// ---------------------------------------------------------------------------
-// P2P in FP64, one warp per target leaf (example/calculate.cpp:24-40, 208-216)
-// ---------------------------------------------------------------------------
-#define P2P_WARPS 4
-__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p64(const int *leaf_cells, int nleaves, const int *pstart,
-                                                          const int *pcount, const int *off_, const int *src,
-                                                          const double *px, const double *py, const double *pz,
-                                                          const uint32_t *perm, const double *S, int so,
-                                                          double *Fnear) {
-  __shared__ double sx[P2P_WARPS][32], sy[P2P_WARPS][32], sz[P2P_WARPS][32], sq[P2P_WARPS][32][3];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int leaf = blockIdx.x * P2P_WARPS + w;
-  if (leaf >= nleaves) return;
-  const int A = leaf_cells[leaf];
-  const int a0 = pstart[A], na = pcount[A];
-  const int k0 = off_[A], k1 = off_[A + 1];
-  for (int tb = 0; tb < na; tb += 32) {
-    const int i = a0 + tb + lane;
-    const bool ok = tb + lane < na;
-    double xi = 0, yi = 0, zi = 0;
-    if (ok) { xi = px[i]; yi = py[i]; zi = pz[i]; }
-    double phi = 0, ex = 0, ey = 0, ez = 0;
-    for (int k = k0; k < k1; k++) {
-      const int B = src[k];
-      const int b0 = pstart[B], nb = pcount[B];
-      for (int sb = 0; sb < nb; sb += 32) {
-        __syncwarp();
-        int j = b0 + sb + lane;
-        if (sb + lane < nb) {
-          sx[w][lane] = px[j]; sy[w][lane] = py[j]; sz[w][lane] = pz[j];
-          uint32_t o = perm[j];
-          if (so == 0) sq[w][lane][0] = S[o];
-          else { sq[w][lane][0] = S[3 * (size_t)o]; sq[w][lane][1] = S[3 * (size_t)o + 1]; sq[w][lane][2] = S[3 * (size_t)o + 2]; }
-        }
-        __syncwarp();
-        const int cnt = min(32, nb - sb);
-        if (ok) {
-          for (int jj = 0; jj < cnt; jj++) {
-            if (b0 + sb + jj == i) continue;  // l2 != l1
-            double dx = xi - sx[w][jj], dy = yi - sy[w][jj], dz = zi - sz[w][jj];
-            double r2 = dx * dx + dy * dy + dz * dz;
-            double rinv = rsqrt(r2);
-            double r3 = rinv * rinv * rinv;
-            if (so == 0) {
-              double q = sq[w][jj][0];
-              phi += q * rinv;
-              double qr3 = q * r3;
-              ex += qr3 * dx; ey += qr3 * dy; ez += qr3 * dz;
-            } else {
-              double sxj = sq[w][jj][0], syj = sq[w][jj][1], szj = sq[w][jj][2];
-              double sr = sxj * dx + syj * dy + szj * dz;
-              double r5 = 3.0 * sr * r3 * rinv * rinv;
-              phi -= sr * r3;
-              ex += sxj * r3 - r5 * dx; ey += syj * r3 - r5 * dy; ez += szj * r3 - r5 * dz;
-            }
-          }
-        }
-      }
-    }
-    if (ok) {
-      Fnear[4 * (size_t)i] = phi; Fnear[4 * (size_t)i + 1] = ex;
-      Fnear[4 * (size_t)i + 2] = ey; Fnear[4 * (size_t)i + 3] = ez;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// P2P in FP32 with compensated accumulation (mixed precision)
-// ---------------------------------------------------------------------------
-// Positions are FP32 offsets from the particle's own leaf centre; the offset
-// between the two leaf centres is formed in FP64 once per leaf pair.  Each
-// source leaf's contribution is summed in FP32 (<= ncrit terms) and folded into
-// a Kahan-compensated FP32 total.  rsqrt is the hardware approximation plus
-// one Newton step.
-__device__ __forceinline__ float rsqrt_nr(float r2) {
-  float y = rsqrtf(r2);
-  return y * fmaf(-0.5f * r2 * y, y, 1.5f);
-}
-__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
-  float y = v - c;
-  float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-// Two-float leaf-pair offset: c_A - c_B = d * s_L exactly as (hi, lo), with d
-// the integer offset of the centres in half-widths of the finer level L.
-__device__ __forceinline__ void offset2(int d, float2 sc, float &hi, float &lo) {
-  float df = (float)d;
-  hi = df * sc.x;
-  lo = fmaf(df, sc.x, -hi) + df * sc.y;
-}
-// t = (a_hi + a_lo) + (o_hi + o_lo) as (hi, lo), exact two-sum on the high parts
-__device__ __forceinline__ void add2(float ah, float al, float oh, float ol, float &th, float &tl) {
-  th = ah + oh;
-  float bv = th - ah;
-  tl = ((ah - (th - bv)) + (oh - bv)) + (al + ol);
-}
-
-__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
-                                                          const int *pcount, const int *off_, const int *src,
-                                                          const int *ix, const int *iy, const int *iz,
-                                                          const unsigned char *clevel, const float2 *levf,
-                                                          const float4 *phi4, const float4 *plo4,
-                                                          const float4 *sdip, int so, double *Fnear) {
-  __shared__ float4 sh[P2P_WARPS][32], sl[P2P_WARPS][32], sd[P2P_WARPS][32];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int leaf = blockIdx.x * P2P_WARPS + w;
-  if (leaf >= nleaves) return;
-  const int A = leaf_cells[leaf];
-  const int a0 = pstart[A], na = pcount[A];
-  const int k0 = off_[A], k1 = off_[A + 1];
-  const int la = clevel[A], iax = 2 * ix[A] + 1, iay = 2 * iy[A] + 1, iaz = 2 * iz[A] + 1;
-  for (int tb = 0; tb < na; tb += 32) {
-    const int i = a0 + tb + lane;
-    const bool ok = tb + lane < na;
-    float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
-    if (ok) { th = phi4[i]; tl = plo4[i]; }
-    float s0 = 0, s1 = 0, s2 = 0, s3 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-    for (int k = k0; k < k1; k++) {
-      const int B = src[k];
-      const int b0 = pstart[B], nb = pcount[B];
-      const int lb = clevel[B], L = max(la, lb);
-      const float2 sc = levf[L];
-      float oxh, oxl, oyh, oyl, ozh, ozl;
-      offset2((iax << (L - la)) - ((2 * ix[B] + 1) << (L - lb)), sc, oxh, oxl);
-      offset2((iay << (L - la)) - ((2 * iy[B] + 1) << (L - lb)), sc, oyh, oyl);
-      offset2((iaz << (L - la)) - ((2 * iz[B] + 1) << (L - lb)), sc, ozh, ozl);
-      float txh, txl, tyh, tyl, tzh, tzl;
-      add2(th.x, tl.x, oxh, oxl, txh, txl);
-      add2(th.y, tl.y, oyh, oyl, tyh, tyl);
-      add2(th.z, tl.z, ozh, ozl, tzh, tzl);
-      float phi = 0, ex = 0, ey = 0, ez = 0;
-      for (int sb = 0; sb < nb; sb += 32) {
-        __syncwarp();
-        int j = b0 + sb + lane;
-        if (sb + lane < nb) {
-          sh[w][lane] = phi4[j];
-          sl[w][lane] = plo4[j];
-          if (so) sd[w][lane] = sdip[j];
-        }
-        __syncwarp();
-        const int cnt = min(32, nb - sb);
-        const int self = (B == A) ? (i - (b0 + sb)) : -1;  // skip l2 == l1
-        if (so == 0) {
-#pragma unroll 4
-          for (int jj = 0; jj < cnt; jj++) {
-            float4 q = sh[w][jj];
-            float4 ql = sl[w][jj];
-            float dx = (txh - q.x) + (txl - ql.x), dy = (tyh - q.y) + (tyl - ql.y), dz = (tzh - q.z) + (tzl - ql.z);
-            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            float rinv = (jj == self) ? 0.f : rsqrt_nr(r2);
-            float qr = q.w * rinv;
-            float qr3 = qr * rinv * rinv;
-            phi += qr;
-            ex = fmaf(qr3, dx, ex); ey = fmaf(qr3, dy, ey); ez = fmaf(qr3, dz, ez);
-          }
-        } else {
-          for (int jj = 0; jj < cnt; jj++) {
-            float4 q = sh[w][jj];
-            float4 ql = sl[w][jj];
-            float4 d = sd[w][jj];
-            float dx = (txh - q.x) + (txl - ql.x), dy = (tyh - q.y) + (tyl - ql.y), dz = (tzh - q.z) + (tzl - ql.z);
-            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            float rinv = (jj == self) ? 0.f : rsqrt_nr(r2);
-            float r3 = rinv * rinv * rinv;
-            float sr = fmaf(d.x, dx, fmaf(d.y, dy, d.z * dz));
-            float r5 = 3.f * sr * r3 * rinv * rinv;
-            phi -= sr * r3;
-            ex += d.x * r3 - r5 * dx; ey += d.y * r3 - r5 * dy; ez += d.z * r3 - r5 * dz;
-          }
-        }
-      }
-      kahan_add(s0, c0, phi); kahan_add(s1, c1, ex); kahan_add(s2, c2, ey); kahan_add(s3, c3, ez);
-    }
-    if (ok) {
-      Fnear[4 * (size_t)i] = (double)s0 - (double)c0;
-      Fnear[4 * (size_t)i + 1] = (double)s1 - (double)c1;
-      Fnear[4 * (size_t)i + 2] = (double)s2 - (double)c2;
-      Fnear[4 * (size_t)i + 3] = (double)s3 - (double)c3;
-    }
-  }
-}
-
-// Per evaluate: positions as two-float offsets from the leaf centre (hi in .xyz,
-// the charge in .w) plus the low parts; dipole moments in FP32.
-__global__ void k_stage_particles(const int *leaf_cells, int nleaves, const int *pstart, const int *pcount,
-                                  const double *cx, const double *cy, const double *cz, const double *px,
-                                  const double *py, const double *pz, const uint32_t *perm, const double *S, int so,
-                                  float4 *phi4, float4 *plo4, float4 *sdip) {
-  int leaf = blockIdx.x;
-  if (leaf >= nleaves) return;
-  int c = leaf_cells[leaf];
-  for (int j = threadIdx.x; j < pcount[c]; j += blockDim.x) {
-    int i = pstart[c] + j;
-    double dx = px[i] - cx[c], dy = py[i] - cy[c], dz = pz[i] - cz[c];
-    float hx = (float)dx, hy = (float)dy, hz = (float)dz;
-    uint32_t o = perm[i];
-    phi4[i] = make_float4(hx, hy, hz, so == 0 ? (float)S[o] : 0.f);
-    plo4[i] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), 0.f);
-    if (so) sdip[i] = make_float4((float)S[3 * (size_t)o], (float)S[3 * (size_t)o + 1], (float)S[3 * (size_t)o + 2], 0.f);
-  }
-}
+// P2P and the FP32 staging live in p2p.cu
+int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st);
+int fmm_stage_particles(DevTree *t, const double *S, cudaStream_t st);
 
 // F[caller index][outsize] = near + far, in FP64
 __global__ void k_finalize(const double *Fnear, const double *Ffar, const uint32_t *perm, long N, int potential,
@@ -523,54 +326,58 @@ static int rec(DevTree *t, int i, cudaStream_t st) {
 }
 
 template <typename T>
-static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, cudaStream_t st) {
+static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, int mstr, int lstr,
+                    int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so;
   const double *lev = t->d_root.p + 16;
   const int nl = t->nleaves, nc = t->ncells;
   // P2M
   fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
       t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
-      t->pz.p, t->perm.p, S, so, p, lev, M);
+      t->pz.p, t->perm.p, S, so, p, lev, M, mstr);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 1, st));
   // M2M, deepest parents first
   for (int l = t->nlevels - 2; l >= 0; l--) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
     fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, M);
+        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, M,
+        mstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 2, st));
-  // M2L
-  fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-      ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
-      mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L);
+  // M2L: register-resident generated kernels where this order has them (FP32),
+  // else the warp contraction engine
+  m2l_reg_kernel kg[4];
+  int ng = mixed ? m2l_reg_kernels(p, so, kg) : 0;
+  if (ng > 0) {
+    for (int g = 0; g < ng; g++)
+      fmm_note_launch(), kg[g]<<<fmm_blocks(nc, 128), 128, 0, st>>>(
+          nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, (const float *)t->cls_Df.p, t->clevel.p,
+          (const float *)(const void *)M, (float *)(void *)L);
+  } else {
+    fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
+        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
+        lstr, dstr);
+  }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 3, st));
   // P2P
-  if (mixed)
-    fmm_note_launch(), k_p2p32<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
-        t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->ix.p, t->iy.p, t->iz.p,
-        t->clevel.p, t->levf.p, t->phi4.p, t->plo4.p, t->sdip.p, so, t->Fnear.p);
-  else
-    fmm_note_launch(), k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
-        t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->px.p, t->py.p, t->pz.p,
-        t->perm.p, S, so, t->Fnear.p);
-  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(fmm_p2p_launch(t, mixed, S, st));
   TRY(rec(t, 4, st));
   // L2L, top-down
   for (int l = 1; l < t->nlevels; l++) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
-    fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(ps->l2l, lo, hi, so, p, t->parent.p,
-                                                                         t->clevel.p, t->cx.p, t->cy.p, t->cz.p,
-                                                                         lev, L);
+    fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        ps->l2l, lo, hi, so, p, t->parent.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, L, lstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 5, st));
   // L2P
-  fmm_note_launch(), k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(t->leaf_cells.p, nl, t->pstart.p, t->pcount.p,
-                                                                  t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p,
-                                                                  t->py.p, t->pz.p, so, p, lev, L, t->Ffar.p);
+  fmm_note_launch(), k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(
+      t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
+      t->pz.p, so, p, lev, L, t->Ffar.p, lstr);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 6, st));
   return FMM_OK;
@@ -590,19 +397,18 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
   TRY(fmm_reserve(t->Ffar, 4 * (size_t)t->N));
   TRY(rec(t, 0, st));
   if (mixed) {
-    TRY(fmm_reserve(t->Mf, nc * msize));
-    TRY(fmm_reserve(t->Lf, nc * lsize));
+    // FP32 rows padded to 16 bytes for the float4 loads of the M2L kernels
+    const int mstr = fmm_stride4((int)msize), lstr = fmm_stride4((int)lsize), dstr = fmm_stride4(fmm_nterms(p));
+    TRY(fmm_reserve(t->Mf, nc * mstr));
+    TRY(fmm_reserve(t->Lf, nc * lstr));
     TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
     TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
-    fmm_note_launch(), k_stage_particles<<<t->nleaves, 128, 0, st>>>(
-        t->leaf_cells.p, t->nleaves, t->pstart.p, t->pcount.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p, t->pz.p,
-        t->perm.p, S, t->so, t->phi4.p, t->plo4.p, t->sdip.p);
-    FMM_CUDA_TRY(cudaGetLastError());
-    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, st));
+    TRY(fmm_stage_particles(t, S, st));
+    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, mstr, lstr, dstr, st));
   } else {
     TRY(fmm_reserve(t->M, nc * msize));
     TRY(fmm_reserve(t->L, nc * lsize));
-    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, st));
+    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, (int)msize, (int)lsize, fmm_nterms(p), st));
   }
   fmm_note_launch(), k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N, potential, field, F);
   FMM_CUDA_TRY(cudaGetLastError());

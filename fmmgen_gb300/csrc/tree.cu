@@ -381,7 +381,7 @@ __global__ void k_class_derivs(const int *key4, int ncls, int p, double *D64, fl
   int nt = fmm_nterms(p);
   for (int i = lane; i < nt; i += 32) {
     D64[(size_t)c * nt + i] = sD[w][i];
-    D32[(size_t)c * nt + i] = (float)sD[w][i];
+    D32[(size_t)c * fmm_stride4(nt) + i] = (float)sD[w][i];
   }
 }
 
@@ -738,7 +738,7 @@ static int build_classes(DevTree *t, cudaStream_t st) {
                                                      dlmin, t->cls_table.p, t->m2l_cls.p);
   int nt = fmm_nterms(p);
   TRY(fmm_reserve(t->cls_D, (size_t)ncls * nt));
-  TRY(fmm_reserve(t->cls_Df, (size_t)ncls * nt));
+  TRY(fmm_reserve(t->cls_Df, (size_t)ncls * fmm_stride4(nt)));
   fmm_note_launch(), k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
                                                                          t->cls_Df.p);
   FMM_CUDA_TRY(cudaGetLastError());
