@@ -353,7 +353,8 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   if (ng > 0) {
     for (int g = 0; g < ng; g++)
       fmm_note_launch(), kg[g]<<<fmm_blocks(nc, 128), 128, 0, st>>>(
-          nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, (const float *)t->cls_Df.p, t->clevel.p,
+          t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
+          (const float *)t->cls_Df.p, t->clevel.p,
           (const float *)(const void *)M, (float *)(void *)L);
   } else {
     fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
@@ -363,7 +364,8 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 3, st));
-  // P2P
+  // P2P (running it concurrently with M2L on a second stream was measured to
+  // give no gain: the two kernels slow each other down when co-resident)
   TRY(fmm_p2p_launch(t, mixed, S, st));
   TRY(rec(t, 4, st));
   // L2L, top-down

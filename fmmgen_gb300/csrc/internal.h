@@ -56,7 +56,8 @@ struct DevTree {
   DevBuf<int> leaf_cells;                 // leaf cell indices
   DevBuf<int> cell_leaf;                  // cell -> leaf ordinal or -1
   // interaction lists, grouped by target cell (CSR over cells)
-  DevBuf<int> m2l_off, m2l_src, m2l_cls;
+  DevBuf<int> m2l_off, m2l_src, m2l_cls;  // per target: sorted by class
+  DevBuf<int> m2l_order;                  // cells in M2L processing order (level, interaction pattern)
   DevBuf<int> p2p_off, p2p_src;
   // M2L translation classes: operator vectors D^(k)(d/s_target), |k| <= order
   DevBuf<int> cls_key4;                   // [nclasses][4]: dlev, dx, dy, dz
@@ -70,6 +71,8 @@ struct DevTree {
   DevBuf<double> Fnear, Ffar;             // [N][4] sorted order
   // scratch
   DevBuf<int> fa, fb, fa2, fb2;           // traversal frontiers
+  DevBuf<unsigned char> wdec;             // decision of each frontier pair
+  DevBuf<float> wmargin;                  // MAC band decided in FP64, per level
   DevBuf<char> tmp;                       // scan / sort / misc scratch
   DevBuf<uint32_t> d_eflags;
   DevBuf<double> d_root;                  // sums / maxima for the root box

@@ -88,10 +88,11 @@ __global__ void k_keys(const double *__restrict__ pos, long N, const double *roo
   for (int l = 0; l < FMM_MAXLEVEL; l++) {
     int oct = (x > cx) + ((y > cy) << 1) + ((z > cz) << 2);
     key = (key << 3) | (uint64_t)oct;
-    r = __ddiv_rn(r, 2.0);
-    cx = __dadd_rn(cx, __dmul_rn(r, (double)((oct & 1) * 2 - 1)));
-    cy = __dadd_rn(cy, __dmul_rn(r, (double)((oct & 2) - 1)));
-    cz = __dadd_rn(cz, __dmul_rn(r, (double)((oct & 4) / 2 - 1)));
+    // r / 2.0 and r * (+-1) are exact: halving and a sign select round identically
+    r = __dmul_rn(r, 0.5);
+    cx = __dadd_rn(cx, (oct & 1) ? r : -r);
+    cy = __dadd_rn(cy, (oct & 2) ? r : -r);
+    cz = __dadd_rn(cz, (oct & 4) ? r : -r);
   }
   keys[i] = key;
   idx[i] = (uint32_t)i;
@@ -175,9 +176,9 @@ __global__ void k_write_children(int lo, int hi, int level, const double *lev, c
     int nb = lower_digit(keys, b, e, level + 1, o + 1);
     if (nb > b) {
       // add_child (example/tree.cpp:95-98)
-      cx[j] = __dadd_rn(px, __dmul_rn(r, (double)((o & 1) * 2 - 1)));
-      cy[j] = __dadd_rn(py, __dmul_rn(r, (double)((o & 2) - 1)));
-      cz[j] = __dadd_rn(pz, __dmul_rn(r, (double)((o & 4) / 2 - 1)));
+      cx[j] = __dadd_rn(px, (o & 1) ? r : -r);
+      cy[j] = __dadd_rn(py, (o & 2) ? r : -r);
+      cz[j] = __dadd_rn(pz, (o & 4) ? r : -r);
       cid[j] = (cid[c] << 3) | (uint64_t)o;
       ix[j] = 2 * ix[c] + (o & 1);
       iy[j] = 2 * iy[c] + ((o >> 1) & 1);
@@ -213,27 +214,65 @@ struct WalkCells {
   const double *cx, *cy, *cz, *lev;
   const unsigned char *mask, *clevel;
   const int *child_first;
+  const int *ix, *iy, *iz;
+  const float *margin;  // per finer level: relative band around the MAC boundary decided in FP64
+  float theta2;
 };
 
-// 0 = M2L, 1 = P2P, 2 = split A, 3 = split B
+// The MAC  R*theta > rmax_A + rmax_B  (example/calculate.cpp:93) is first
+// evaluated on the exact integer geometry of the two cells (centres on the
+// level grid, rmax = sqrt(3)*r_level):  R^2 theta^2 / (rmax_A + rmax_B)^2 =
+// |g_A - g_B|^2 theta^2 / (3 (2^(L-lA) + 2^(L-lB))^2)  with g the doubled
+// integer coordinates at the finer level L.  Only when that ratio lies within
+// `margin` of 1 -- where the rounding of the FP64 centres can matter -- is the
+// reference's own FP64 expression evaluated, with the same roundings.
+// Returns 0 = M2L, 1 = P2P, 2 = split A, 3 = split B.
 __device__ __forceinline__ int walk_decide(const WalkCells &W, int A, int B, double theta) {
-  double dx = __dsub_rn(W.cx[A], W.cx[B]);
-  double dy = __dsub_rn(W.cy[A], W.cy[B]);
-  double dz = __dsub_rn(W.cz[A], W.cz[B]);
-  double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-  double ra = W.lev[2 * W.clevel[A] + 1], rb = W.lev[2 * W.clevel[B] + 1];
-  if (__dmul_rn(R, theta) > __dadd_rn(ra, rb)) return 0;
-  bool la = W.mask[A] == 0, lb = W.mask[B] == 0;
-  if (la && lb) return 1;  // the nleaf >= ncrit leaf-leaf branch is unreachable
-  if (lb || (ra >= rb && !la)) return 2;
+  const int la = W.clevel[A], lb = W.clevel[B], L = max(la, lb);
+  const int sa = L - la, sb = L - lb;
+  const long long gx = ((long long)(2 * W.ix[A] + 1) << sa) - ((long long)(2 * W.ix[B] + 1) << sb);
+  const long long gy = ((long long)(2 * W.iy[A] + 1) << sa) - ((long long)(2 * W.iy[B] + 1) << sb);
+  const long long gz = ((long long)(2 * W.iz[A] + 1) << sa) - ((long long)(2 * W.iz[B] + 1) << sb);
+  const long long n2 = gx * gx + gy * gy + gz * gz;
+  const long long base = (1ll << sa) + (1ll << sb);
+  const float rho = (float)n2 * W.theta2 / (3.f * (float)(base * base));
+  const float m = W.margin[L];
+  bool mac;
+  if (rho > 1.f + m) mac = true;
+  else if (rho < 1.f - m) mac = false;
+  else {
+    double dx = __dsub_rn(W.cx[A], W.cx[B]);
+    double dy = __dsub_rn(W.cy[A], W.cy[B]);
+    double dz = __dsub_rn(W.cz[A], W.cz[B]);
+    double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    double ra = W.lev[2 * la + 1], rb = W.lev[2 * lb + 1];
+    mac = __dmul_rn(R, theta) > __dadd_rn(ra, rb);
+  }
+  if (mac) return 0;
+  bool leafa = W.mask[A] == 0, leafb = W.mask[B] == 0;
+  if (leafa && leafb) return 1;  // the nleaf >= ncrit leaf-leaf branch is unreachable
+  if (leafb || (la <= lb && !leafa)) return 2;  // rmax_A >= rmax_B  <=>  lA <= lB
   return 3;
 }
 
-__global__ void k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, U3 *cnt) {
+// margin[l] for pairs whose finer level is l: FP32 evaluation error plus a bound
+// on how far FP64 centre rounding can move R relative to the level half-width
+__global__ void k_walk_margins(const double *root, const double *lev, double theta, float *margin) {
+  int l = threadIdx.x;
+  if (l > FMM_MAXLEVEL) return;
+  double cmax = fmax(fmax(fabs(root[0]), fabs(root[1])), fabs(root[2])) + root[3];
+  double s = lev[2 * l];
+  double m = 1e-5 + 64.0 * ldexp(1.0, -52) * cmax / s * fmax(1.0, theta);
+  margin[l] = s > 0 && m < 0.01 ? (float)m : 1e30f;  // 1e30: always decide in FP64
+}
+
+__global__ void k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, U3 *cnt,
+                             unsigned char *dec) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nf) return;
   int A = fa[i], B = fb[i];
   int d = walk_decide(W, A, B, theta);
+  dec[i] = (unsigned char)d;
   U3 c{0u, 0u, 0u};
   if (d == 0) c.x = 1;
   else if (d == 1) c.y = 1;
@@ -242,13 +281,13 @@ __global__ void k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t
   cnt[i] = c;
 }
 
-__global__ void k_walk_write(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, const U3 *off,
-                             U3 base, int *m2l_src, int *m2l_tgt, int *p2p_tgt, int *p2p_src, int *na,
-                             int *nb) {
+__global__ void k_walk_write(WalkCells W, const int *fa, const int *fb, uint32_t nf, const unsigned char *dec,
+                             const U3 *off, U3 base, int *m2l_src, int *m2l_tgt, int *p2p_tgt, int *p2p_src,
+                             int *na, int *nb) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nf) return;
   int A = fa[i], B = fb[i];
-  int d = walk_decide(W, A, B, theta);
+  int d = dec[i];
   U3 o = off[i];
   if (d == 0) {
     m2l_src[base.x + o.x] = B;
@@ -321,11 +360,17 @@ __global__ void k_class_range(const int *src, const int *tgt, long n, const int 
     dlp = max(dlp, __shfl_xor_sync(0xffffffffu, dlp, d));
     dlm = max(dlm, __shfl_xor_sync(0xffffffffu, dlm, d));
   }
+  // one atomic per block: all blocks hit the same three words
+  __shared__ int sm[3];
+  if (threadIdx.x < 3) sm[threadIdx.x] = 0;
+  __syncthreads();
   if ((threadIdx.x & 31) == 0) {
-    atomicMax(&rng[0], m);
-    atomicMax(&rng[1], dlp);
-    atomicMax(&rng[2], dlm);
+    atomicMax(&sm[0], m);
+    atomicMax(&sm[1], dlp);
+    atomicMax(&sm[2], dlm);
   }
+  __syncthreads();
+  if (threadIdx.x < 3) atomicMax(&rng[threadIdx.x], sm[threadIdx.x]);
 }
 
 __device__ __forceinline__ long class_slot(int dl, int dx, int dy, int dz, int R, int dlmin) {
@@ -366,6 +411,62 @@ __global__ void k_class_assign(const int *src, const int *tgt, long n, const int
   int dl, dx, dy, dz;
   pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
   cls[i] = table[class_slot(dl, dx, dy, dz, R, dlmin)];
+}
+
+// Sorts each target's M2L list by class (warp per target, bitonic in shared
+// memory; lists longer than SORT_MAX stay in walk order) and returns a key per
+// cell: level in the top byte, then a hash of the sorted class list, so that
+// cells with the same interaction pattern can be processed side by side and
+// read the same operator rows at the same time.
+#define SORT_MAX 1024
+__global__ void k_sort_lists(const int *off, int nc, int *src, int *cls, const unsigned char *clevel,
+                             uint64_t *key, uint32_t *idx) {
+  __shared__ unsigned long long buf[FMM_WARPS][SORT_MAX];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * FMM_WARPS + w;
+  if (c >= nc) return;
+  const int k0 = off[c], n = off[c + 1] - k0;
+  const bool sorted = n > 1 && n <= SORT_MAX;
+  if (sorted) {
+    int np = 1;
+    while (np < n) np <<= 1;
+    for (int i = lane; i < np; i += 32)
+      buf[w][i] = i < n ? ((unsigned long long)(unsigned)cls[k0 + i] << 32) | (unsigned)src[k0 + i] : ~0ull;
+    __syncwarp();
+    for (int kk = 2; kk <= np; kk <<= 1)
+      for (int j = kk >> 1; j > 0; j >>= 1) {
+        for (int i = lane; i < np; i += 32) {
+          int l = i ^ j;
+          if (l > i) {
+            unsigned long long a = buf[w][i], b = buf[w][l];
+            bool up = (i & kk) == 0;
+            if ((a > b) == up) { buf[w][i] = b; buf[w][l] = a; }
+          }
+        }
+        __syncwarp();
+      }
+    for (int i = lane; i < n; i += 32) {
+      cls[k0 + i] = (int)(buf[w][i] >> 32);
+      src[k0 + i] = (int)(buf[w][i] & 0xffffffffu);
+    }
+    __syncwarp();
+  }
+  // order-dependent hash of the class list: XOR of mixed (position, class)
+  unsigned long long h = 0;
+  for (int i = lane; i < n; i += 32) {
+    unsigned long long v = sorted ? (buf[w][i] >> 32) : (unsigned long long)(unsigned)cls[k0 + i];
+    unsigned long long x = (v + 1) * 0x9E3779B97F4A7C15ull ^ ((unsigned long long)i * 0xC2B2AE3D27D4EB4Full);
+    x ^= x >> 31;
+    x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 29;
+    h ^= x;
+  }
+  for (int d = 16; d; d >>= 1) h ^= __shfl_xor_sync(0xffffffffu, h, d);
+  if (lane == 0) {
+    h ^= (unsigned long long)n * 0x94D049BB133111EBull;
+    key[c] = ((uint64_t)clevel[c] << 56) | (h >> 8);
+    idx[c] = (uint32_t)c;
+  }
 }
 
 // Operator vector of a class: D_k(d / s_A), |k| <= p, in FP64 (one warp per class).
@@ -603,7 +704,10 @@ static int group_by_target(DevTree *t, int *tgt, int *src, long n, DevBuf<int> &
 
 static int build_lists(DevTree *t, cudaStream_t st) {
   int nc = t->ncells;
-  WalkCells W{t->cx.p, t->cy.p, t->cz.p, t->d_root.p + 16, t->child_mask.p, t->clevel.p, t->child_first.p};
+  TRY(fmm_reserve(t->wmargin, FMM_MAXLEVEL + 1));
+  fmm_note_launch(), k_walk_margins<<<1, 32, 0, st>>>(t->d_root.p + 6, t->d_root.p + 16, t->theta, t->wmargin.p);
+  WalkCells W{t->cx.p, t->cy.p, t->cz.p, t->d_root.p + 16, t->child_mask.p, t->clevel.p, t->child_first.p,
+              t->ix.p, t->iy.p, t->iz.p, t->wmargin.p, (float)(t->theta * t->theta)};
   // raw (ungrouped) lists live in the frontier buffers' companions
   DevBuf<int> m2l_src_raw, m2l_tgt_raw, p2p_tgt_raw, p2p_src_raw;
   size_t cap_pairs = (size_t)nc * 64 + 1024;
@@ -628,7 +732,9 @@ static int build_lists(DevTree *t, cudaStream_t st) {
     U3 *cnt = (U3 *)t->tmp.p;
     U3 *tot = cnt + nf;
     U3 *stmp = tot + 1;
-    fmm_note_launch(), k_walk_count<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt);
+    if ((rc = fmm_reserve(t->wdec, nf))) break;
+    fmm_note_launch(), k_walk_count<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt,
+                                                                        t->wdec.p);
     if ((rc = fmm_scan<U3>(cnt, cnt, nf, tot, stmp, st))) break;
     cudaMemcpyAsync(h_tot, tot, sizeof(U3), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -638,7 +744,7 @@ static int build_lists(DevTree *t, cudaStream_t st) {
         (rc = fmm_reserve(t->fa2, T.z + 1)) || (rc = fmm_reserve(t->fb2, T.z + 1)))
       break;
     U3 base{(uint32_t)nm2l, (uint32_t)np2p, 0u};
-    fmm_note_launch(), k_walk_write<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt, base,
+    fmm_note_launch(), k_walk_write<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->wdec.p, cnt, base,
                                                      m2l_src_raw.p, m2l_tgt_raw.p, p2p_tgt_raw.p, p2p_src_raw.p,
                                                      t->fa2.p, t->fb2.p);
     if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -742,6 +848,23 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
                                                                          t->cls_Df.p);
   FMM_CUDA_TRY(cudaGetLastError());
+  // class-sorted lists and the M2L processing order (level, interaction pattern)
+  size_t nbh = fmm_rs_nblocks(nc);
+  size_t hist_n = 256 * nbh;
+  TRY(tmp_reserve(t, (size_t)nc * 24 + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 256));
+  char *q = t->tmp.p;
+  uint64_t *k1 = (uint64_t *)q; q += (size_t)nc * 8;
+  uint64_t *k2 = (uint64_t *)q; q += (size_t)nc * 8;
+  uint32_t *v1 = (uint32_t *)q; q += (size_t)nc * 4;
+  uint32_t *v2 = (uint32_t *)q; q += (size_t)nc * 4;
+  uint32_t *hist = (uint32_t *)q; q += hist_n * 4;
+  uint32_t *stmp2 = (uint32_t *)q;
+  fmm_note_launch(), k_sort_lists<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+      t->m2l_off.p, nc, t->m2l_src.p, t->m2l_cls.p, t->clevel.p, k1, v1);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(fmm_radix_sort(k1, v1, k2, v2, nc, 0, 64, hist, stmp2, st));
+  TRY(fmm_reserve(t->m2l_order, nc));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->m2l_order.p, v1, sizeof(int) * nc, cudaMemcpyDeviceToDevice, st));
   return FMM_OK;
 }
 
@@ -754,12 +877,13 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->ix); fmm_release(t->iy); fmm_release(t->iz);
   fmm_release(t->pstart); fmm_release(t->pcount); fmm_release(t->parent); fmm_release(t->child_first);
   fmm_release(t->child_mask); fmm_release(t->clevel); fmm_release(t->leaf_cells); fmm_release(t->cell_leaf);
-  fmm_release(t->m2l_off); fmm_release(t->m2l_src); fmm_release(t->m2l_cls);
+  fmm_release(t->m2l_off); fmm_release(t->m2l_src); fmm_release(t->m2l_cls); fmm_release(t->m2l_order);
   fmm_release(t->p2p_off); fmm_release(t->p2p_src);
   fmm_release(t->cls_key4); fmm_release(t->cls_D); fmm_release(t->cls_Df); fmm_release(t->cls_table);
   fmm_release(t->M); fmm_release(t->L); fmm_release(t->Mf); fmm_release(t->Lf);
   fmm_release(t->Fnear); fmm_release(t->Ffar);
   fmm_release(t->fa); fmm_release(t->fb); fmm_release(t->fa2); fmm_release(t->fb2);
+  fmm_release(t->wdec); fmm_release(t->wmargin);
   fmm_release(t->tmp); fmm_release(t->d_eflags); fmm_release(t->d_root);
   if (t->ev_ready)
     for (int i = 0; i < 16; i++) cudaEventDestroy(t->ev[i]);
