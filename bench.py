@@ -10,7 +10,10 @@ through the public API from pinned host buffers, copies included.  The plain
 FP64 GPU FMM is timed beside it, and the field error of both against an FP64
 direct sum on a 10,000-particle subset is reported.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config NAME]
+
+--config selects another configuration of the same path (10^4 charges at p=4;
+2x10^6 Plummer dipoles at p=6); the default is the headline above.
 
 Multi-GPU: the path is replicated (independent systems per rank, no collective
 on the data path); `value` is the job total.
@@ -33,23 +36,49 @@ METRIC = "particles/s full FMM, N=1M p=8 at 1e-6 rel field err: mixed/learned vs
 UNIT = "particles/s"
 
 
+# name -> (N, order, ncrit, theta, source_order, distribution, potential, field)
+CONFIGS = {
+    # the headline: 1e6 uniform charges, p=8 (Nterms=165), field output
+    "uniform_1m_p8": (1_000_000, 8, 128, 0.5, 0, "uniform", False, True),
+    # the reference's CPU-runnable case: 1e4 uniform charges, p=4, potential and field
+    "uniform_10k_p4": (10_000, 4, 64, 0.5, 0, "uniform", True, True),
+    # 2e6 dipoles in a Plummer sphere (scale 0.1, truncated at radius 1), p=6, potential and field
+    "plummer_dipole_2m_p6": (2_000_000, 6, 64, 0.5, 1, "plummer", True, True),
+}
+
+
 def args_parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--order", type=int, default=8)
-    ap.add_argument("--ncrit", type=int, default=128)
-    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="uniform_1m_p8")
+    ap.add_argument("--n", type=int, default=None, help="override the configuration's particle count")
+    ap.add_argument("--order", type=int, default=None)
+    ap.add_argument("--ncrit", type=int, default=None)
+    ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup + timed steps only (no e2e, FP64, direct sum, CPU baseline): for ncu captures")
-    return ap.parse_args()
+    a = ap.parse_args()
+    n, order, ncrit, theta, so, dist, pot, fld = CONFIGS[a.config]
+    a.n = a.n or n
+    a.order = a.order or order
+    a.ncrit = a.ncrit or ncrit
+    a.theta = a.theta or theta
+    a.so, a.dist, a.potential, a.field = so, dist, pot, fld
+    a.outsize = (1 if pot else 0) + (3 if fld else 0)
+    return a
+
+
+def metric_name(a):
+    if a.config == "uniform_1m_p8" and a.n == 1_000_000:
+        return METRIC
+    return f"particles/s full FMM, {a.config} (N={a.n})"
 
 
 def dist_env():
@@ -59,17 +88,41 @@ def dist_env():
     return rank, world, local
 
 
-def workload(n, seed):
+def plummer(rng, n, a=0.1, rmax=1.0):
+    """Plummer sphere of scale a truncated at rmax: r = a / sqrt(u^(-2/3) - 1), isotropic directions."""
+    out, have = [], 0
+    while have < n:
+        u = rng.uniform(0.0, 1.0, 2 * (n - have) + 16)
+        r = a / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        r = r[r <= rmax]
+        v = rng.standard_normal((len(r), 3))
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        out.append(v * r[:, None])
+        have += len(r)
+    return np.concatenate(out)[:n]
+
+
+def workload(a, seed):
+    """Seeded synthetic inputs of the configuration's shape (no dataset is involved)."""
     rng = np.random.default_rng(seed)
-    pos = rng.uniform(0.0, 1.0, (n, 3))
-    q = rng.uniform(-1.0, 1.0, (n, 1))
-    return pos, q
+    if a.dist == "plummer":
+        pos = plummer(rng, a.n)
+    else:
+        pos = rng.uniform(0.0, 1.0, (a.n, 3))
+    if a.so == 0:
+        S = rng.uniform(-1.0, 1.0, (a.n, 1))
+    else:
+        S = rng.standard_normal((a.n, 3))
+    return pos, S
 
 
 def config(a, world):
-    return {"workload": f"octree FMM, {a.n} uniform Coulomb charges in the unit cube, p={a.order}, "
-                        f"ncrit={a.ncrit}, theta={a.theta}, field output, tree+lists+evaluation per step",
-            "N": a.n, "order": a.order, "ncrit": a.ncrit, "theta": a.theta, "source_order": 0,
+    kind = "Coulomb charges" if a.so == 0 else "dipoles"
+    where = "uniform in the unit cube" if a.dist == "uniform" else "in a Plummer sphere (a=0.1, r<=1)"
+    out = "+".join(x for x, f in (("potential", a.potential), ("field", a.field)) if f)
+    return {"workload": f"octree FMM, {a.n} {kind} {where}, p={a.order}, ncrit={a.ncrit}, theta={a.theta}, "
+                        f"{out} output, tree+lists+evaluation per step",
+            "name": a.config, "N": a.n, "order": a.order, "ncrit": a.ncrit, "theta": a.theta, "source_order": a.so,
             "precision": "mixed (FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation)",
             "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"}
 
@@ -136,14 +189,19 @@ class ClockSampler:
 def cpu_sample(pos, q, a, stride):
     from oracle import oracle as orc
 
+    if a.n <= 100_000:
+        stride = 1  # small systems run in full
     t0 = time.perf_counter()
-    ot = orc.OracleTree(pos, q, a.ncrit, a.order, a.theta, 0)
+    ot = orc.OracleTree(pos, q, a.ncrit, a.order, a.theta, a.so)
     t_build = time.perf_counter() - t0
-    _, ph = ot.evaluate(potential=False, field=True, sample_stride=stride)
+    _, ph = ot.evaluate(potential=a.potential, field=a.field, sample_stride=stride)
     p2m, m2m, m2l, p2p, l2l, l2p = ph.tolist()
     t_full = t_build + p2m + m2m + l2l + stride * (m2l + p2p + l2p)
-    sample = (f"oracle port (C, OpenMP) on this host: full tree build, P2M, M2M, L2L; M2L, P2P, L2P on every "
-              f"{stride}-th target cell, scaled by {stride}; N={a.n}")
+    if stride == 1:
+        sample = f"oracle port (C, OpenMP) on this host: the full tree build and evaluation, N={a.n}"
+    else:
+        sample = (f"oracle port (C, OpenMP) on this host: full tree build, P2M, M2M, L2L; M2L, P2P, L2P on every "
+                  f"{stride}-th target cell, scaled by {stride}; N={a.n}")
     return a.n / t_full, t_full, sample, orc.num_threads()
 
 
@@ -154,7 +212,7 @@ def run_reference(a, rank, world):
     import subprocess as sp
 
     sp.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
-    pos, q = workload(a.n, a.seed)
+    pos, q = workload(a, a.seed)
     stride = max(a.cpu_stride, 64)
     for _ in range(a.warmup):
         cpu_sample(pos, q, a, stride)
@@ -165,9 +223,9 @@ def run_reference(a, rank, world):
         est += t_full
     wall = time.perf_counter() - t0
     value = a.n * a.steps / est
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+    line = {"impl": "reference", "metric": metric_name(a), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": 1e3 * est / a.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform)", "config": config(a, world),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config(a, world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
@@ -204,19 +262,19 @@ def main():
         if pg:
             pg.barrier()
 
-    pos_np, q_np = workload(a.n, a.seed + rank)
+    pos_np, q_np = workload(a, a.seed + rank)
     pos = torch.tensor(pos_np, device=dev)
     q = torch.tensor(q_np, device=dev)
     st = torch.cuda.current_stream()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    F = torch.empty((a.n, 3), dtype=torch.float64, device=dev)
+    F = torch.empty((a.n, a.outsize), dtype=torch.float64, device=dev)
     L = fg.lib()
 
-    tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta)
+    tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta, source_order=a.so)
 
     def step(precision="mixed"):
         tree.rebuild(pos)
-        tree.compute_field_fmm(F, potential=False, field=True, precision=precision)
+        tree.compute_field_fmm(F, potential=a.potential, field=a.field, precision=precision)
 
     phase_sum = {}
 
@@ -265,7 +323,7 @@ def main():
     # ---- e2e through the public API from pinned host memory ----
     pos_h = torch.tensor(pos_np).pin_memory()
     q_h = torch.tensor(q_np).pin_memory()
-    F_h = torch.empty((a.n, 3), dtype=torch.float64).pin_memory()
+    F_h = torch.empty((a.n, a.outsize), dtype=torch.float64).pin_memory()
     pos_d = torch.empty_like(pos)
     q_d = torch.empty_like(q)
 
@@ -273,7 +331,7 @@ def main():
         pos_d.copy_(pos_h, non_blocking=True)
         q_d.copy_(q_h, non_blocking=True)
         tree.rebuild(pos_d)
-        tree.compute_field_fmm(F, S=q_d, potential=False, field=True, precision="mixed")
+        tree.compute_field_fmm(F, S=q_d, potential=a.potential, field=a.field, precision="mixed")
         F_h.copy_(F, non_blocking=True)
 
     e2e_step()
@@ -292,7 +350,7 @@ def main():
 
     # ---- accuracy vs FP64 direct sum, and the plain FP64 GPU FMM ----
     tg = torch.arange(0, a.n, max(1, a.n // 10000), device=dev)[:10000]
-    Fd = fg.direct(pos, q, targets=tg, potential=False, field=True)
+    Fd = fg.direct(pos, q, targets=tg, source_order=a.so, potential=False, field=True)
 
     def err(Fx):
         return (torch.linalg.norm(Fx[tg] - Fd) / torch.linalg.norm(Fd)).item()
@@ -318,7 +376,7 @@ def main():
         pass
     sm_max = peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal at the max SM clock
-    p2p_flops = 20.0 * tree.p2p_interactions
+    p2p_flops = (20.0 if a.so == 0 else 38.0) * tree.p2p_interactions
     m2l_flops = 2.0 * math.comb(a.order + 6, 6) * tree.nm2l
     cand = {"P2P": (ph.get("P2P", 0.0), p2p_flops), "M2L": (ph.get("M2L", 0.0), m2l_flops)}
     dom = max(cand, key=lambda k: cand[k][0])
@@ -343,9 +401,9 @@ def main():
                     if m2l_ms > 0 and peaks.get("bf16_tflops") else None,
                     "note": "M2L runs on the FP32 pipe in this build; fraction is of the measured bf16 tensor peak"}
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+    line = {"metric": metric_name(a), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64", "data": "synthetic (seeded uniform positions and charges)",
+            "dtype": "f32+f64", "data": "synthetic (seeded positions and sources)",
             "config": config(a, world), "rel_field_err": err_mixed,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roofline, "roofline_m2l": roofline_m2l,
