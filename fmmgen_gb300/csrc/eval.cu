@@ -349,10 +349,11 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   // M2L: register-resident generated kernels where this order has them (FP32),
   // else the warp contraction engine
   m2l_reg_kernel kg[4];
-  int ng = mixed ? m2l_reg_kernels(p, so, kg) : 0;
+  int kthreads[4];
+  int ng = mixed ? m2l_reg_kernels(p, so, kg, kthreads) : 0;
   if (ng > 0) {
     for (int g = 0; g < ng; g++)
-      fmm_note_launch(), kg[g]<<<fmm_blocks(nc, 128), 128, 0, st>>>(
+      fmm_note_launch(), kg[g]<<<(nc + kthreads[g] - 1) / kthreads[g], kthreads[g], 0, st>>>(
           t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
           (const float *)t->cls_Df.p, t->clevel.p,
           (const float *)(const void *)M, (float *)(void *)L);

@@ -4,8 +4,9 @@ For a pair (B -> A) of translation class c the scaled M2L (see csrc/eval.cu) is
     L^_n += sum_m D_c[n + m] * rho^|m| * M~_m,     |n| + |m| <= p, |m| >= so
 (the contraction of fmmgen/expansions.py:144-172).  The emitted kernels give
 each thread one target cell and one group of its outputs n: the thread loops
-over the target's sources, loads the source multipole terms the group needs
-into registers (float4 loads), streams the class's derivative vector in float4
+over the target's sources, takes the source multipole terms the group needs
+into registers (the warp first stages its 32 lanes' source rows in shared
+memory with coalesced loads), streams the class's derivative vector in float4
 quads, and issues the group's multiply-adds with every index resolved at
 generation time.  Outputs are split into groups so that accumulators plus
 resident multipole terms stay within the register file; groups are chosen to
@@ -85,33 +86,47 @@ def emit_kernel(p, so, g, lo, hi):
     L = []
     L.append(f"// order {p}, source order {so}, outputs of degree {lo}..{hi}: {len(outs)} outputs, "
              f"{len(need_m)} multipole terms, {len(terms)} multiply-adds per pair")
-    L.append(f"__global__ void __launch_bounds__(128) {name}(const int *__restrict__ tgt, int ntgt, "
+    quads = sorted({j // 4 for j in need_m})
+    nq = quads[-1] + 1  # the needed terms are a prefix of the multipole row
+    # warps per block: the staging buffer (32 rows x (nq + 1) quads per warp) stays within 48 KB
+    warps = max(1, min(4, 49152 // (32 * (nq + 1) * 16)))
+    L.append(f"__global__ void __launch_bounds__({32 * warps}) {name}(const int *__restrict__ tgt, int ntgt, "
              "const int *__restrict__ off, const int *__restrict__ src, const int *__restrict__ cls, "
              "const float *__restrict__ clsD, const unsigned char *__restrict__ clevel, "
              "const float *__restrict__ M, float *__restrict__ L) {")
+    L.append(f"  __shared__ float4 sM[{warps}][32][{nq + 1}];  // per warp: the 32 lanes' source rows (+1 quad pad)")
     L.append("  const int t = blockIdx.x * blockDim.x + threadIdx.x;")
-    L.append("  if (t >= ntgt) return;")
-    L.append("  const int A = tgt ? tgt[t] : t;  // cells without sources store zeros")
+    L.append("  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;")
+    L.append("  const bool act = t < ntgt;")
+    L.append("  const int A = act ? (tgt ? tgt[t] : t) : 0;  // cells without sources store zeros")
     L.append("  const int la = clevel[A];")
+    L.append("  const int k0 = act ? off[A] : 0;")
+    L.append("  const int n = act ? off[A + 1] - k0 : 0;")
+    L.append("  int nmax = n;")
+    L.append("  for (int o = 16; o; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));")
     for oi in range(len(outs)):
         L.append(f"  float a{oi} = 0.f;")
-    L.append("  const int k1 = off[A + 1];")
-    L.append("  for (int k = off[A]; k < k1; k++) {")
-    L.append("    const int B = src[k];")
-    L.append(f"    const float *__restrict__ Dp = clsD + (size_t)cls[k] * {stride(nterms(p))};")
-    L.append(f"    const float *__restrict__ Mp = M + (size_t)B * {stride(ms)};")
-    L.append("    if (k + 1 < k1) {")
-    L.append(f"      const float *Mn = M + (size_t)src[k + 1] * {stride(ms)};")
-    L.append(f"      const float *Dn = clsD + (size_t)cls[k + 1] * {stride(nterms(p))};")
-    for q in range(0, stride(ms) * 4, 128):
-        L.append(f"      asm volatile(\"prefetch.global.L1 [%0];\" :: \"l\"((const char *)Mn + {q}));")
-    for q in range(0, stride(nterms(p)) * 4, 128):
-        L.append(f"      asm volatile(\"prefetch.global.L1 [%0];\" :: \"l\"((const char *)Dn + {q}));")
+    L.append("  for (int j = 0; j < nmax; j++) {")
+    L.append("    const bool on = j < n;")
+    L.append("    const int B = on ? src[k0 + j] : -1;")
+    L.append("    const int c = on ? cls[k0 + j] : 0;")
+    L.append("    // stage the lanes' source rows with asynchronous 16-byte copies: the warp walks the")
+    L.append(f"    // 32 x {nq} quads row after row, so each warp-wide copy covers one contiguous segment")
+    L.append("    __syncwarp();")
+    L.append("#pragma unroll 6")
+    L.append(f"    for (int i = lane; i < {32 * nq}; i += 32) {{")
+    L.append(f"      const int r = i / {nq}, q = i - r * {nq};")
+    L.append("      const int Br = __shfl_sync(0xffffffffu, B, r);")
+    L.append("      if (Br >= 0)")
+    L.append(f"        cp_async16(&sM[wq][r][q], M + (size_t)Br * {stride(ms)} + 4 * q);")
     L.append("    }")
+    L.append("    cp_async_wait_all();")
+    L.append("    __syncwarp();")
+    L.append("    if (!on) continue;")
+    L.append(f"    const float *__restrict__ Dp = clsD + (size_t)c * {stride(nterms(p))};")
     # multipole terms, scaled by rho^|m| = 2^((lA - lB)|m|)
-    quads = sorted({j // 4 for j in need_m})
     for q in quads:
-        L.append(f"    const float4 mq{q} = __ldg((const float4 *)(Mp + {4 * q}));")
+        L.append(f"    const float4 mq{q} = sM[wq][lane][{q}];")
     comp = "xyzw"
     for j in need_m:
         L.append(f"    float m{j} = mq{j // 4}.{comp[j % 4]};")
@@ -149,31 +164,41 @@ def emit_kernel(p, so, g, lo, hi):
     for oi in sorted(partial):
         L.append(f"    a{oi} += t{oi};")
     L.append("  }")
+    L.append("  if (!act) return;")
     for oi, i in enumerate(outs):
         L.append(f"  L[(size_t)A * {stride(ls)} + {i}] = a{oi};")
     L.append("}")
-    return name, "\n".join(L)
+    return name, 32 * warps, "\n".join(L)
 
 
 def generate():
     parts = ["// m2l_gen.cuh -- generated by fmmgen_gb300/gen_m2l.py; do not edit.",
              "// Register-resident FP32 M2L kernels, one thread per (target cell, output group).",
-             "#pragma once", "#include <cuda_runtime.h>", ""]
+             "#pragma once", "#include <cuda_runtime.h>", "",
+             "// 16-byte global -> shared copy that bypasses the registers (cp.async, L2 only)",
+             "static __device__ __forceinline__ void cp_async16(void *dst, const void *src) {",
+             "  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);",
+             "  asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\\n\" :: \"r\"(d), \"l\"(src) : \"memory\");",
+             "}",
+             "static __device__ __forceinline__ void cp_async_wait_all() {",
+             "  asm volatile(\"cp.async.wait_all;\\n\" ::: \"memory\");",
+             "}", ""]
     table = []
     for (p, so), groups in CONFIGS.items():
         names = []
         for g, (lo, hi) in enumerate(groups):
-            name, code = emit_kernel(p, so, g, lo, hi)
+            name, threads, code = emit_kernel(p, so, g, lo, hi)
             parts.append(code)
             parts.append("")
-            names.append(name)
+            names.append((name, threads))
         table.append((p, so, names))
     parts.append("typedef void (*m2l_reg_kernel)(const int *, int, const int *, const int *, const int *, "
                  "const float *, const unsigned char *, const float *, float *);")
-    parts.append("// kernels of the output groups for (order, source order); n = 0 when none was generated")
-    parts.append("static inline int m2l_reg_kernels(int p, int so, m2l_reg_kernel *k) {")
+    parts.append("// kernels of the output groups for (order, source order) and their block sizes;")
+    parts.append("// returns 0 when none was generated")
+    parts.append("static inline int m2l_reg_kernels(int p, int so, m2l_reg_kernel *k, int *threads) {")
     for p, so, names in table:
-        body = " ".join(f"k[{i}] = {n};" for i, n in enumerate(names))
+        body = " ".join(f"k[{i}] = {n}; threads[{i}] = {t};" for i, (n, t) in enumerate(names))
         parts.append(f"  if (p == {p} && so == {so}) {{ {body} return {len(names)}; }}")
     parts.append("  return 0;")
     parts.append("}")
