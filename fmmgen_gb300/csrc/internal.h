@@ -71,6 +71,9 @@ struct DevTree {
   DevBuf<double> Fnear, Ffar;             // [N][4] sorted order
   // scratch
   DevBuf<int> fa, fb, fa2, fb2;           // traversal frontiers
+  DevBuf<int> m2l_tgt_raw, m2l_src_raw;   // walk output in frontier order (kept between builds)
+  DevBuf<int> p2p_tgt_raw, p2p_src_raw;
+  uint32_t *h_pinned = nullptr;           // 64 pinned host bytes for count readbacks
   DevBuf<unsigned char> wdec;             // decision of each frontier pair
   DevBuf<float> wmargin;                  // MAC band decided in FP64, per level
   DevBuf<char> tmp;                       // scan / sort / misc scratch

@@ -1,5 +1,5 @@
-// prims.cuh -- device-wide exclusive scan and stable LSD radix sort (u64 keys,
-// u32 values), written for this library (no CUB/Thrust on the hot path).
+// prims.cuh -- device-wide exclusive scan and stable LSD radix sort (u32 or u64
+// keys, u32 values), written for this library (no CUB/Thrust on the hot path).
 #pragma once
 #include "common.cuh"
 
@@ -119,7 +119,7 @@ template <typename T> int fmm_scan(const T *in, T *out, size_t n, T *total, T *t
 #define RS_ROUNDS 16
 #define RS_TILE (RS_BS * RS_ROUNDS)
 
-__global__ void k_rs_hist(const uint64_t *keys, size_t n, int shift, uint32_t *hist, int nb) {
+template <typename K> __global__ void k_rs_hist(const K *keys, size_t n, int shift, uint32_t *hist, int nb) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -132,7 +132,8 @@ __global__ void k_rs_hist(const uint64_t *keys, size_t n, int shift, uint32_t *h
   hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout, uint32_t *vout,
+template <typename K>
+__global__ void k_rs_scatter(const K *kin, const uint32_t *vin, K *kout, uint32_t *vout,
                              size_t n, int shift, const uint32_t *offs, int nb) {
   __shared__ uint32_t s_run[256];
   __shared__ uint32_t s_wh[RS_BS / 32][256];
@@ -146,7 +147,7 @@ __global__ void k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t 
     __syncthreads();
     size_t i = base + (size_t)r * RS_BS + t;
     bool valid = i < n;
-    uint64_t k = 0;
+    K k = 0;
     uint32_t v = 0, d = 256;
     if (valid) { k = kin[i]; v = vin[i]; d = (uint32_t)((k >> shift) & 255u); }
     unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -176,27 +177,28 @@ __global__ void k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t 
 // (keys2, vals2) as ping-pong space; the result always ends in (keys, vals).
 // hist must hold 256 * nblocks u32, scantmp fmm_scan_tmp_elems<uint32_t>(256*nblocks).
 static inline size_t fmm_rs_nblocks(size_t n) { return (n + RS_TILE - 1) / RS_TILE; }
-static inline int fmm_radix_sort(uint64_t *keys, uint32_t *vals, uint64_t *keys2, uint32_t *vals2, size_t n,
+template <typename K>
+static inline int fmm_radix_sort(K *keys, uint32_t *vals, K *keys2, uint32_t *vals2, size_t n,
                                  int begin_bit, int end_bit, uint32_t *hist, uint32_t *scantmp,
                                  cudaStream_t st) {
   if (n <= 1) return FMM_OK;
   int nb = (int)fmm_rs_nblocks(n);
-  uint64_t *ka = keys, *kb = keys2;
+  K *ka = keys, *kb = keys2;
   uint32_t *va = vals, *vb = vals2;
   int passes = 0;
   for (int shift = begin_bit; shift < end_bit; shift += 8) {
-    fmm_note_launch(), k_rs_hist<<<nb, RS_BS, 0, st>>>(ka, n, shift, hist, nb);
+    fmm_note_launch(), k_rs_hist<K><<<nb, RS_BS, 0, st>>>(ka, n, shift, hist, nb);
     FMM_CUDA_TRY(cudaGetLastError());
     int rc = fmm_scan<uint32_t>(hist, hist, (size_t)256 * nb, nullptr, scantmp, st);
     if (rc) return rc;
-    fmm_note_launch(), k_rs_scatter<<<nb, RS_BS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
+    fmm_note_launch(), k_rs_scatter<K><<<nb, RS_BS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
     FMM_CUDA_TRY(cudaGetLastError());
-    uint64_t *tk = ka; ka = kb; kb = tk;
+    K *tk = ka; ka = kb; kb = tk;
     uint32_t *tv = va; va = vb; vb = tv;
     passes++;
   }
   if (passes & 1) {
-    FMM_CUDA_TRY(cudaMemcpyAsync(keys, ka, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+    FMM_CUDA_TRY(cudaMemcpyAsync(keys, ka, n * sizeof(K), cudaMemcpyDeviceToDevice, st));
     FMM_CUDA_TRY(cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   }
   return FMM_OK;

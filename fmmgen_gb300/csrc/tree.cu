@@ -312,19 +312,25 @@ __global__ void k_walk_write(WalkCells W, const int *fa, const int *fb, uint32_t
 // ---------------------------------------------------------------------------
 // grouping pairs by target cell
 // ---------------------------------------------------------------------------
-__global__ void k_pair_keys(const int *tgt, long n, uint64_t *keys, uint32_t *idx) {
+// sort key of a pair: target in the high bits, then (optionally) its class
+template <typename K>
+__global__ void k_pair_keys(const int *tgt, const int *cls, long n, int cbits, K *keys) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  keys[i] = (uint64_t)(uint32_t)tgt[i];
-  idx[i] = (uint32_t)i;
+  K k = (K)(uint32_t)tgt[i] << cbits;
+  if (cls) k |= (K)(uint32_t)cls[i];
+  keys[i] = k;
 }
-__global__ void k_pair_gather(const uint32_t *idx, const int *src_in, long n, int *src_out) {
+// CSR offsets of pairs sorted by target (off[c] = first pair of target c,
+// off[nc] = n), and the class of each sorted pair from the key's low bits.
+template <typename K>
+__global__ void k_csr_from_sorted(const K *keys, long n, int cbits, int nc, int *off, int *cls) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < n) src_out[i] = src_in[idx[i]];
-}
-__global__ void k_target_count(const int *tgt, long n, int *cnt) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < n) atomicAdd(&cnt[tgt[i]], 1);
+  if (i > n) return;
+  const int cur = i < n ? (int)(keys[i] >> cbits) : nc;
+  const int prev = i > 0 ? (int)(keys[i - 1] >> cbits) : -1;
+  for (int c = prev + 1; c <= cur; c++) off[c] = (int)i;
+  if (cls && i < n) cls[i] = (int)(keys[i] & (((K)1 << cbits) - 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -413,48 +419,20 @@ __global__ void k_class_assign(const int *src, const int *tgt, long n, const int
   cls[i] = table[class_slot(dl, dx, dy, dz, R, dlmin)];
 }
 
-// Sorts each target's M2L list by class (warp per target, bitonic in shared
-// memory; lists longer than SORT_MAX stay in walk order) and returns a key per
-// cell: level in the top byte, then a hash of the sorted class list, so that
-// cells with the same interaction pattern can be processed side by side and
-// read the same operator rows at the same time.
-#define SORT_MAX 1024
-__global__ void k_sort_lists(const int *off, int nc, int *src, int *cls, const unsigned char *clevel,
-                             uint64_t *key, uint32_t *idx) {
-  __shared__ unsigned long long buf[FMM_WARPS][SORT_MAX];
+// Key per cell for the M2L processing order: level in the top byte, then a
+// hash of the cell's class-sorted list, so that cells with the same
+// interaction pattern are processed side by side and read the same operator
+// rows at the same time (one warp per cell).
+__global__ void k_list_keys(const int *off, int nc, const int *cls, const unsigned char *clevel, uint64_t *key,
+                            uint32_t *idx) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * FMM_WARPS + w;
   if (c >= nc) return;
   const int k0 = off[c], n = off[c + 1] - k0;
-  const bool sorted = n > 1 && n <= SORT_MAX;
-  if (sorted) {
-    int np = 1;
-    while (np < n) np <<= 1;
-    for (int i = lane; i < np; i += 32)
-      buf[w][i] = i < n ? ((unsigned long long)(unsigned)cls[k0 + i] << 32) | (unsigned)src[k0 + i] : ~0ull;
-    __syncwarp();
-    for (int kk = 2; kk <= np; kk <<= 1)
-      for (int j = kk >> 1; j > 0; j >>= 1) {
-        for (int i = lane; i < np; i += 32) {
-          int l = i ^ j;
-          if (l > i) {
-            unsigned long long a = buf[w][i], b = buf[w][l];
-            bool up = (i & kk) == 0;
-            if ((a > b) == up) { buf[w][i] = b; buf[w][l] = a; }
-          }
-        }
-        __syncwarp();
-      }
-    for (int i = lane; i < n; i += 32) {
-      cls[k0 + i] = (int)(buf[w][i] >> 32);
-      src[k0 + i] = (int)(buf[w][i] & 0xffffffffu);
-    }
-    __syncwarp();
-  }
   // order-dependent hash of the class list: XOR of mixed (position, class)
   unsigned long long h = 0;
   for (int i = lane; i < n; i += 32) {
-    unsigned long long v = sorted ? (buf[w][i] >> 32) : (unsigned long long)(unsigned)cls[k0 + i];
+    unsigned long long v = (unsigned long long)(unsigned)cls[k0 + i];
     unsigned long long x = (v + 1) * 0x9E3779B97F4A7C15ull ^ ((unsigned long long)i * 0xC2B2AE3D27D4EB4Full);
     x ^= x >> 31;
     x *= 0xBF58476D1CE4E5B9ull;
@@ -530,6 +508,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
     for (int i = 0; i < 16; i++) FMM_CUDA_TRY(cudaEventCreate(&t->ev[i]));
     t->ev_ready = true;
   }
+  if (!t->h_pinned) FMM_CUDA_TRY(cudaMallocHost((void **)&t->h_pinned, 64));
   TRY(rec(t, 0, st));
   TRY(fmm_reserve(t->d_eflags, 4));
   FMM_CUDA_TRY(cudaMemsetAsync(t->d_eflags.p, 0, sizeof(uint32_t), st));
@@ -603,8 +582,7 @@ static int build_cells(DevTree *t, cudaStream_t st) {
   t->level_off.assign(1, 0);
   t->level_off.push_back(1);
   int lo = 0, hi = 1, level = 0;
-  uint32_t *h_total = nullptr;
-  FMM_CUDA_TRY(cudaMallocHost((void **)&h_total, sizeof(uint32_t)));
+  uint32_t *h_total = t->h_pinned;
   int rc = FMM_OK;
   while (true) {
     int n = hi - lo;
@@ -639,7 +617,6 @@ static int build_cells(DevTree *t, cudaStream_t st) {
     level++;
     t->level_off.push_back(hi);
   }
-  cudaFreeHost(h_total);
   if (rc) return rc;
   t->ncells = hi;
   t->nlevels = level + 1;
@@ -656,49 +633,59 @@ static int build_cells(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_leaf_compact<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->ncrit, t->pcount.p, flag, t->leaf_cells.p,
                                                       t->cell_leaf.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  uint32_t nl = 0;
-  FMM_CUDA_TRY(cudaMemcpyAsync(&nl, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
-  t->nleaves = (int)nl;
+  t->nleaves = (int)t->h_pinned[0];
   return FMM_OK;
 }
 
-// Sort (tgt, src) pairs by target, stably, and build the CSR offsets.
-static int group_by_target(DevTree *t, int *tgt, int *src, long n, DevBuf<int> &off, DevBuf<int> &src_out,
-                           cudaStream_t st) {
+static int bits_for(long n) {  // bits that hold the values 0..n-1
+  int b = 0;
+  while ((1L << b) < n) b++;
+  return b;
+}
+
+template <typename K>
+static int sort_pairs(DevTree *t, const int *tgt, const int *cls, int cbits, int end_bit, DevBuf<int> &src_raw,
+                      long n, DevBuf<int> &off, int *cls_out, cudaStream_t st) {
+  size_t nbh = fmm_rs_nblocks(n);
+  size_t hist_n = 256 * nbh;
+  size_t bytes = (size_t)n * (2 * sizeof(K) + 4) + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 256;
+  TRY(tmp_reserve(t, bytes));
+  char *p = t->tmp.p;
+  K *k1 = (K *)p; p += (size_t)n * sizeof(K);
+  K *k2 = (K *)p; p += (size_t)n * sizeof(K);
+  uint32_t *v2 = (uint32_t *)p; p += (size_t)n * 4;
+  uint32_t *hist = (uint32_t *)p; p += hist_n * 4;
+  uint32_t *stmp = (uint32_t *)p;
+  fmm_note_launch(), k_pair_keys<K><<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, cls, n, cbits, k1);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(fmm_radix_sort<K>(k1, (uint32_t *)src_raw.p, k2, v2, n, 0, end_bit, hist, stmp, st));
+  fmm_note_launch(), k_csr_from_sorted<K><<<fmm_blocks(n + 1, 256), 256, 0, st>>>(k1, n, cbits, t->ncells, off.p,
+                                                                                 cls_out);
+  FMM_CUDA_TRY(cudaGetLastError());
+  return FMM_OK;
+}
+
+// Sort the walk's (tgt, src) pairs by target -- and by class within a target
+// when cls is given -- stably, and build the CSR offsets.  The sort runs in
+// place on src_raw, which is then swapped into src_out.
+static int group_by_target(DevTree *t, DevBuf<int> &tgt_raw, DevBuf<int> &src_raw, const int *cls, int ncls,
+                           long n, DevBuf<int> &off, DevBuf<int> &src_out, int *cls_out, cudaStream_t st) {
   int nc = t->ncells;
   TRY(fmm_reserve(off, (size_t)nc + 1));
-  TRY(fmm_reserve(src_out, n > 0 ? n : 1));
   if (n == 0) {
+    TRY(fmm_reserve(src_out, 1));
     FMM_CUDA_TRY(cudaMemsetAsync(off.p, 0, sizeof(int) * (nc + 1), st));
     return FMM_OK;
   }
-  int bits = 1;
-  while ((1L << bits) < nc) bits++;
-  int end_bit = ((bits + 7) / 8) * 8;
-  size_t nbh = fmm_rs_nblocks(n);
-  size_t hist_n = 256 * nbh;
-  size_t bytes = (size_t)n * (8 + 4 + 8 + 4) + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 +
-                 ((size_t)nc + 1) * 4 + fmm_scan_tmp_elems<int>(nc + 1) * 4 + 256;
-  TRY(tmp_reserve(t, bytes));
-  char *p = t->tmp.p;
-  uint64_t *k1 = (uint64_t *)p; p += (size_t)n * 8;
-  uint64_t *k2 = (uint64_t *)p; p += (size_t)n * 8;
-  uint32_t *v1 = (uint32_t *)p; p += (size_t)n * 4;
-  uint32_t *v2 = (uint32_t *)p; p += (size_t)n * 4;
-  uint32_t *hist = (uint32_t *)p; p += hist_n * 4;
-  uint32_t *stmp = (uint32_t *)p; p += fmm_scan_tmp_elems<uint32_t>(hist_n) * 4;
-  int *cnt = (int *)p; p += ((size_t)nc + 1) * 4;
-  int *stmp2 = (int *)p;
-  fmm_note_launch(), k_pair_keys<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, k1, v1);
-  FMM_CUDA_TRY(cudaGetLastError());
-  TRY(fmm_radix_sort(k1, v1, k2, v2, n, 0, end_bit, hist, stmp, st));
-  fmm_note_launch(), k_pair_gather<<<fmm_blocks(n, 256), 256, 0, st>>>(v1, src, n, src_out.p);
-  // the sorted tgt order is implied by the offsets
-  FMM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nc + 1), st));
-  fmm_note_launch(), k_target_count<<<fmm_blocks(n, 256), 256, 0, st>>>(tgt, n, cnt);
-  FMM_CUDA_TRY(cudaGetLastError());
-  TRY(fmm_scan<int>(cnt, off.p, nc + 1, nullptr, stmp2, st));
+  const int cbits = cls ? bits_for(ncls) : 0;
+  const int kbits = bits_for(nc) + cbits;
+  if (kbits <= 32)
+    TRY(sort_pairs<uint32_t>(t, tgt_raw.p, cls, cbits, kbits, src_raw, n, off, cls_out, st));
+  else
+    TRY(sort_pairs<uint64_t>(t, tgt_raw.p, cls, cbits, kbits, src_raw, n, off, cls_out, st));
+  std::swap(src_raw, src_out);
   return FMM_OK;
 }
 
@@ -708,24 +695,21 @@ static int build_lists(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_walk_margins<<<1, 32, 0, st>>>(t->d_root.p + 6, t->d_root.p + 16, t->theta, t->wmargin.p);
   WalkCells W{t->cx.p, t->cy.p, t->cz.p, t->d_root.p + 16, t->child_mask.p, t->clevel.p, t->child_first.p,
               t->ix.p, t->iy.p, t->iz.p, t->wmargin.p, (float)(t->theta * t->theta)};
-  // raw (ungrouped) lists live in the frontier buffers' companions
-  DevBuf<int> m2l_src_raw, m2l_tgt_raw, p2p_tgt_raw, p2p_src_raw;
+  // raw lists in walk order; the buffers keep their capacity between builds,
+  // so a rebuild of a similar tree allocates nothing
+  DevBuf<int> &m2l_src_raw = t->m2l_src_raw, &m2l_tgt_raw = t->m2l_tgt_raw;
+  DevBuf<int> &p2p_tgt_raw = t->p2p_tgt_raw, &p2p_src_raw = t->p2p_src_raw;
   size_t cap_pairs = (size_t)nc * 64 + 1024;
   TRY(fmm_reserve(t->fa, cap_pairs)); TRY(fmm_reserve(t->fb, cap_pairs));
   TRY(fmm_reserve(t->fa2, cap_pairs)); TRY(fmm_reserve(t->fb2, cap_pairs));
+  TRY(fmm_reserve(m2l_src_raw, cap_pairs)); TRY(fmm_reserve(m2l_tgt_raw, cap_pairs));
+  TRY(fmm_reserve(p2p_tgt_raw, cap_pairs)); TRY(fmm_reserve(p2p_src_raw, cap_pairs));
   int rc = FMM_OK;
   long nm2l = 0, np2p = 0;
   uint32_t nf = 1;
-  U3 *h_tot = nullptr;
-  cudaMallocHost((void **)&h_tot, sizeof(U3));
-  int zero = 0;
-  FMM_CUDA_TRY(cudaMemcpyAsync(t->fa.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-  FMM_CUDA_TRY(cudaMemcpyAsync(t->fb.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-  if ((rc = fmm_reserve(m2l_src_raw, cap_pairs)) || (rc = fmm_reserve(m2l_tgt_raw, cap_pairs)) ||
-      (rc = fmm_reserve(p2p_tgt_raw, cap_pairs)) || (rc = fmm_reserve(p2p_src_raw, cap_pairs))) {
-    cudaFreeHost(h_tot);
-    return rc;
-  }
+  U3 *h_tot = (U3 *)t->h_pinned;
+  FMM_CUDA_TRY(cudaMemsetAsync(t->fa.p, 0, sizeof(int), st));
+  FMM_CUDA_TRY(cudaMemsetAsync(t->fb.p, 0, sizeof(int), st));
   while (nf > 0) {
     size_t need = (size_t)nf * sizeof(U3) + fmm_scan_tmp_elems<U3>(nf) * sizeof(U3) + 2 * sizeof(U3);
     if ((rc = tmp_reserve(t, need))) break;
@@ -754,29 +738,21 @@ static int build_lists(DevTree *t, cudaStream_t st) {
     std::swap(t->fa, t->fa2);
     std::swap(t->fb, t->fb2);
   }
-  cudaFreeHost(h_tot);
-  if (!rc) {
-    t->nm2l = nm2l;
-    t->np2p = np2p;
-    rc = group_by_target(t, m2l_tgt_raw.p, m2l_src_raw.p, nm2l, t->m2l_off, t->m2l_src, st);
-    if (!rc) rc = group_by_target(t, p2p_tgt_raw.p, p2p_src_raw.p, np2p, t->p2p_off, t->p2p_src, st);
-  }
-  if (!rc) {
-    rc = tmp_reserve(t, 64);
-    if (!rc) {
-      unsigned long long *d = (unsigned long long *)t->tmp.p;
-      cudaMemsetAsync(d, 0, sizeof(*d), st);
-      fmm_note_launch(), k_p2p_count<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->p2p_off.p, t->p2p_src.p, nc,
-                                                                          t->pcount.p, d);
-      unsigned long long h = 0;
-      cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
-      FMM_CUDA_TRY(cudaStreamSynchronize(st));
-      t->p2p_interactions = (long long)h;
-    }
-  }
+  if (rc) return rc;
+  // the M2L pairs stay in walk order here: build_classes groups them by
+  // (target, class) once the classes are known
+  t->nm2l = nm2l;
+  t->np2p = np2p;
+  TRY(group_by_target(t, p2p_tgt_raw, p2p_src_raw, nullptr, 0, np2p, t->p2p_off, t->p2p_src, nullptr, st));
+  TRY(tmp_reserve(t, 64));
+  unsigned long long *d = (unsigned long long *)t->tmp.p;
+  FMM_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(*d), st));
+  fmm_note_launch(), k_p2p_count<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->p2p_off.p, t->p2p_src.p, nc, t->pcount.p, d);
+  FMM_CUDA_TRY(cudaGetLastError());
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, d, sizeof(*d), cudaMemcpyDeviceToHost, st));
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
-  fmm_release(m2l_src_raw); fmm_release(m2l_tgt_raw); fmm_release(p2p_tgt_raw); fmm_release(p2p_src_raw);
-  return rc;
+  t->p2p_interactions = (long long)*(unsigned long long *)t->h_pinned;
+  return FMM_OK;
 }
 
 // particle-particle interactions of the P2P list (self pairs skip i == j)
@@ -792,28 +768,24 @@ __global__ void k_p2p_count(const int *off, const int *src, int nc, const int *p
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
 }
 
-__global__ void k_expand_targets(const int *off, int nc, int *tgt) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nc) return;
-  for (int k = off[c]; k < off[c + 1]; k++) tgt[k] = c;
-}
-
 static int build_classes(DevTree *t, cudaStream_t st) {
   long n = t->nm2l;
   int nc = t->ncells;
   int p = t->order;
   TRY(fmm_reserve(t->m2l_cls, n > 0 ? n : 1));
-  if (n == 0) { t->nclasses = 0; return FMM_OK; }
-  TRY(fmm_reserve(t->fa, n));
-  fmm_note_launch(), k_expand_targets<<<fmm_blocks(nc, 128), 128, 0, st>>>(t->m2l_off.p, nc, t->fa.p);
-  const int *tgt = t->fa.p, *src = t->m2l_src.p;
+  if (n == 0) {
+    t->nclasses = 0;
+    return group_by_target(t, t->m2l_tgt_raw, t->m2l_src_raw, nullptr, 0, 0, t->m2l_off, t->m2l_src, nullptr, st);
+  }
+  // classes of the raw (walk-order) pairs
+  const int *tgt = t->m2l_tgt_raw.p, *src = t->m2l_src_raw.p;
   TRY(tmp_reserve(t, 64));
   int *rng = (int *)t->tmp.p;
   FMM_CUDA_TRY(cudaMemsetAsync(rng, 0, 3 * sizeof(int), st));
   fmm_note_launch(), k_class_range<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, rng);
   FMM_CUDA_TRY(cudaGetLastError());
-  int h[3];
-  FMM_CUDA_TRY(cudaMemcpyAsync(h, rng, sizeof(h), cudaMemcpyDeviceToHost, st));
+  int *h = (int *)t->h_pinned;
+  FMM_CUDA_TRY(cudaMemcpyAsync(h, rng, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
   int R = h[0], dlmin = -h[2], dlmax = h[1];
   long w = 2L * R + 1;
@@ -834,37 +806,42 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_class_mark<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R, dlmin,
                                                    mark);
   TRY(fmm_scan<uint32_t>(mark, id, nslots, total, stmp, st));
-  uint32_t ncls = 0;
-  FMM_CUDA_TRY(cudaMemcpyAsync(&ncls, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  const uint32_t ncls = t->h_pinned[0];
   t->nclasses = (int)ncls;
   TRY(fmm_reserve(t->cls_key4, 4 * (size_t)ncls));
   fmm_note_launch(), k_class_list<<<fmm_blocks(nslots, 256), 256, 0, st>>>(mark, id, nslots, R, dlmin, t->cls_table.p, t->cls_key4.p);
+  // raw classes go to the (finished) walk frontier buffer
+  TRY(fmm_reserve(t->fa, n));
   fmm_note_launch(), k_class_assign<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R,
-                                                     dlmin, t->cls_table.p, t->m2l_cls.p);
+                                                     dlmin, t->cls_table.p, t->fa.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  // group by (target, class): a target has at most one source per class, so
+  // the order within a list is fully determined
+  TRY(group_by_target(t, t->m2l_tgt_raw, t->m2l_src_raw, t->fa.p, (int)ncls, n, t->m2l_off, t->m2l_src,
+                      t->m2l_cls.p, st));
   int nt = fmm_nterms(p);
   TRY(fmm_reserve(t->cls_D, (size_t)ncls * nt));
   TRY(fmm_reserve(t->cls_Df, (size_t)ncls * fmm_stride4(nt)));
   fmm_note_launch(), k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
                                                                          t->cls_Df.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  // class-sorted lists and the M2L processing order (level, interaction pattern)
+  // the M2L processing order (level, interaction pattern)
   size_t nbh = fmm_rs_nblocks(nc);
   size_t hist_n = 256 * nbh;
-  TRY(tmp_reserve(t, (size_t)nc * 24 + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 256));
+  TRY(tmp_reserve(t, (size_t)nc * 20 + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 256));
   char *q = t->tmp.p;
   uint64_t *k1 = (uint64_t *)q; q += (size_t)nc * 8;
   uint64_t *k2 = (uint64_t *)q; q += (size_t)nc * 8;
-  uint32_t *v1 = (uint32_t *)q; q += (size_t)nc * 4;
   uint32_t *v2 = (uint32_t *)q; q += (size_t)nc * 4;
   uint32_t *hist = (uint32_t *)q; q += hist_n * 4;
   uint32_t *stmp2 = (uint32_t *)q;
-  fmm_note_launch(), k_sort_lists<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-      t->m2l_off.p, nc, t->m2l_src.p, t->m2l_cls.p, t->clevel.p, k1, v1);
-  FMM_CUDA_TRY(cudaGetLastError());
-  TRY(fmm_radix_sort(k1, v1, k2, v2, nc, 0, 64, hist, stmp2, st));
   TRY(fmm_reserve(t->m2l_order, nc));
-  FMM_CUDA_TRY(cudaMemcpyAsync(t->m2l_order.p, v1, sizeof(int) * nc, cudaMemcpyDeviceToDevice, st));
+  fmm_note_launch(), k_list_keys<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+      t->m2l_off.p, nc, t->m2l_cls.p, t->clevel.p, k1, (uint32_t *)t->m2l_order.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(fmm_radix_sort<uint64_t>(k1, (uint32_t *)t->m2l_order.p, k2, v2, nc, 0, 64, hist, stmp2, st));
   return FMM_OK;
 }
 
@@ -883,8 +860,12 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->M); fmm_release(t->L); fmm_release(t->Mf); fmm_release(t->Lf);
   fmm_release(t->Fnear); fmm_release(t->Ffar);
   fmm_release(t->fa); fmm_release(t->fb); fmm_release(t->fa2); fmm_release(t->fb2);
+  fmm_release(t->m2l_tgt_raw); fmm_release(t->m2l_src_raw);
+  fmm_release(t->p2p_tgt_raw); fmm_release(t->p2p_src_raw);
   fmm_release(t->wdec); fmm_release(t->wmargin);
   fmm_release(t->tmp); fmm_release(t->d_eflags); fmm_release(t->d_root);
+  if (t->h_pinned) cudaFreeHost(t->h_pinned);
+  t->h_pinned = nullptr;
   if (t->ev_ready)
     for (int i = 0; i < 16; i++) cudaEventDestroy(t->ev[i]);
   t->ev_ready = false;
