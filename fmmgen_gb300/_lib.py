@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libfmmgen_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "fmmgen_gb300.h")
 
 OK, ERR_ARG, ERR_CUDA, ERR_DEPTH, ERR_RANGE, ERR_STATE = range(6)
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_SIMT = 0, 1, 2
 
 
 class FMMError(RuntimeError):

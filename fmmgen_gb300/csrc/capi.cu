@@ -317,6 +317,10 @@ extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, doubl
 extern "C" int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8) {
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   FMM_CUDA_TRY(cudaDeviceSynchronize());
+  if (tree->t.h_pinned && tree->t.h_pinned[FMM_PINNED_TCERR]) {
+    fmm_set_error_text("tensor-core M2L: a pipeline wait timed out");
+    return ret(FMM_ERR_CUDA);
+  }
   if (build_ms6) memcpy(build_ms6, tree->t.build_ms, sizeof(float) * 6);
   if (eval_ms8 && tree->last_precision >= 0) {
     fmm_eval_times(&tree->t);

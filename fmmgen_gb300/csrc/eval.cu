@@ -326,8 +326,8 @@ static int rec(DevTree *t, int i, cudaStream_t st) {
 }
 
 template <typename T>
-static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, int mstr, int lstr,
-                    int dstr, cudaStream_t st) {
+static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, bool tc, int mstr,
+                    int lstr, int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so;
   const double *lev = t->d_root.p + 16;
   const int nl = t->nleaves, nc = t->ncells;
@@ -346,12 +346,15 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 2, st));
-  // M2L: register-resident generated kernels where this order has them (FP32),
-  // else the warp contraction engine
+  // M2L: tensor cores (FP32 mixed pass, order <= 9), else register-resident
+  // generated kernels where this order has them (FP32), else the warp
+  // contraction engine
   m2l_reg_kernel kg[4];
   int kthreads[4];
-  int ng = mixed ? m2l_reg_kernels(p, so, kg, kthreads) : 0;
-  if (ng > 0) {
+  int ng = mixed && !tc ? m2l_reg_kernels(p, so, kg, kthreads) : 0;
+  if (tc) {
+    TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
+  } else if (ng > 0) {
     for (int g = 0; g < ng; g++)
       fmm_note_launch(), kg[g]<<<(nc + kthreads[g] - 1) / kthreads[g], kthreads[g], 0, st>>>(
           t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
@@ -389,10 +392,11 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
 int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
                       cudaStream_t st) {
   if (!t || t->ncells == 0) return FMM_ERR_STATE;
-  if (!S || !F || (!potential && !field) || precision < 0 || precision > 1) return FMM_ERR_ARG;
+  if (!S || !F || (!potential && !field) || precision < 0 || precision > 2) return FMM_ERR_ARG;
   const PlanSet *ps = fmm_get_plans(t->order, t->so);
   if (!ps) return FMM_ERR_CUDA;
-  const bool mixed = precision == 1;
+  const bool mixed = precision != 0;
+  const bool tc = precision == 1 && fmm_m2l_tc_supported(t->order, t->so);
   const int p = t->order, so = t->so;
   const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
   const size_t nc = t->ncells;
@@ -407,11 +411,11 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
     TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
     TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
     TRY(fmm_stage_particles(t, S, st));
-    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, mstr, lstr, dstr, st));
+    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, tc, mstr, lstr, dstr, st));
   } else {
     TRY(fmm_reserve(t->M, nc * msize));
     TRY(fmm_reserve(t->L, nc * lsize));
-    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, (int)msize, (int)lsize, fmm_nterms(p), st));
+    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, false, (int)msize, (int)lsize, fmm_nterms(p), st));
   }
   fmm_note_launch(), k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N, potential, field, F);
   FMM_CUDA_TRY(cudaGetLastError());

@@ -74,6 +74,13 @@ struct DevTree {
   DevBuf<int> m2l_tgt_raw, m2l_src_raw;   // walk output in frontier order (kept between builds)
   DevBuf<int> p2p_tgt_raw, p2p_src_raw;
   uint32_t *h_pinned = nullptr;           // 64 pinned host bytes for count readbacks
+#define FMM_PINNED_TCERR 12               // h_pinned word holding the last tensor-core M2L error flags
+  // tensor-core M2L operands (m2l_tc.cu)
+  DevBuf<unsigned char> tc_T;             // split, swizzled operator records per class
+  DevBuf<uint16_t> tc_Mh, tc_Ml;          // scaled, split source multipoles (FP16 bits)
+  DevBuf<int> tc_mexp;                    // per cell: scale exponent of its multipole row
+  DevBuf<uint32_t> d_tcerr;               // kernel timeout flags
+  uint64_t build_serial = 0, tc_serial = ~0ull;  // tc_T belongs to the build with this serial
   DevBuf<unsigned char> wdec;             // decision of each frontier pair
   DevBuf<float> wmargin;                  // MAC band decided in FP64, per level
   DevBuf<char> tmp;                       // scan / sort / misc scratch
@@ -91,5 +98,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
 int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
                       cudaStream_t st);
 void fmm_tree_destroy(DevTree *t);
+bool fmm_m2l_tc_supported(int p, int so);
+int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st);
 int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
                int potential, int field, double *F, cudaStream_t st);

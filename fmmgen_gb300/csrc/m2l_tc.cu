@@ -1,0 +1,681 @@
+// m2l_tc.cu -- M2L on the fifth-generation tensor cores (tcgen05, kind::f16).
+//
+// The scaled M2L of a pair (B -> A) of translation class c is
+//     L^_A[n] += sum_m T_c[m][n] M~_B[m],  T_c[m][n] = D_c[n + m] 2^(-dlev_c |m|),
+// |n| + |m| <= p, |m| >= source_order (the contraction of
+// fmmgen/expansions.py:144-172 in the scaled form of eval.cu).  For a tile of
+// 128 target cells this is a sum of GEMMs, one per class c of the union of the
+// tile's class-sorted lists:
+//     D[128 x Nout] += A_c[128 x K] * T_c[K x Nout],
+// where row i of A_c is the source multipole of target i in class c (zero when
+// the target has no source of that class).  K runs over the multipole terms in
+// chunks of 16 (one f16 MMA); since |n| <= p - |m|, a chunk whose lowest term
+// has degree d only feeds the first NT(p - d) outputs, and its MMA uses that
+// prefix as N (~2x the useful multiply-adds instead of ~9x for the square).
+//
+// FP32 accuracy from FP16 operands ("3xFP16"): each operand is brought near
+// 2^14 by an exact power-of-two scale -- per source row for A, per (class,
+// output column) for T -- and stored as hi + lo, both FP16, and each chunk
+// issues hi*hi + hi*lo + lo*hi (relative product error ~2^-22).  The tensor
+// cores' accumulator does not round to nearest, so each class step
+// accumulates in a fresh tensor-memory buffer (33 MMAs deep at p = 8) and the
+// epilogue warps multiply the step's result by the two scales and add it into
+// FP32 registers with round-to-nearest -- the per-pair partial sums of the
+// CUDA-core kernels.
+//
+// Tiles take 128 cells of one level and one octant-within-parent, parents in
+// Morton order: those cells have near-identical interaction lists, so a tile
+// visits ~1.4x the classes of one list.
+//
+// Per CTA (one per SM, persistent), 9 warps:
+//  * warps 0-7 gather the 128 source rows of each (class, 64-term K-block)
+//    step into a stage slot with cp.async, in the 128-byte swizzled K-major
+//    layout, and arrive on the slot's mbarrier when their copies land
+//    (cp.async.mbarrier.arrive); thread 0 also fetches the class's pre-split
+//    operator chunks (32-byte swizzled) with a bulk copy.  The same warps fold
+//    each finished class step out of tensor memory (warps w and w+4 take the
+//    two column halves of lane quarter w % 4) and store the tile's rows;
+//  * warp 8 allocates 512 tensor-memory columns (two accumulators) and one of
+//    its lanes issues the MMAs.
+// Stage slots and accumulators circulate through mbarriers; every wait is
+// bounded and reports a timeout through an error flag instead of hanging.
+#include <algorithm>
+#include <cstddef>
+#include <cuda_fp16.h>
+#include "internal.h"
+
+namespace {
+
+constexpr int TC_ROWS = 128;      // target cells per tile (MMA M)
+constexpr int TC_CH = 16;         // multipole terms per K chunk (one kind::f16 MMA)
+constexpr int TC_KB = 64;         // terms per K-block: one 128-byte swizzle row of FP16
+constexpr int TC_A_BYTES = TC_ROWS * 128;  // one operand half (hi or lo) of a K-block
+constexpr int TC_MAXCH = 16;      // K chunks (p <= 9: at most 14)
+constexpr int TC_MAXKB = 4;
+constexpr int TC_GATHER = 256;    // gather / epilogue threads (warps 0-7)
+constexpr int TC_THREADS = TC_GATHER + 32;
+constexpr int TC_MAXSLOTS = 4;
+constexpr int TC_ACC_COLS = 256;  // tensor-memory columns per accumulator
+constexpr int TC_EBIAS = 14;      // operands are scaled to [2^14, 2^15) in magnitude
+constexpr unsigned TC_NONE = 0xffffffffu;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+
+struct TcParams {
+  const int *order;               // cells in M2L processing order
+  int ncells, ntiles;
+  const int *off, *src, *cls;     // class-sorted M2L lists (CSR over targets)
+  const __half *Mh, *Ml;          // scaled, split source multipoles, row stride kpad
+  const int *mexp;                // per cell: row scale exponent (M~ = 2^mexp (Mh + Ml))
+  const unsigned char *T;         // per class: split, swizzled operator chunks, then column scales
+  float *L;                       // scaled local expansions (FP32), row stride lstride
+  int lstride, lsize, kpad, kch, nkb, nslots;
+  int cls_bytes, cls_scale, slot_bytes, nout;
+  int nch[TC_MAXCH];              // MMA N of each K chunk
+  int choff[TC_MAXCH + 1];        // byte offset of each chunk's (hi, lo) block in a class record
+  uint32_t *err;                  // bit 0: a gather-side wait timed out, bit 1: an MMA-side wait
+};
+
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase with the given parity to complete; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t i = 0; i < TC_WAIT_LIMIT; i++) {
+    if (mbar_try(bar, parity)) return true;
+    if (i >= 32) __nanosleep(128);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+// arrive on the mbarrier when all cp.async copies this thread issued so far have landed
+__device__ __forceinline__ void cp_arrive(uint32_t bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// make this thread's generic-proxy shared-memory writes visible to the async proxy (tensor cores)
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptors of K-major operands.  128-byte swizzle:
+// rows of 128 bytes, 8-row groups 1024 bytes apart; 32-byte swizzle: rows of
+// 32 bytes (one 8-term chunk), 8-row groups 256 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t sbo, uint32_t layout) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                           // leading byte offset (unused: K fits one swizzle row)
+  d |= (uint64_t)(sbo >> 4) << 32;                  // stride byte offset: one 8-row group
+  d |= (uint64_t)1 << 46;                           // descriptor version
+  d |= (uint64_t)layout << 61;                      // swizzle mode
+  return d;
+}
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) { return smem_desc(saddr, 1024, 2); }
+__device__ __forceinline__ uint64_t sw32_desc(uint32_t saddr) { return smem_desc(saddr, 256, 6); }
+// Instruction descriptor: kind::f16 with FP16 A and B (both K-major), FP32
+// accumulator, M = 128.
+__device__ __forceinline__ uint32_t idesc_f16(int n) {
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_ROWS >> 4) << 24);
+}
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// arrive on the mbarrier once all MMAs this thread issued so far have completed
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// 8 consecutive accumulator columns of this thread's lane (load and wait in
+// one statement, so no register is read before the load has landed)
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// x = 2^e (hi + lo) with hi, lo FP16 and |x 2^-e| in [2^14, 2^15) for the
+// largest |x| of its row or column (e from that maximum)
+__device__ __forceinline__ int scale_exp(float amax) {
+  if (!(amax > 0.f) || !isfinite(amax)) return 0;
+  return ilogbf(amax) - TC_EBIAS;
+}
+__device__ __forceinline__ void split_f16(float x, int e, __half &hi, __half &lo) {
+  const float y = ldexpf(x, -e);  // exact: a power-of-two scale
+  hi = __float2half_rn(y);
+  lo = __float2half_rn(y - __half2float(hi));
+}
+
+}  // namespace
+
+namespace {
+
+// control block placed after the stage slots
+struct TcShared {
+  alignas(16) float colf[2][TC_ACC_COLS];  // column scales 2^g of the class in each accumulator (bulk-copy
+                                           // destination: 16-byte aligned)
+  uint64_t full[TC_MAXSLOTS];   // slot filled: 256 cp.async arrivals + thread 0's expect_tx arrival
+  uint64_t empty[TC_MAXSLOTS];  // slot consumed: MMA commit
+  uint64_t accfull[2];          // class step accumulated: MMA commit
+  uint64_t accempty[2];         // accumulator folded out: 256 epilogue arrivals
+  uint64_t colfull[2];          // column scales of the class in each accumulator landed (bulk copy)
+  uint64_t drain;               // every MMA complete (before tensor memory is released)
+  int hdr[TC_MAXSLOTS];         // K-block of the slot's step; -1: end of work
+  uint32_t ch_idesc[TC_MAXCH];  // per K chunk: instruction descriptor (N of the chunk)
+  uint32_t ch_boff[TC_MAXCH];   // per K chunk: offset of its hi block in the slot's operator area, >> 4
+  uint32_t ch_nlo[TC_MAXCH];    // per K chunk: offset of its lo block from its hi block, >> 4
+  unsigned smin[2][8];          // per-warp partial minima (double-buffered)
+  uint32_t wok[2];              // outcome of a wait thread 0 did for the gather group
+  uint32_t tmem;                // tensor-memory base address
+};
+
+// the structure starts 1024-byte aligned: bulk-copy destinations need 16
+// bytes, mbarriers 8
+static_assert(offsetof(TcShared, colf) % 16 == 0 && sizeof(TcShared::colf[0]) % 16 == 0, "colf alignment");
+static_assert(offsetof(TcShared, full) % 8 == 0 && offsetof(TcShared, drain) % 8 == 0, "mbarrier alignment");
+
+__device__ __forceinline__ void gather_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// minimum over the 256 gather threads
+__device__ __forceinline__ unsigned gather_min(unsigned v, TcShared *cs, uint32_t &par) {
+  v = __reduce_min_sync(0xffffffffu, v);
+  unsigned *b = cs->smin[par & 1];
+  par++;
+  if ((threadIdx.x & 31) == 0) b[threadIdx.x >> 5] = v;
+  gather_bar();
+  unsigned m = b[0];
+#pragma unroll
+  for (int i = 1; i < 8; i++) m = min(m, b[i]);
+  return m;
+}
+
+// Thread 0 waits on the mbarrier; the outcome reaches the whole gather group
+// through the named barrier, so every gather thread takes the same branch.
+__device__ __forceinline__ bool gather_wait(uint32_t bar, uint32_t parity, TcShared *cs, uint32_t &par) {
+  uint32_t *w = &cs->wok[par & 1];
+  par++;
+  if (threadIdx.x == 0) *w = mbar_wait(bar, parity) ? 1u : 0u;
+  gather_bar();
+  return *w != 0;
+}
+
+// Add class step v's accumulator (this thread's lane, HALF columns from col0),
+// times its row scale 2^e and the class's column scales, into the FP32 running
+// sums, and hand the accumulator back to the MMA issuer.
+template <int HALF>
+__device__ __forceinline__ bool fold(float *acc, uint32_t tlane, int col0, uint32_t v, int e, uint32_t accfull0,
+                                     uint32_t accempty0, uint32_t colfull0, TcShared *cs, uint32_t &wpar) {
+  const uint32_t b = v & 1;
+  uint32_t *w = &cs->wok[wpar & 1];
+  wpar++;
+  if (threadIdx.x == 0)
+    *w = mbar_wait(colfull0 + 8 * b, (v >> 1) & 1) && mbar_wait(accfull0 + 8 * b, (v >> 1) & 1) ? 1u : 0u;
+  gather_bar();
+  if (!*w) return false;
+  tc_fence_after();
+  __syncwarp();  // tcgen05.ld is warp-collective
+  const float rowf = ldexpf(1.f, e);
+  const float *cf = cs->colf[b] + col0;
+#pragma unroll
+  for (int c0 = 0; c0 < HALF; c0 += 8) {
+    float t[8];
+    tmem_ld8(tlane + b * TC_ACC_COLS + c0, t);
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc[c0 + i] = fmaf(t[i], rowf * cf[c0 + i], acc[c0 + i]);
+  }
+  tc_fence_before();
+  mbar_arrive(accempty0 + 8 * b);
+  return true;
+}
+
+template <int NOUT>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
+  constexpr int HALF = NOUT / 2;  // accumulator columns folded by each epilogue thread
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  const uint32_t raw = su32(tc_smem);
+  const uint32_t base = (raw + 1023u) & ~1023u;  // the 128-byte swizzle pattern repeats every 1024 bytes
+  TcShared *cs = (TcShared *)(tc_smem + (base - raw) + P.nslots * P.slot_bytes);
+  const uint32_t full0 = su32(&cs->full[0]), empty0 = su32(&cs->empty[0]);
+  const uint32_t accfull0 = su32(&cs->accfull[0]), accempty0 = su32(&cs->accempty[0]);
+  const uint32_t colfull0 = su32(&cs->colfull[0]), drain = su32(&cs->drain);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid < TC_MAXCH) {
+    const int ch = tid;
+    cs->ch_idesc[ch] = ch < P.kch ? idesc_f16(P.nch[ch]) : 0u;
+    cs->ch_boff[ch] = ch < P.kch ? (uint32_t)(P.choff[ch] - P.choff[ch & ~3]) >> 4 : 0u;
+    cs->ch_nlo[ch] = ch < P.kch ? (uint32_t)P.nch[ch] * 2u : 0u;  // nch rows x 32 bytes, >> 4
+  }
+  if (tid == 0) {
+    for (int i = 0; i < P.nslots; i++) {
+      mbar_init(full0 + 8 * i, TC_GATHER + 1);
+      mbar_init(empty0 + 8 * i, 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(accfull0 + 8 * i, 1);
+      mbar_init(accempty0 + 8 * i, TC_GATHER);
+      mbar_init(colfull0 + 8 * i, 1);
+    }
+    mbar_init(drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&cs->tmem)),
+                 "r"(2 * TC_ACC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = cs->tmem;
+
+  if (warp < 8) {
+    // ---------------- gather + fold + store ----------------
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = 32 * quarter + lane;  // tile row whose list this thread walks
+    const uint32_t tlane = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(half * HALF);
+    uint32_t g = 0, u = 0, par = 0, wpar = 0;
+    bool ok = true;
+    float acc[HALF];
+    for (int tile = blockIdx.x; tile < P.ntiles && ok; tile += gridDim.x) {
+      const int rr = tile * TC_ROWS + row;
+      const int A = rr < P.ncells ? P.order[rr] : -1;
+      float *Lrow = A >= 0 ? P.L + (size_t)A * P.lstride + half * HALF : nullptr;
+      const int ncol = min(HALF, P.lsize - half * HALF);  // stored columns of this half
+      int k = 0, kend = 0;
+      if (A >= 0) {
+        k = P.off[A];
+        kend = P.off[A + 1];
+      }
+      unsigned head = k < kend ? (unsigned)P.cls[k] : TC_NONE;
+      unsigned c = gather_min(head, cs, par);
+      int e_last = 0;  // row scale exponent of the step issued last
+      if (c == TC_NONE) {  // no M2L into this tile
+        if (Lrow)
+          for (int i = 0; i < ncol; i++) Lrow[i] = 0.f;
+        continue;
+      }
+#pragma unroll
+      for (int i = 0; i < HALF; i++) acc[i] = 0.f;
+      uint32_t steps = 0;
+      while (true) {
+        const int mysrc = head == c ? P.src[k] : -1;
+        if (head == c) {
+          k++;
+          head = k < kend ? (unsigned)P.cls[k] : TC_NONE;
+        }
+        const int e_this = mysrc >= 0 ? P.mexp[mysrc] : 0;
+        const unsigned cnext = gather_min(head, cs, par);
+        for (int kb = 0; kb < P.nkb; kb++) {
+          const int slot = (int)(g % (uint32_t)P.nslots);
+          const uint32_t use = g / (uint32_t)P.nslots;
+          if (!gather_wait(empty0 + 8 * slot, (use & 1) ^ 1, cs, wpar)) { ok = false; break; }
+          const uint32_t sa = base + (uint32_t)slot * P.slot_bytes;
+          const int qn = min(8, (P.kpad - TC_KB * kb) >> 3);  // valid 16-byte chunks of the K-block
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) {
+            const int rl = 16 * half + 4 * jj + (lane >> 3), q = lane & 7;
+            const int r = 32 * quarter + rl;
+            const int s = __shfl_sync(0xffffffffu, mysrc, rl);
+            if (q < qn) {
+              const size_t e = (size_t)(s < 0 ? 0 : s) * P.kpad + TC_KB * kb + 8 * q;
+              const uint32_t o = (uint32_t)r * 128u + ((uint32_t)(q ^ (r & 7)) << 4);
+              const uint32_t nb = s < 0 ? 0u : 16u;  // zero fill: no source of this class
+              cp16(sa + o, P.Mh + e, nb);
+              cp16(sa + TC_A_BYTES + o, P.Ml + e, nb);
+            }
+          }
+          if (tid == 0) {
+            cs->hdr[slot] = kb;
+            const unsigned char *rec = P.T + (size_t)c * P.cls_bytes;
+            const uint32_t b0 = P.choff[4 * kb], b1 = P.choff[min(4 * kb + 4, P.kch)];
+            mbar_arrive_tx(full0 + 8 * slot, b1 - b0);
+            bulk_g2s(sa + 2 * TC_A_BYTES, rec + b0, b1 - b0, full0 + 8 * slot);
+            if (kb == 0) {  // the class's column scales, for the fold of this step
+              const uint32_t sc = 4u * (uint32_t)P.nout, cb = colfull0 + 8 * (u & 1);
+              fence_async_smem();  // the folds' reads of this buffer precede its overwrite
+              mbar_arrive_tx(cb, sc);
+              bulk_g2s(su32(cs->colf[u & 1]), rec + P.cls_scale, sc, cb);
+            }
+          }
+          cp_arrive(full0 + 8 * slot);
+          g++;
+        }
+        if (!ok) break;
+        // fold the previous class step while the MMAs of this one run
+        if (steps > 0 &&
+            !fold<HALF>(acc, tlane, half * HALF, u - 1, e_last, accfull0, accempty0, colfull0, cs, wpar)) {
+          ok = false;
+          break;
+        }
+        e_last = e_this;
+        steps++;
+        u++;
+        if (cnext == TC_NONE) break;
+        c = cnext;
+      }
+      if (!ok) break;
+      if (!fold<HALF>(acc, tlane, half * HALF, u - 1, e_last, accfull0, accempty0, colfull0, cs, wpar)) {
+        ok = false;
+        break;
+      }
+      if (Lrow)
+#pragma unroll
+        for (int i = 0; i < HALF; i++)
+          if (i < ncol) Lrow[i] = acc[i];
+    }
+    // end of work: one more slot carrying only the end mark
+    if (ok) {
+      const int slot = (int)(g % (uint32_t)P.nslots);
+      const uint32_t use = g / (uint32_t)P.nslots;
+      if (gather_wait(empty0 + 8 * slot, (use & 1) ^ 1, cs, wpar)) {
+        if (tid == 0) {
+          cs->hdr[slot] = -1;
+          mbar_arrive(full0 + 8 * slot);
+        }
+        mbar_arrive(full0 + 8 * slot);
+      } else {
+        ok = false;
+      }
+    }
+    cp_wait_all();
+    if (!ok && tid == 0) atomicOr(P.err, 1u);
+  } else if (lane == 0) {
+    // ---------------- MMA issue (one thread) ----------------
+    uint32_t g = 0, u = 0;
+    bool ok = true;
+    while (true) {
+      const int slot = (int)(g % (uint32_t)P.nslots);
+      if (!mbar_wait(full0 + 8 * slot, (g / (uint32_t)P.nslots) & 1)) { ok = false; break; }
+      fence_async_smem();  // the gathered rows were written by cp.async (generic proxy)
+      tc_fence_after();
+      const int kb = cs->hdr[slot];
+      if (kb < 0) break;
+      const uint32_t b = u & 1;
+      if (kb == 0) {  // a class step starts: its accumulator must have been folded out
+        if (!mbar_wait(accempty0 + 8 * b, ((u >> 1) & 1) ^ 1)) { ok = false; break; }
+        tc_fence_after();
+      }
+      // descriptors: the slot's base descriptors plus per-chunk offsets in
+      // 16-byte units (all shared addresses stay below 256 KB, so the 14-bit
+      // start-address field never carries)
+      const uint32_t sa = base + (uint32_t)slot * P.slot_bytes;
+      const uint64_t ah0 = sw128_desc(sa), al0 = sw128_desc(sa + TC_A_BYTES);
+      const uint64_t b0 = sw32_desc(sa + 2 * TC_A_BYTES);
+      const uint32_t d = tmem + b * TC_ACC_COLS;
+      const int nc = min(4, P.kch - 4 * kb);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (j < nc) {
+          const int ch = 4 * kb + j;
+          const uint32_t id = cs->ch_idesc[ch];
+          const uint64_t bh = b0 + cs->ch_boff[ch], bl = bh + cs->ch_nlo[ch];
+          const uint64_t ah = ah0 + 2 * j, al = al0 + 2 * j;  // 32 bytes along the 128-byte row
+          mma_f16(d, ah, bh, id, (kb == 0 && j == 0) ? 0u : 1u);
+          mma_f16(d, ah, bl, id, 1u);
+          mma_f16(d, al, bh, id, 1u);
+        }
+      }
+      mma_commit(empty0 + 8 * slot);
+      if (kb == P.nkb - 1) {
+        mma_commit(accfull0 + 8 * b);
+        u++;
+      }
+      g++;
+    }
+    // every MMA issued has completed before tensor memory is released
+    mma_commit(drain);
+    if (!mbar_wait(drain, 0)) ok = false;
+    if (!ok) atomicOr(P.err, 2u);
+  }
+  __syncwarp();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 8) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_ACC_COLS)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// operands
+// ---------------------------------------------------------------------------
+namespace {
+
+struct TcPlan {
+  int p, so, msize, lsize, kch, kpad, nkb, nout, cls_scale, cls_bytes, slot_bytes, nslots, smem;
+  int nch[TC_MAXCH], choff[TC_MAXCH + 1];
+};
+
+bool tc_plan(int p, int so, TcPlan &pl) {
+  if (p < 1 || p > 9 || so < 0 || so > 1 || p < so + 1) return false;
+  pl.p = p;
+  pl.so = so;
+  const int moff = fmm_nterms(so - 1);
+  pl.msize = fmm_nterms(p) - moff;
+  pl.lsize = fmm_nterms(p - so);
+  pl.kch = (pl.msize + TC_CH - 1) / TC_CH;
+  pl.kpad = TC_CH * pl.kch;
+  pl.nkb = (pl.kch + 3) / 4;
+  if (pl.kch > TC_MAXCH || pl.nkb > TC_MAXKB) return false;
+  pl.choff[0] = 0;
+  for (int k = 0; k < pl.kch; k++) {
+    const int dm = fmm_decode(moff + TC_CH * k).d;  // lowest degree in the chunk (terms sorted by degree)
+    int nout = std::min(pl.lsize, fmm_nterms(p - dm));
+    if (nout < 1) nout = 1;
+    pl.nch[k] = (nout + 15) / 16 * 16;
+    pl.choff[k + 1] = pl.choff[k] + 2 * pl.nch[k] * 32;  // (hi, lo) blocks of nch rows x 16 FP16
+  }
+  pl.nout = pl.nch[0];
+  if (pl.nout > TC_ACC_COLS) return false;
+  pl.cls_scale = pl.choff[pl.kch];
+  pl.cls_bytes = (pl.cls_scale + 4 * pl.nout + 1023) / 1024 * 1024;
+  int bmax = 0;
+  for (int b = 0; b < pl.nkb; b++)
+    bmax = std::max(bmax, pl.choff[std::min(4 * b + 4, pl.kch)] - pl.choff[4 * b]);
+  pl.slot_bytes = (2 * TC_A_BYTES + bmax + 1023) / 1024 * 1024;
+  const int budget = 227 * 1024 - 1024 - (int)sizeof(TcShared);
+  pl.nslots = std::min(TC_MAXSLOTS, budget / pl.slot_bytes);
+  if (pl.nslots < 2) return false;
+  pl.smem = 1024 + pl.nslots * pl.slot_bytes + (int)sizeof(TcShared);
+  return true;
+}
+
+// T_c[m][n] = D_c[n + m] 2^(-dlev |m|) in FP64 (0 outside |n| + |m| <= p)
+__device__ __forceinline__ double op_entry(const double *D, int dlev, int p, int moff, int lsize, int msize, int n,
+                                           int pos) {
+  if (n >= lsize || pos >= msize) return 0.0;
+  const MI nn = fmm_decode(n), mm = fmm_decode(moff + pos);
+  if (nn.d + mm.d > p) return 0.0;
+  return ldexp(D[fmm_idx3(nn.x + mm.x, nn.y + mm.y, nn.z + mm.z)], -dlev * (int)mm.d);
+}
+
+// Operator record of a class: per K chunk, the (hi, lo) FP16 blocks of
+// 2^-g_n T_c[m][n] (row n, the chunk's 16 terms m) in the 32-byte swizzled
+// K-major layout (the two 16-byte halves of row n trade places when bit 2 of n
+// is set), then the column scales 2^g_n as FP32.
+__global__ void k_tc_operators(const double *D64, const int *key4, int ncls, TcPlan pl, unsigned char *T) {
+  __shared__ int g[TC_ACC_COLS];
+  const int c = blockIdx.x;
+  if (c >= ncls) return;
+  const int moff = fmm_nterms(pl.so - 1);
+  const double *D = D64 + (size_t)c * fmm_nterms(pl.p);
+  const int dlev = key4[4 * c];
+  unsigned char *rec = T + (size_t)c * pl.cls_bytes;
+  for (int n = threadIdx.x; n < pl.nout; n += blockDim.x) {
+    double mx = 0.0;
+    for (int pos = 0; pos < pl.msize; pos++)
+      mx = fmax(mx, fabs(op_entry(D, dlev, pl.p, moff, pl.lsize, pl.msize, n, pos)));
+    const int e = mx > 0.0 ? ilogb(mx) - TC_EBIAS : 0;
+    g[n] = e;
+    ((float *)(rec + pl.cls_scale))[n] = ldexpf(1.f, e);
+  }
+  __syncthreads();
+  for (int k = 0; k < pl.kch; k++) {
+    const int nr = pl.nch[k];
+    __half *blk = (__half *)(rec + pl.choff[k]);
+    for (int i = threadIdx.x; i < nr * 16; i += blockDim.x) {
+      const int n = i >> 4, pe = i & 15;
+      const int e16 = ((((pe >> 3) ^ (n >> 2)) & 1) << 3) | (pe & 7);  // term of the chunk stored here
+      const double y = ldexp(op_entry(D, dlev, pl.p, moff, pl.lsize, pl.msize, n, TC_CH * k + e16), -g[n]);
+      const __half hi = __float2half_rn((float)y);
+      blk[i] = hi;
+      blk[nr * 16 + i] = __float2half_rn((float)(y - (double)__half2float(hi)));
+    }
+  }
+}
+
+// Source multipoles as 2^e (hi + lo), hi and lo FP16 rows of kpad terms, e per
+// cell from the row's largest magnitude (one warp per cell).
+__global__ void k_tc_split(const float *M, int ncells, int mstr, int msize, int kpad, __half *Mh, __half *Ml,
+                           int *mexp) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= ncells) return;
+  const float *row = M + (size_t)w * mstr;
+  float mx = 0.f;
+  for (int i = lane; i < msize; i += 32) mx = fmaxf(mx, fabsf(row[i]));
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int e = scale_exp(mx);
+  if (lane == 0) mexp[w] = e;
+  for (int i = lane; i < kpad; i += 32) {
+    __half hi, lo;
+    split_f16(i < msize ? row[i] : 0.f, e, hi, lo);
+    Mh[(size_t)w * kpad + i] = hi;
+    Ml[(size_t)w * kpad + i] = lo;
+  }
+}
+
+int tc_sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n < 1) n = 1;
+  }
+  return n;
+}
+
+template <int NOUT> int tc_launch(const TcParams &P, int smem, int grid, cudaStream_t st) {
+  FMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l_tc<NOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  fmm_note_launch(), k_m2l_tc<NOUT><<<grid, TC_THREADS, smem, st>>>(P);
+  FMM_CUDA_TRY(cudaGetLastError());
+  return FMM_OK;
+}
+
+}  // namespace
+
+bool fmm_m2l_tc_supported(int p, int so) {
+  TcPlan pl;
+  return tc_plan(p, so, pl);
+}
+
+// M2L of the mixed-precision pass on the tensor cores: reads the FP32 scaled
+// multipoles M (row stride mstr) and writes every cell's FP32 scaled local
+// expansion L (row stride lstr).
+int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st) {
+  TcPlan pl;
+  if (!tc_plan(t->order, t->so, pl)) return FMM_ERR_ARG;
+  const int nc = t->ncells;
+  if (t->nm2l == 0) {
+    FMM_CUDA_TRY(cudaMemset2DAsync(L, sizeof(float) * lstr, 0, sizeof(float) * pl.lsize, nc, st));
+    return FMM_OK;
+  }
+  // operator records: once per build
+  if (t->tc_serial != t->build_serial) {
+    if (fmm_reserve(t->tc_T, (size_t)t->nclasses * pl.cls_bytes)) return FMM_ERR_CUDA;
+    fmm_note_launch(), k_tc_operators<<<t->nclasses, 256, 0, st>>>(t->cls_D.p, t->cls_key4.p, t->nclasses, pl,
+                                                                   t->tc_T.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    t->tc_serial = t->build_serial;
+  }
+  const size_t nm = (size_t)nc * pl.kpad;
+  if (fmm_reserve(t->tc_Mh, nm) || fmm_reserve(t->tc_Ml, nm) || fmm_reserve(t->tc_mexp, nc) ||
+      fmm_reserve(t->d_tcerr, 1))
+    return FMM_ERR_CUDA;
+  fmm_note_launch(), k_tc_split<<<fmm_blocks((size_t)nc * 32, 256), 256, 0, st>>>(
+      M, nc, mstr, pl.msize, pl.kpad, (__half *)t->tc_Mh.p, (__half *)t->tc_Ml.p, t->tc_mexp.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  FMM_CUDA_TRY(cudaMemsetAsync(t->d_tcerr.p, 0, sizeof(uint32_t), st));
+
+  TcParams P;
+  P.order = t->m2l_order.p;
+  P.ncells = nc;
+  P.ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
+  P.off = t->m2l_off.p;
+  P.src = t->m2l_src.p;
+  P.cls = t->m2l_cls.p;
+  P.Mh = (const __half *)t->tc_Mh.p;
+  P.Ml = (const __half *)t->tc_Ml.p;
+  P.mexp = t->tc_mexp.p;
+  P.T = t->tc_T.p;
+  P.L = L;
+  P.lstride = lstr;
+  P.lsize = pl.lsize;
+  P.kpad = pl.kpad;
+  P.kch = pl.kch;
+  P.nkb = pl.nkb;
+  P.nslots = pl.nslots;
+  P.cls_bytes = pl.cls_bytes;
+  P.cls_scale = pl.cls_scale;
+  P.slot_bytes = pl.slot_bytes;
+  P.nout = pl.nout;
+  for (int k = 0; k < TC_MAXCH; k++) P.nch[k] = k < pl.kch ? pl.nch[k] : 0;
+  for (int k = 0; k <= TC_MAXCH; k++) P.choff[k] = k <= pl.kch ? pl.choff[k] : pl.cls_scale;
+  P.err = t->d_tcerr.p;
+  const int grid = std::min(P.ntiles, tc_sm_count());
+  int rc;
+  switch (pl.nout) {
+    case 16: rc = tc_launch<16>(P, pl.smem, grid, st); break;
+    case 32: rc = tc_launch<32>(P, pl.smem, grid, st); break;
+    case 48: rc = tc_launch<48>(P, pl.smem, grid, st); break;
+    case 64: rc = tc_launch<64>(P, pl.smem, grid, st); break;
+    case 96: rc = tc_launch<96>(P, pl.smem, grid, st); break;
+    case 128: rc = tc_launch<128>(P, pl.smem, grid, st); break;
+    case 176: rc = tc_launch<176>(P, pl.smem, grid, st); break;
+    case 224: rc = tc_launch<224>(P, pl.smem, grid, st); break;
+    default: return FMM_ERR_ARG;
+  }
+  if (rc) return rc;
+  // timeout flags reach the host with the stream (read by fmmgen_tree_times)
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, st));
+  return FMM_OK;
+}

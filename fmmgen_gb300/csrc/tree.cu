@@ -419,32 +419,22 @@ __global__ void k_class_assign(const int *src, const int *tgt, long n, const int
   cls[i] = table[class_slot(dl, dx, dy, dz, R, dlmin)];
 }
 
-// Key per cell for the M2L processing order: level in the top byte, then a
-// hash of the cell's class-sorted list, so that cells with the same
-// interaction pattern are processed side by side and read the same operator
-// rows at the same time (one warp per cell).
-__global__ void k_list_keys(const int *off, int nc, const int *cls, const unsigned char *clevel, uint64_t *key,
-                            uint32_t *idx) {
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * FMM_WARPS + w;
+// Key per cell for the M2L processing order: (level, octant within the
+// parent, parent index).  A cell's interaction list depends on which octant of
+// its parent it is (the children of the parent's neighbours that pass the MAC),
+// so grouping the cells of one level by octant, with parents in Morton order
+// (cell indices are Morton order within a level), puts cells with
+// near-identical class lists side by side: the 128-cell tiles of the tensor-core
+// M2L then visit ~1.4x the classes of one list instead of ~3.5x in plain Morton
+// order, and the warps of the CUDA-core M2L read the same operator rows.
+// Cells are stored level by level in parent order, so a stable sort on
+// (level, octant) alone keeps the parents in Morton order.
+__global__ void k_order_keys(int nc, const uint64_t *cid, const unsigned char *clevel, uint64_t *key,
+                             uint32_t *idx) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  const int k0 = off[c], n = off[c + 1] - k0;
-  // order-dependent hash of the class list: XOR of mixed (position, class)
-  unsigned long long h = 0;
-  for (int i = lane; i < n; i += 32) {
-    unsigned long long v = (unsigned long long)(unsigned)cls[k0 + i];
-    unsigned long long x = (v + 1) * 0x9E3779B97F4A7C15ull ^ ((unsigned long long)i * 0xC2B2AE3D27D4EB4Full);
-    x ^= x >> 31;
-    x *= 0xBF58476D1CE4E5B9ull;
-    x ^= x >> 29;
-    h ^= x;
-  }
-  for (int d = 16; d; d >>= 1) h ^= __shfl_xor_sync(0xffffffffu, h, d);
-  if (lane == 0) {
-    h ^= (unsigned long long)n * 0x94D049BB133111EBull;
-    key[c] = ((uint64_t)clevel[c] << 56) | (h >> 8);
-    idx[c] = (uint32_t)c;
-  }
+  key[c] = ((uint64_t)clevel[c] << 56) | ((cid[c] & 7u) << 48);
+  idx[c] = (uint32_t)c;
 }
 
 // Operator vector of a class: D_k(d / s_A), |k| <= p, in FP64 (one warp per class).
@@ -508,7 +498,11 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
     for (int i = 0; i < 16; i++) FMM_CUDA_TRY(cudaEventCreate(&t->ev[i]));
     t->ev_ready = true;
   }
-  if (!t->h_pinned) FMM_CUDA_TRY(cudaMallocHost((void **)&t->h_pinned, 64));
+  if (!t->h_pinned) {
+    FMM_CUDA_TRY(cudaMallocHost((void **)&t->h_pinned, 64));
+    memset(t->h_pinned, 0, 64);
+  }
+  t->build_serial++;
   TRY(rec(t, 0, st));
   TRY(fmm_reserve(t->d_eflags, 4));
   FMM_CUDA_TRY(cudaMemsetAsync(t->d_eflags.p, 0, sizeof(uint32_t), st));
@@ -838,10 +832,10 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   uint32_t *hist = (uint32_t *)q; q += hist_n * 4;
   uint32_t *stmp2 = (uint32_t *)q;
   TRY(fmm_reserve(t->m2l_order, nc));
-  fmm_note_launch(), k_list_keys<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-      t->m2l_off.p, nc, t->m2l_cls.p, t->clevel.p, k1, (uint32_t *)t->m2l_order.p);
+  fmm_note_launch(), k_order_keys<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->cid.p, t->clevel.p, k1,
+                                                                        (uint32_t *)t->m2l_order.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  TRY(fmm_radix_sort<uint64_t>(k1, (uint32_t *)t->m2l_order.p, k2, v2, nc, 0, 64, hist, stmp2, st));
+  TRY(fmm_radix_sort<uint64_t>(k1, (uint32_t *)t->m2l_order.p, k2, v2, nc, 48, 64, hist, stmp2, st));
   return FMM_OK;
 }
 
@@ -862,6 +856,9 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->fa); fmm_release(t->fb); fmm_release(t->fa2); fmm_release(t->fb2);
   fmm_release(t->m2l_tgt_raw); fmm_release(t->m2l_src_raw);
   fmm_release(t->p2p_tgt_raw); fmm_release(t->p2p_src_raw);
+  fmm_release(t->tc_T); fmm_release(t->tc_Mh); fmm_release(t->tc_Ml); fmm_release(t->tc_mexp);
+  fmm_release(t->d_tcerr);
+  t->tc_serial = ~0ull;
   fmm_release(t->wdec); fmm_release(t->wmargin);
   fmm_release(t->tmp); fmm_release(t->d_eflags); fmm_release(t->d_root);
   if (t->h_pinned) cudaFreeHost(t->h_pinned);

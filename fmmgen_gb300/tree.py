@@ -18,7 +18,7 @@ import torch
 from . import _lib
 from ._lib import check, lib
 
-PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, "mixed_simt": _lib.PREC_MIXED_SIMT}
 
 
 def _stream_ptr(stream=None):

@@ -38,7 +38,9 @@ extern "C" {
 
 /* precision modes of fmmgen_tree_compute_field_fmm */
 #define FMMGEN_PREC_FP64 0   /* every phase in FP64 */
-#define FMMGEN_PREC_MIXED 1  /* FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation */
+#define FMMGEN_PREC_MIXED 1  /* FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation;
+                                M2L on the tensor cores (3xTF32) for orders <= 9 */
+#define FMMGEN_PREC_MIXED_SIMT 2  /* as FMMGEN_PREC_MIXED with the M2L on the FP32 CUDA cores */
 
 const char *fmmgen_last_error(void);
 const char *fmmgen_version(void);
