@@ -63,8 +63,8 @@ struct DevTree {
   DevBuf<int> cls_key4;                   // [nclasses][4]: dlev, dx, dy, dz
   DevBuf<double> cls_D;                   // [nclasses][Nterms(order)]
   DevBuf<float> cls_Df;
-  DevBuf<int> cls_table;                  // dense table key -> class id
-  int cls_range = 0, cls_dlmin = 0, cls_dlmax = 0;
+  DevBuf<uint64_t> cls_hkeys;             // open-addressing table of class keys
+  DevBuf<int> cls_table;                  // class id of each table slot
   // expansions (scaled: M~_n = M_n / s^|n|, L^_n = s^(|n|+1) L_n)
   DevBuf<double> M, L;
   DevBuf<float> Mf, Lf;

@@ -321,7 +321,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
         k = P.off[A];
         kend = P.off[A + 1];
       }
+      // the current list entry and the next one, loaded a class step before
+      // they are needed so that no global-load latency sits in the step loop
       unsigned head = k < kend ? (unsigned)P.cls[k] : TC_NONE;
+      int hsrc = k < kend ? P.src[k] : 0;
+      unsigned nhead = k + 1 < kend ? (unsigned)P.cls[k + 1] : TC_NONE;
+      int nsrc = k + 1 < kend ? P.src[k + 1] : 0;
       unsigned c = gather_min(head, cs, par);
       int e_last = 0;  // row scale exponent of the step issued last
       if (c == TC_NONE) {  // no M2L into this tile
@@ -333,12 +338,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
       for (int i = 0; i < HALF; i++) acc[i] = 0.f;
       uint32_t steps = 0;
       while (true) {
-        const int mysrc = head == c ? P.src[k] : -1;
-        if (head == c) {
+        const bool mine = head == c;
+        const int mysrc = mine ? hsrc : -1;
+        const int e_this = mine ? P.mexp[hsrc] : 0;  // first used by the fold one step later
+        if (mine) {
+          head = nhead;
+          hsrc = nsrc;
           k++;
-          head = k < kend ? (unsigned)P.cls[k] : TC_NONE;
+          nhead = k + 1 < kend ? (unsigned)P.cls[k + 1] : TC_NONE;
+          nsrc = k + 1 < kend ? P.src[k + 1] : 0;
         }
-        const int e_this = mysrc >= 0 ? P.mexp[mysrc] : 0;
         const unsigned cnext = gather_min(head, cs, par);
         for (int kb = 0; kb < P.nkb; kb++) {
           const int slot = (int)(g % (uint32_t)P.nslots);
@@ -416,6 +425,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
     if (!ok && tid == 0) atomicOr(P.err, 1u);
   } else if (lane == 0) {
     // ---------------- MMA issue (one thread) ----------------
+    // Per-chunk instruction descriptors and operator offsets live in
+    // registers (compile-time indices below), so nothing but descriptor
+    // arithmetic sits between consecutive MMAs.
+    uint32_t idr[TC_MAXCH], bor[TC_MAXCH], nlr[TC_MAXCH];
+#pragma unroll
+    for (int ch = 0; ch < TC_MAXCH; ch++) {
+      idr[ch] = cs->ch_idesc[ch];
+      bor[ch] = cs->ch_boff[ch];
+      nlr[ch] = cs->ch_nlo[ch];
+    }
+    const int kch = P.kch;
     uint32_t g = 0, u = 0;
     bool ok = true;
     while (true) {
@@ -437,19 +457,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
       const uint64_t ah0 = sw128_desc(sa), al0 = sw128_desc(sa + TC_A_BYTES);
       const uint64_t b0 = sw32_desc(sa + 2 * TC_A_BYTES);
       const uint32_t d = tmem + b * TC_ACC_COLS;
-      const int nc = min(4, P.kch - 4 * kb);
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        if (j < nc) {
-          const int ch = 4 * kb + j;
-          const uint32_t id = cs->ch_idesc[ch];
-          const uint64_t bh = b0 + cs->ch_boff[ch], bl = bh + cs->ch_nlo[ch];
-          const uint64_t ah = ah0 + 2 * j, al = al0 + 2 * j;  // 32 bytes along the 128-byte row
-          mma_f16(d, ah, bh, id, (kb == 0 && j == 0) ? 0u : 1u);
-          mma_f16(d, ah, bl, id, 1u);
-          mma_f16(d, al, bh, id, 1u);
-        }
+#define TC_CHUNK(KB, J)                                                                 \
+  if (4 * (KB) + (J) < kch) {                                                           \
+    const uint64_t bh = b0 + bor[4 * (KB) + (J)], bl = bh + nlr[4 * (KB) + (J)];        \
+    const uint64_t ah = ah0 + 2 * (J), al = al0 + 2 * (J); /* 32 bytes along the row */ \
+    mma_f16(d, ah, bh, idr[4 * (KB) + (J)], ((KB) == 0 && (J) == 0) ? 0u : 1u);         \
+    mma_f16(d, ah, bl, idr[4 * (KB) + (J)], 1u);                                        \
+    mma_f16(d, al, bh, idr[4 * (KB) + (J)], 1u);                                        \
+  }
+#define TC_KBLOCK(KB) \
+  TC_CHUNK(KB, 0)     \
+  TC_CHUNK(KB, 1)     \
+  TC_CHUNK(KB, 2)     \
+  TC_CHUNK(KB, 3)
+      switch (kb) {
+        case 0: { TC_KBLOCK(0) } break;
+        case 1: { TC_KBLOCK(1) } break;
+        case 2: { TC_KBLOCK(2) } break;
+        default: { TC_KBLOCK(3) } break;
       }
+#undef TC_KBLOCK
+#undef TC_CHUNK
       mma_commit(empty0 + 8 * slot);
       if (kb == P.nkb - 1) {
         mma_commit(accfull0 + 8 * b);

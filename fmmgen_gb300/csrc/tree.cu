@@ -338,85 +338,104 @@ __global__ void k_csr_from_sorted(const K *keys, long n, int cbits, int nc, int 
 // ---------------------------------------------------------------------------
 // A pair (B -> A) with levels lA, lB is, up to the scale of A, fixed by
 // (dlev = lB - lA, integer offset of the centres in half-widths of the finer
-// level).  Classes are shared across levels.
-__device__ __forceinline__ void pair_class(const int *ix, const int *iy, const int *iz, const unsigned char *clevel,
-                                           int A, int B, int &dl, int &dx, int &dy, int &dz) {
-  int la = clevel[A], lb = clevel[B];
-  int L = la > lb ? la : lb;
-  int sa = L - la, sb = L - lb;
-  dl = lb - la;
-  dx = ((2 * ix[A] + 1) << sa) - ((2 * ix[B] + 1) << sb);
-  dy = ((2 * iy[A] + 1) << sa) - ((2 * iy[B] + 1) << sb);
-  dz = ((2 * iz[A] + 1) << sa) - ((2 * iz[B] + 1) << sb);
+// level).  Classes are shared across levels.  The class key packs
+// (dlev + 64, dx + 2^18, dy + 2^18, dz + 2^18) into 7 + 3 x 19 bits, so keys
+// order lexicographically by (dlev, dx, dy, dz); class ids are the ranks of
+// the distinct keys in that order.
+#define CLS_EMPTY 0xffffffffffffffffull
+#define CLS_LIM (1LL << 18)
+__device__ __forceinline__ uint64_t pair_key(const int *ix, const int *iy, const int *iz, const unsigned char *clevel,
+                                             int A, int B) {
+  const int la = clevel[A], lb = clevel[B];
+  const int L = la > lb ? la : lb;
+  const int sa = L - la, sb = L - lb;
+  const long long dx = ((2LL * ix[A] + 1) << sa) - ((2LL * ix[B] + 1) << sb);
+  const long long dy = ((2LL * iy[A] + 1) << sa) - ((2LL * iy[B] + 1) << sb);
+  const long long dz = ((2LL * iz[A] + 1) << sa) - ((2LL * iz[B] + 1) << sb);
+  if (llabs(dx) >= CLS_LIM || llabs(dy) >= CLS_LIM || llabs(dz) >= CLS_LIM) return CLS_EMPTY;
+  return ((uint64_t)(lb - la + 64) << 57) | ((uint64_t)(dx + CLS_LIM) << 38) | ((uint64_t)(dy + CLS_LIM) << 19) |
+         (uint64_t)(dz + CLS_LIM);
+}
+__device__ __forceinline__ void key_decode(uint64_t k, int *key4) {
+  key4[0] = (int)(k >> 57) - 64;
+  key4[1] = (int)((long long)((k >> 38) & 0x7FFFF) - CLS_LIM);
+  key4[2] = (int)((long long)((k >> 19) & 0x7FFFF) - CLS_LIM);
+  key4[3] = (int)((long long)(k & 0x7FFFF) - CLS_LIM);
+}
+// slot sequence of a key in the open-addressing table (splitmix64 finalizer)
+__device__ __forceinline__ uint32_t key_hash(uint64_t k) {
+  k ^= k >> 30;
+  k *= 0xBF58476D1CE4E5B9ull;
+  k ^= k >> 27;
+  k *= 0x94D049BB133111EBull;
+  k ^= k >> 31;
+  return (uint32_t)k;
+}
+__device__ __forceinline__ long key_find(const uint64_t *tab, uint32_t mask, uint64_t k) {
+  uint32_t h = key_hash(k) & mask;
+  for (uint32_t probe = 0; probe <= mask; probe++) {
+    const uint64_t cur = tab[h];
+    if (cur == k) return h;
+    if (cur == CLS_EMPTY) return -1;
+    h = (h + 1) & mask;
+  }
+  return -1;
 }
 
-__global__ void k_class_range(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
-                              const unsigned char *clevel, int *rng /*[3]: max|d|, max dl, max -dl*/) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  int m = 0, dlp = 0, dlm = 0;
-  if (i < n) {
-    int dl, dx, dy, dz;
-    pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
-    m = max(abs(dx), max(abs(dy), abs(dz)));
-    dlp = max(dl, 0);
-    dlm = max(-dl, 0);
-  }
-  for (int d = 16; d; d >>= 1) {
-    m = max(m, __shfl_xor_sync(0xffffffffu, m, d));
-    dlp = max(dlp, __shfl_xor_sync(0xffffffffu, dlp, d));
-    dlm = max(dlm, __shfl_xor_sync(0xffffffffu, dlm, d));
-  }
-  // one atomic per block: all blocks hit the same three words
-  __shared__ int sm[3];
-  if (threadIdx.x < 3) sm[threadIdx.x] = 0;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&sm[0], m);
-    atomicMax(&sm[1], dlp);
-    atomicMax(&sm[2], dlm);
-  }
-  __syncthreads();
-  if (threadIdx.x < 3) atomicMax(&rng[threadIdx.x], sm[threadIdx.x]);
-}
-
-__device__ __forceinline__ long class_slot(int dl, int dx, int dy, int dz, int R, int dlmin) {
-  long w = 2 * R + 1;
-  return ((((long)(dl - dlmin) * w + (dx + R)) * w + (dy + R)) * w + (dz + R));
-}
-
-__global__ void k_class_mark(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
-                             const unsigned char *clevel, int R, int dlmin, uint32_t *mark) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+// Class key of every pair, inserted into the table; stat[0] counts distinct
+// keys, stat[1] flags a table that filled up.
+__global__ void k_class_keys(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
+                             const unsigned char *clevel, uint64_t *keys, uint64_t *tab, uint32_t mask,
+                             uint32_t *stat, uint32_t *eflags) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int dl, dx, dy, dz;
-  pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
-  long s = class_slot(dl, dx, dy, dz, R, dlmin);
-  if (mark[s] == 0) mark[s] = 1;
+  const uint64_t k = pair_key(ix, iy, iz, clevel, tgt[i], src[i]);
+  keys[i] = k;
+  if (k == CLS_EMPTY) {
+    atomicOr(eflags, FMM_EFLAG_RANGE);
+    return;
+  }
+  uint32_t h = key_hash(k) & mask;
+  for (uint32_t probe = 0; probe <= mask; probe++) {
+    uint64_t cur = tab[h];
+    if (cur == CLS_EMPTY) {
+      cur = atomicCAS((unsigned long long *)&tab[h], CLS_EMPTY, (unsigned long long)k);
+      if (cur == CLS_EMPTY) {
+        atomicAdd(&stat[0], 1u);
+        return;
+      }
+    }
+    if (cur == k) return;
+    h = (h + 1) & mask;
+  }
+  atomicOr(&stat[1], 1u);
 }
 
-__global__ void k_class_list(const uint32_t *mark, const uint32_t *id, long nslots, int R, int dlmin,
-                             int *table, int *key4) {
-  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (s >= nslots) return;
-  if (!mark[s]) { table[s] = -1; return; }
-  int c = (int)id[s];
-  table[s] = c;
-  long w = 2 * R + 1;
-  long t = s;
-  int dz = (int)(t % w) - R; t /= w;
-  int dy = (int)(t % w) - R; t /= w;
-  int dx = (int)(t % w) - R; t /= w;
-  int dl = (int)t + dlmin;
-  key4[4 * c] = dl; key4[4 * c + 1] = dx; key4[4 * c + 2] = dy; key4[4 * c + 3] = dz;
+__global__ void k_class_collect(const uint64_t *tab, uint32_t nslots, uint64_t *uniq, uint32_t *idx,
+                                uint32_t *counter) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslots || tab[s] == CLS_EMPTY) return;
+  const uint32_t r = atomicAdd(counter, 1u);
+  uniq[r] = tab[s];
+  idx[r] = r;
 }
 
-__global__ void k_class_assign(const int *src, const int *tgt, long n, const int *ix, const int *iy, const int *iz,
-                               const unsigned char *clevel, int R, int dlmin, const int *table, int *cls) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+// ids by rank of the sorted distinct keys; the class table entry of each key
+__global__ void k_class_rank(const uint64_t *uniq, int nu, const uint64_t *tab, uint32_t mask, int *tabval,
+                             int *key4) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nu) return;
+  const long s = key_find(tab, mask, uniq[r]);
+  if (s >= 0) tabval[s] = r;
+  key_decode(uniq[r], key4 + 4 * r);
+}
+
+__global__ void k_class_lookup(const uint64_t *keys, long n, const uint64_t *tab, uint32_t mask, const int *tabval,
+                               int *cls) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int dl, dx, dy, dz;
-  pair_class(ix, iy, iz, clevel, tgt[i], src[i], dl, dx, dy, dz);
-  cls[i] = table[class_slot(dl, dx, dy, dz, R, dlmin)];
+  const long s = keys[i] == CLS_EMPTY ? -1 : key_find(tab, mask, keys[i]);
+  cls[i] = s >= 0 ? tabval[s] : 0;  // out-of-range pairs were flagged when their keys were made
 }
 
 // Key per cell for the M2L processing order: (level, octant within the
@@ -771,45 +790,56 @@ static int build_classes(DevTree *t, cudaStream_t st) {
     t->nclasses = 0;
     return group_by_target(t, t->m2l_tgt_raw, t->m2l_src_raw, nullptr, 0, 0, t->m2l_off, t->m2l_src, nullptr, st);
   }
-  // classes of the raw (walk-order) pairs
+  // classes of the raw (walk-order) pairs: the distinct keys through an
+  // open-addressing table, ids by rank of the sorted distinct keys
   const int *tgt = t->m2l_tgt_raw.p, *src = t->m2l_src_raw.p;
-  TRY(tmp_reserve(t, 64));
-  int *rng = (int *)t->tmp.p;
-  FMM_CUDA_TRY(cudaMemsetAsync(rng, 0, 3 * sizeof(int), st));
-  fmm_note_launch(), k_class_range<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, rng);
-  FMM_CUDA_TRY(cudaGetLastError());
-  int *h = (int *)t->h_pinned;
-  FMM_CUDA_TRY(cudaMemcpyAsync(h, rng, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
-  FMM_CUDA_TRY(cudaStreamSynchronize(st));
-  int R = h[0], dlmin = -h[2], dlmax = h[1];
-  long w = 2L * R + 1;
-  long nslots = (long)(dlmax - dlmin + 1) * w * w * w;
-  if (nslots > (1L << 28)) {
-    fmm_set_error_text("M2L offsets span a range too wide for the class table");
-    return FMM_ERR_RANGE;
+  uint32_t hsize = 1u << 16;
+  while ((long)hsize < std::min<long>(n, 1L << 20) / 4) hsize <<= 1;
+  uint64_t *keys = nullptr, *U1 = nullptr, *U2 = nullptr;
+  uint32_t *stat = nullptr, *I1 = nullptr, *I2 = nullptr, *uhist = nullptr, *uscan = nullptr;
+  uint32_t ncls = 0;
+  for (int attempt = 0;; attempt++) {
+    const size_t umax = hsize / 2;
+    const size_t histu = 256 * fmm_rs_nblocks(umax);
+    TRY(tmp_reserve(t, (size_t)n * 8 + 64 + umax * 24 + histu * 4 + fmm_scan_tmp_elems<uint32_t>(histu) * 4 + 256));
+    char *q = t->tmp.p;
+    keys = (uint64_t *)q; q += (size_t)n * 8;
+    stat = (uint32_t *)q; q += 64;
+    U1 = (uint64_t *)q; q += umax * 8;
+    U2 = (uint64_t *)q; q += umax * 8;
+    I1 = (uint32_t *)q; q += umax * 4;
+    I2 = (uint32_t *)q; q += umax * 4;
+    uhist = (uint32_t *)q; q += histu * 4;
+    uscan = (uint32_t *)q;
+    TRY(fmm_reserve(t->cls_hkeys, hsize));
+    FMM_CUDA_TRY(cudaMemsetAsync(t->cls_hkeys.p, 0xff, sizeof(uint64_t) * hsize, st));  // all CLS_EMPTY
+    FMM_CUDA_TRY(cudaMemsetAsync(stat, 0, 4 * sizeof(uint32_t), st));
+    fmm_note_launch(), k_class_keys<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p,
+                                                                        t->clevel.p, keys, t->cls_hkeys.p,
+                                                                        hsize - 1, stat, t->d_eflags.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, stat, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    ncls = t->h_pinned[0];
+    if (!t->h_pinned[1] && ncls <= umax) break;
+    if (hsize >= (1u << 28) || attempt >= 4) {
+      fmm_set_error_text("M2L translation classes: the class table could not hold the distinct offsets");
+      return FMM_ERR_RANGE;
+    }
+    hsize <<= 4;
   }
-  t->cls_range = R; t->cls_dlmin = dlmin; t->cls_dlmax = dlmax;
-  TRY(fmm_reserve(t->cls_table, nslots));
-  size_t bytes = (size_t)nslots * 8 + fmm_scan_tmp_elems<uint32_t>(nslots) * 4 + 64;
-  TRY(tmp_reserve(t, bytes));
-  uint32_t *mark = (uint32_t *)t->tmp.p;
-  uint32_t *id = mark + nslots;
-  uint32_t *total = id + nslots;
-  uint32_t *stmp = total + 1;
-  FMM_CUDA_TRY(cudaMemsetAsync(mark, 0, sizeof(uint32_t) * nslots, st));
-  fmm_note_launch(), k_class_mark<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R, dlmin,
-                                                   mark);
-  TRY(fmm_scan<uint32_t>(mark, id, nslots, total, stmp, st));
-  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  FMM_CUDA_TRY(cudaStreamSynchronize(st));
-  const uint32_t ncls = t->h_pinned[0];
   t->nclasses = (int)ncls;
-  TRY(fmm_reserve(t->cls_key4, 4 * (size_t)ncls));
-  fmm_note_launch(), k_class_list<<<fmm_blocks(nslots, 256), 256, 0, st>>>(mark, id, nslots, R, dlmin, t->cls_table.p, t->cls_key4.p);
+  TRY(fmm_reserve(t->cls_key4, 4 * (size_t)(ncls > 0 ? ncls : 1)));
+  TRY(fmm_reserve(t->cls_table, hsize));
+  fmm_note_launch(), k_class_collect<<<fmm_blocks(hsize, 256), 256, 0, st>>>(t->cls_hkeys.p, hsize, U1, I1,
+                                                                              stat + 2);
+  TRY(fmm_radix_sort<uint64_t>(U1, I1, U2, I2, ncls, 0, 64, uhist, uscan, st));
+  fmm_note_launch(), k_class_rank<<<fmm_blocks(ncls, 256), 256, 0, st>>>(U1, (int)ncls, t->cls_hkeys.p, hsize - 1,
+                                                                          t->cls_table.p, t->cls_key4.p);
   // raw classes go to the (finished) walk frontier buffer
   TRY(fmm_reserve(t->fa, n));
-  fmm_note_launch(), k_class_assign<<<fmm_blocks(n, 256), 256, 0, st>>>(src, tgt, n, t->ix.p, t->iy.p, t->iz.p, t->clevel.p, R,
-                                                     dlmin, t->cls_table.p, t->fa.p);
+  fmm_note_launch(), k_class_lookup<<<fmm_blocks(n, 256), 256, 0, st>>>(keys, n, t->cls_hkeys.p, hsize - 1,
+                                                                         t->cls_table.p, t->fa.p);
   FMM_CUDA_TRY(cudaGetLastError());
   // group by (target, class): a target has at most one source per class, so
   // the order within a list is fully determined
@@ -851,6 +881,7 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->m2l_off); fmm_release(t->m2l_src); fmm_release(t->m2l_cls); fmm_release(t->m2l_order);
   fmm_release(t->p2p_off); fmm_release(t->p2p_src);
   fmm_release(t->cls_key4); fmm_release(t->cls_D); fmm_release(t->cls_Df); fmm_release(t->cls_table);
+  fmm_release(t->cls_hkeys);
   fmm_release(t->M); fmm_release(t->L); fmm_release(t->Mf); fmm_release(t->Lf);
   fmm_release(t->Fnear); fmm_release(t->Ffar);
   fmm_release(t->fa); fmm_release(t->fb); fmm_release(t->fa2); fmm_release(t->fb2);
