@@ -65,6 +65,9 @@ struct DevTree {
   DevBuf<float> cls_Df;
   DevBuf<uint64_t> cls_hkeys;             // open-addressing table of class keys
   DevBuf<int> cls_table;                  // class id of each table slot
+  DevBuf<uint64_t> cls_prev;              // sorted class keys of the previous build
+  int ncls_prev = -1, order_prev = -1;
+  DevBuf<uint32_t> d_cls_same;            // nonzero: this build's classes equal the previous build's
   // expansions (scaled: M~_n = M_n / s^|n|, L^_n = s^(|n|+1) L_n)
   DevBuf<double> M, L;
   DevBuf<float> Mf, Lf;
@@ -81,6 +84,7 @@ struct DevTree {
   DevBuf<int> tc_mexp;                    // per cell: scale exponent of its multipole row
   DevBuf<uint32_t> d_tcerr;               // kernel timeout flags
   uint64_t build_serial = 0, tc_serial = ~0ull;  // tc_T belongs to the build with this serial
+  int tc_order = -1, tc_so = -1;          // ... and to this expansion order and source order
   DevBuf<unsigned char> wdec;             // decision of each frontier pair
   DevBuf<float> wmargin;                  // MAC band decided in FP64, per level
   DevBuf<char> tmp;                       // scan / sort / misc scratch

@@ -559,10 +559,12 @@ __device__ __forceinline__ double op_entry(const double *D, int dlev, int p, int
 // 2^-g_n T_c[m][n] (row n, the chunk's 16 terms m) in the 32-byte swizzled
 // K-major layout (the two 16-byte halves of row n trade places when bit 2 of n
 // is set), then the column scales 2^g_n as FP32.
-__global__ void k_tc_operators(const double *D64, const int *key4, int ncls, TcPlan pl, unsigned char *T) {
+// (skipped when `same` is given and set: the records of the previous build hold)
+__global__ void k_tc_operators(const double *D64, const int *key4, int ncls, TcPlan pl, unsigned char *T,
+                               const uint32_t *same) {
   __shared__ int g[TC_ACC_COLS];
   const int c = blockIdx.x;
-  if (c >= ncls) return;
+  if (c >= ncls || (same && *same)) return;
   const int moff = fmm_nterms(pl.so - 1);
   const double *D = D64 + (size_t)c * fmm_nterms(pl.p);
   const int dlev = key4[4 * c];
@@ -648,11 +650,17 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   }
   // operator records: once per build
   if (t->tc_serial != t->build_serial) {
-    if (fmm_reserve(t->tc_T, (size_t)t->nclasses * pl.cls_bytes)) return FMM_ERR_CUDA;
+    const size_t bytes = (size_t)t->nclasses * pl.cls_bytes;
+    // the previous build's records stay valid when its classes were the same
+    const bool prev = t->tc_serial + 1 == t->build_serial && t->tc_order == t->order && t->tc_so == t->so &&
+                      t->tc_T.cap >= bytes;
+    if (fmm_reserve(t->tc_T, bytes)) return FMM_ERR_CUDA;
     fmm_note_launch(), k_tc_operators<<<t->nclasses, 256, 0, st>>>(t->cls_D.p, t->cls_key4.p, t->nclasses, pl,
-                                                                   t->tc_T.p);
+                                                                   t->tc_T.p, prev ? t->d_cls_same.p : nullptr);
     FMM_CUDA_TRY(cudaGetLastError());
     t->tc_serial = t->build_serial;
+    t->tc_order = t->order;
+    t->tc_so = t->so;
   }
   const size_t nm = (size_t)nc * pl.kpad;
   if (fmm_reserve(t->tc_Mh, nm) || fmm_reserve(t->tc_Ml, nm) || fmm_reserve(t->tc_mexp, nc) ||

@@ -136,26 +136,44 @@ __device__ __forceinline__ void add2(float ah, float al, float oh, float ol, flo
 }
 
 template <bool SELF>
+__device__ __forceinline__ void coulomb_one(const float4 &q, const float4 &ql, bool self, float txh, float txl,
+                                            float tyh, float tyl, float tzh, float tzl, float &phi, float &ex,
+                                            float &ey, float &ez) {
+  const float dx = (txh - q.x) + (txl - ql.x);
+  const float dy = (tyh - q.y) + (tyl - ql.y);
+  const float dz = (tzh - q.z) + (tzl - ql.z);
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  float rinv = rsqrt_nr(r2);
+  if (SELF) rinv = self ? 0.f : rinv;  // l2 != l1
+  const float qr = q.w * rinv;
+  const float qr3 = qr * (rinv * rinv);
+  phi += qr;
+  ex = fmaf(qr3, dx, ex);
+  ey = fmaf(qr3, dy, ey);
+  ez = fmaf(qr3, dz, ez);
+}
+
+// Sources first, first + step, ... < cnt of the staged chunk.  With one lane
+// per target (step 1) the loop runs in blocks of 8 with constant shared-memory
+// offsets, so nothing but the interaction itself sits in the loop body.
+template <bool SELF>
 __device__ __forceinline__ void p2p_coulomb(const float4 *sh, const float4 *sl, int first, int cnt, int step,
                                             int selfj, float txh, float txl, float tyh, float tyl, float tzh,
                                             float tzl, float &phi, float &ex, float &ey, float &ez) {
-#pragma unroll 4
-  for (int jj = first; jj < cnt; jj += step) {
-    const float4 q = sh[jj];
-    const float4 ql = sl[jj];
-    const float dx = (txh - q.x) + (txl - ql.x);
-    const float dy = (tyh - q.y) + (tyl - ql.y);
-    const float dz = (tzh - q.z) + (tzl - ql.z);
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    float rinv = rsqrt_nr(r2);
-    if (SELF) rinv = (jj == selfj) ? 0.f : rinv;  // l2 != l1
-    const float qr = q.w * rinv;
-    const float qr3 = qr * (rinv * rinv);
-    phi += qr;
-    ex = fmaf(qr3, dx, ex);
-    ey = fmaf(qr3, dy, ey);
-    ez = fmaf(qr3, dz, ez);
+  if (step == 1) {
+    int jj = 0;
+    for (; jj + 8 <= cnt; jj += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        coulomb_one<SELF>(sh[jj + u], sl[jj + u], jj + u == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+    }
+    for (; jj < cnt; jj++)
+      coulomb_one<SELF>(sh[jj], sl[jj], jj == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+    return;
   }
+#pragma unroll 4
+  for (int jj = first; jj < cnt; jj += step)
+    coulomb_one<SELF>(sh[jj], sl[jj], jj == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
 }
 
 template <bool SELF>

@@ -430,6 +430,12 @@ __global__ void k_class_rank(const uint64_t *uniq, int nu, const uint64_t *tab, 
   key_decode(uniq[r], key4 + 4 * r);
 }
 
+// clears *same unless the two sorted key lists are equal
+__global__ void k_keys_equal(const uint64_t *a, const uint64_t *b, int n, uint32_t *same) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && a[i] != b[i]) *same = 0;
+}
+
 __global__ void k_class_lookup(const uint64_t *keys, long n, const uint64_t *tab, uint32_t mask, const int *tabval,
                                int *cls) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -457,11 +463,12 @@ __global__ void k_order_keys(int nc, const uint64_t *cid, const unsigned char *c
 }
 
 // Operator vector of a class: D_k(d / s_A), |k| <= p, in FP64 (one warp per class).
-__global__ void k_class_derivs(const int *key4, int ncls, int p, double *D64, float *D32) {
+// (skipped when `same` is set: the vectors of the previous build still hold)
+__global__ void k_class_derivs(const int *key4, int ncls, int p, double *D64, float *D32, const uint32_t *same) {
   __shared__ double sD[FMM_WARPS][FMM_NTMAX], sT[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_PMAX + 1];
   int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int c = blockIdx.x * FMM_WARPS + w;
-  if (c >= ncls) return;
+  if (c >= ncls || *same) return;
   int dl = key4[4 * c];
   double sc = dl > 0 ? ldexp(1.0, -dl) : 1.0;  // finer-level half-widths -> half-widths of A
   double x = key4[4 * c + 1] * sc, y = key4[4 * c + 2] * sc, z = key4[4 * c + 3] * sc;
@@ -834,6 +841,20 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_class_collect<<<fmm_blocks(hsize, 256), 256, 0, st>>>(t->cls_hkeys.p, hsize, U1, I1,
                                                                               stat + 2);
   TRY(fmm_radix_sort<uint64_t>(U1, I1, U2, I2, ncls, 0, 64, uhist, uscan, st));
+  // same classes as the previous build (same ids): the per-class operator
+  // data of that build still holds and its kernels skip their work
+  TRY(fmm_reserve(t->d_cls_same, 1));
+  if ((int)ncls == t->ncls_prev && p == t->order_prev) {
+    FMM_CUDA_TRY(cudaMemsetAsync(t->d_cls_same.p, 0xff, sizeof(uint32_t), st));
+    fmm_note_launch(), k_keys_equal<<<fmm_blocks(ncls, 256), 256, 0, st>>>(U1, t->cls_prev.p, (int)ncls,
+                                                                          t->d_cls_same.p);
+  } else {
+    FMM_CUDA_TRY(cudaMemsetAsync(t->d_cls_same.p, 0, sizeof(uint32_t), st));
+  }
+  TRY(fmm_reserve(t->cls_prev, ncls > 0 ? ncls : 1));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->cls_prev.p, U1, sizeof(uint64_t) * ncls, cudaMemcpyDeviceToDevice, st));
+  t->ncls_prev = (int)ncls;
+  t->order_prev = p;
   fmm_note_launch(), k_class_rank<<<fmm_blocks(ncls, 256), 256, 0, st>>>(U1, (int)ncls, t->cls_hkeys.p, hsize - 1,
                                                                           t->cls_table.p, t->cls_key4.p);
   // raw classes go to the (finished) walk frontier buffer
@@ -846,10 +867,12 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   TRY(group_by_target(t, t->m2l_tgt_raw, t->m2l_src_raw, t->fa.p, (int)ncls, n, t->m2l_off, t->m2l_src,
                       t->m2l_cls.p, st));
   int nt = fmm_nterms(p);
+  if (t->cls_D.cap < (size_t)ncls * nt || t->cls_Df.cap < (size_t)ncls * fmm_stride4(nt))  // contents lost
+    FMM_CUDA_TRY(cudaMemsetAsync(t->d_cls_same.p, 0, sizeof(uint32_t), st));
   TRY(fmm_reserve(t->cls_D, (size_t)ncls * nt));
   TRY(fmm_reserve(t->cls_Df, (size_t)ncls * fmm_stride4(nt)));
   fmm_note_launch(), k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
-                                                                         t->cls_Df.p);
+                                                                         t->cls_Df.p, t->d_cls_same.p);
   FMM_CUDA_TRY(cudaGetLastError());
   // the M2L processing order (level, interaction pattern)
   size_t nbh = fmm_rs_nblocks(nc);
@@ -881,7 +904,8 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->m2l_off); fmm_release(t->m2l_src); fmm_release(t->m2l_cls); fmm_release(t->m2l_order);
   fmm_release(t->p2p_off); fmm_release(t->p2p_src);
   fmm_release(t->cls_key4); fmm_release(t->cls_D); fmm_release(t->cls_Df); fmm_release(t->cls_table);
-  fmm_release(t->cls_hkeys);
+  fmm_release(t->cls_hkeys); fmm_release(t->cls_prev); fmm_release(t->d_cls_same);
+  t->ncls_prev = t->order_prev = -1;
   fmm_release(t->M); fmm_release(t->L); fmm_release(t->Mf); fmm_release(t->Lf);
   fmm_release(t->Fnear); fmm_release(t->Ffar);
   fmm_release(t->fa); fmm_release(t->fb); fmm_release(t->fa2); fmm_release(t->fb2);

@@ -69,3 +69,22 @@ def test_tc_m2l_rebuild_refreshes_operators(fg):
     F64 = t.compute_field_fmm(precision="fp64").cpu().numpy()
     t.times()
     assert rel(Ftc[:, -3:], F64[:, -3:]) < 2e-6
+
+
+def test_tc_m2l_rebuild_same_classes(fg):
+    """A rebuild whose translation classes equal the previous build's reuses the
+    per-class operator data; results match a fresh tree bit for bit, also when
+    position sets alternate (A, B, A)."""
+    pa, S = system("uniform", 0, 20000, 11)
+    pb, _ = system("clustered", 0, 20000, 12)
+    t = fg.build_tree(pa, S, pa.shape[0], 64, 8, 0.5)
+    Fa = t.compute_field_fmm(precision="mixed").cpu().numpy()
+    t.rebuild(pa)
+    assert np.array_equal(t.compute_field_fmm(precision="mixed").cpu().numpy(), Fa)
+    t.rebuild(pb)
+    Fb = t.compute_field_fmm(precision="mixed").cpu().numpy()
+    t.rebuild(pa)
+    assert np.array_equal(t.compute_field_fmm(precision="mixed").cpu().numpy(), Fa)
+    fresh = fg.build_tree(pb, S, pb.shape[0], 64, 8, 0.5)
+    assert np.array_equal(fresh.compute_field_fmm(precision="mixed").cpu().numpy(), Fb)
+    t.times()
