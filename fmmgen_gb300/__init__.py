@@ -5,7 +5,7 @@ calls.  Compute runs in libfmmgen_gb300.so (hand-written CUDA); this package is
 the host-side binding.
 """
 from ._lib import FMMError, lib  # noqa: F401
-from .tree import Tree, build_tree, direct  # noqa: F401
+from .tree import Tree, build_forest, build_tree, direct  # noqa: F401
 from . import operators  # noqa: F401
 
-__all__ = ["Tree", "build_tree", "direct", "operators", "FMMError", "lib"]
+__all__ = ["Tree", "build_forest", "build_tree", "direct", "operators", "FMMError", "lib"]

@@ -49,12 +49,16 @@ _SIGS = {
     "P2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "fmmgen_tree_build": (C.c_int, [_dp, C.c_long, C.c_long, C.c_int, C.c_double, C.c_int, _vp,
                                     C.POINTER(C.c_void_p)]),
+    "fmmgen_forest_build": (C.c_int, [_dp, _lp, C.c_int, C.c_long, C.c_int, C.c_double, C.c_int, _vp,
+                                      C.POINTER(C.c_void_p)]),
     "fmmgen_tree_compute_field_fmm": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_gpu_direct": (C.c_int, [_dp, _dp, C.c_long, _lp, C.c_long, C.c_int, C.c_int, C.c_int, _dp, _vp]),
     "fmmgen_tree_free": (C.c_int, [_vp]),
     "fmmgen_root_box_noalloc": (C.c_int, [_dp, C.c_long, _dp, _vp]),
     "fmmgen_tree_info": (C.c_int, [_vp, _lp]),
     "fmmgen_tree_root": (C.c_int, [_vp, _dp]),
+    "fmmgen_tree_nsys": (C.c_int, [_vp]),
+    "fmmgen_tree_export_systems": (C.c_int, [_vp, _dp, _vp]),
     "fmmgen_tree_export_cells": (C.c_int, [_vp, _lp, _lp, _dp, _lp, _lp]),
     "fmmgen_tree_export_lists": (C.c_int, [_vp, _lp, _lp]),
     "fmmgen_tree_export_expansions": (C.c_int, [_vp, _dp, _dp]),

@@ -177,6 +177,19 @@ int fmmgen_tree_build(const double *pos, long N, long ncrit, int order, double t
   return ret(rc);
 }
 
+int fmmgen_forest_build(const double *pos, const long *sys_off, int nsys, long ncrit, int order, double theta,
+                        int so, void *stream, fmmgen_tree **tree) {
+  g_err.clear();
+  if (!tree || !sys_off || nsys < 1) return ret(FMM_ERR_ARG);
+  fmmgen_tree *h = *tree;
+  if (!h) h = new fmmgen_tree();
+  h->built = false;
+  int rc = fmm_tree_build(&h->t, pos, sys_off[nsys], ncrit, order, theta, so, S(stream), sys_off, nsys);
+  *tree = h;
+  if (rc == FMM_OK) h->built = true;
+  return ret(rc);
+}
+
 int fmmgen_tree_compute_field_fmm(fmmgen_tree *tree, const double *Sv, double *F, int potential, int field,
                                   int precision, void *stream) {
   g_err.clear();
@@ -207,6 +220,21 @@ int fmmgen_tree_info(fmmgen_tree *tree, long *info) {
   info[0] = t.ncells; info[1] = t.nleaves; info[2] = t.nm2l; info[3] = t.np2p;
   info[4] = t.nlevels; info[5] = t.nclasses; info[6] = t.N; info[7] = t.ncrit;
   info[8] = (long)t.p2p_interactions;
+  return FMM_OK;
+}
+
+int fmmgen_tree_nsys(fmmgen_tree *tree) {
+  if (!tree || !tree->built) return 0;
+  return tree->t.nsys;
+}
+
+int fmmgen_tree_export_systems(fmmgen_tree *tree, double *roots4, int *cell_system) {
+  g_err.clear();
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  if (roots4) FMM_CUDA_TRY(cudaMemcpy(roots4, t.roots.p, sizeof(double) * 4 * t.nsys, cudaMemcpyDeviceToHost));
+  if (cell_system) FMM_CUDA_TRY(cudaMemcpy(cell_system, t.csys.p, sizeof(int) * t.ncells, cudaMemcpyDeviceToHost));
   return FMM_OK;
 }
 
@@ -272,11 +300,11 @@ int fmmgen_tree_export_lists(fmmgen_tree *tree, unsigned long long *m2l, unsigne
 
 // M_n = M~_n s^|n|, L_n = L^_n / s^(|n|+1)
 template <typename T>
-__global__ void k_unscale(const T *Ms, const T *Ls, const unsigned char *clevel, const double *lev, int ncells,
+__global__ void k_unscale(const T *Ms, const T *Ls, const double *cr, int ncells,
                           int msize, int moff, int lsize, int mstr, int lstr, double *Mo, double *Lo) {
   int c = blockIdx.x;
   if (c >= ncells) return;
-  double s = lev[2 * clevel[c]];
+  double s = cr[c];
   for (int j = threadIdx.x; j < msize; j += blockDim.x) {
     int d = c_mi[j + moff][3];
     Mo[(size_t)c * msize + j] = (double)Ms[(size_t)c * mstr + j] * pow(s, d);
@@ -298,9 +326,9 @@ extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, doubl
   FMM_CUDA_TRY(cudaMalloc((void **)&dM, nc * ms * sizeof(double)));
   FMM_CUDA_TRY(cudaMalloc((void **)&dL, nc * ls * sizeof(double)));
   if (tree->last_precision == FMMGEN_PREC_FP64)
-    fmm_note_launch(), k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, ms, ls, dM, dL);
+    fmm_note_launch(), k_unscale<double><<<(unsigned)nc, 128>>>(t.M.p, t.L.p, t.cr.p, (int)nc, ms, moff, ls, ms, ls, dM, dL);
   else
-    fmm_note_launch(), k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.clevel.p, t.d_root.p + 16, (int)nc, ms, moff, ls, fmm_stride4(ms),
+    fmm_note_launch(), k_unscale<float><<<(unsigned)nc, 128>>>(t.Mf.p, t.Lf.p, t.cr.p, (int)nc, ms, moff, ls, fmm_stride4(ms),
                                                    fmm_stride4(ls), dM, dL);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(M, dM, nc * ms * sizeof(double), cudaMemcpyDeviceToHost);

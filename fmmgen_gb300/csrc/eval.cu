@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
                                                         const double *cx, const double *cy, const double *cz,
                                                         const double *px, const double *py, const double *pz,
                                                         const uint32_t *perm, const double *S, int so, int order,
-                                                        const double *lev, T *M, int mstr) {
+                                                        const double *cr, T *M, int mstr) {
   __shared__ T tb[FMM_WARPS][3][32][FMM_PMAX + 1];
   __shared__ T sq[FMM_WARPS][32][3];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
   if (leaf >= nleaves) return;
   const int c = leaf_cells[leaf];
   const int off = fmm_nterms(so - 1), msize = fmm_nterms(order) - off;
-  const double s = lev[2 * clevel[c]];
+  const double s = cr[c];
   const double inv_s = s > 0 ? 1.0 / s : 0.0;  // a zero-width root (coincident points) has no far field
   const double ccx = cx[c], ccy = cy[c], ccz = cz[c];
   const int p0 = pstart[c], np = pcount[c];
@@ -157,7 +157,7 @@ template <typename T>
 __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, int so, int order,
                                                         const unsigned char *child_mask, const int *child_first,
                                                         const unsigned char *clevel, const double *cx,
-                                                        const double *cy, const double *cz, const double *lev,
+                                                        const double *cy, const double *cz, const double *cr,
                                                         T *M, int mstr) {
   __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2m(Plan P, int lo, int hi, 
   unsigned mask = child_mask[c];
   if (!mask) return;
   const int off = fmm_nterms(so - 1), msize = fmm_nterms(order) - off;
-  const double inv_s = 1.0 / lev[2 * clevel[c]];
+  const double inv_s = 1.0 / cr[c];
   for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
   int ch = child_first[c];
   int nch = __popc(mask);
@@ -224,14 +224,14 @@ template <typename T>
 __global__ void __launch_bounds__(32 * FMM_WARPS) k_l2l(Plan P, int lo, int hi, int so, int order,
                                                         const int *parent, const unsigned char *clevel,
                                                         const double *cx, const double *cy, const double *cz,
-                                                        const double *lev, T *L, int lstr) {
+                                                        const double *cr, T *L, int lstr) {
   __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = lo + blockIdx.x * FMM_WARPS + w;
   if (c >= hi) return;
   const int p = parent[c];
   const int lsize = fmm_nterms(order - so);
-  const double inv_s = 1.0 / lev[2 * clevel[p]];
+  const double inv_s = 1.0 / cr[p];
   for (int k = lane; k < P.nseg; k += 32) sS[w][k] = T(0);
   warp_monomials<T>((cx[c] - cx[p]) * inv_s, (cy[c] - cy[p]) * inv_s, (cz[c] - cz[p]) * inv_s, order - so, sA[w],
                     lane);
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
                                                         const int *pcount, const unsigned char *clevel,
                                                         const double *cx, const double *cy, const double *cz,
                                                         const double *px, const double *py, const double *pz,
-                                                        int so, int order, const double *lev, const T *L,
+                                                        int so, int order, const double *cr, const T *L,
                                                         double *Ffar, int lstr) {
   __shared__ T sL[L2P_WARPS][FMM_NTMAX];
   __shared__ T tb[L2P_WARPS][3][FMM_PMAX + 1][33];
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
   if (leaf >= nleaves) return;
   const int c = leaf_cells[leaf];
   const int pl = order - so, lsize = fmm_nterms(pl);
-  const double s = lev[2 * clevel[c]], inv_s = s > 0 ? 1.0 / s : 0.0;
+  const double s = cr[c], inv_s = s > 0 ? 1.0 / s : 0.0;
   for (int j = lane; j < lsize; j += 32) sL[w][j] = s > 0 ? L[(size_t)c * lstr + j] : T(0);
   __syncwarp();
   const int p0 = pstart[c], np = pcount[c];
@@ -329,19 +329,19 @@ template <typename T>
 static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, bool tc, int mstr,
                     int lstr, int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so;
-  const double *lev = t->d_root.p + 16;
+  const double *cr = t->cr.p;  // per-cell half-widths
   const int nl = t->nleaves, nc = t->ncells;
   // P2M
   fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
       t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
-      t->pz.p, t->perm.p, S, so, p, lev, M, mstr);
+      t->pz.p, t->perm.p, S, so, p, cr, M, mstr);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 1, st));
   // M2M, deepest parents first
   for (int l = t->nlevels - 2; l >= 0; l--) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
     fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, M,
+        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, M,
         mstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
@@ -376,14 +376,14 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   for (int l = 1; l < t->nlevels; l++) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
     fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        ps->l2l, lo, hi, so, p, t->parent.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, lev, L, lstr);
+        ps->l2l, lo, hi, so, p, t->parent.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, L, lstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 5, st));
   // L2P
   fmm_note_launch(), k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(
       t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
-      t->pz.p, so, p, lev, L, t->Ffar.p, lstr);
+      t->pz.p, so, p, cr, L, t->Ffar.p, lstr);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 6, st));
   return FMM_OK;

@@ -28,6 +28,11 @@ const PlanSet *fmm_get_plans(int order, int so);  // cached per device
 struct DevTree {
   // configuration
   long N = 0, ncrit = 0;
+  int nsys = 1;                           // independent systems (a forest when > 1)
+  std::vector<long> sys_off_h;            // particle offsets of the systems in the caller's order, nsys + 1
+  DevBuf<long> sys_off;                   // the same on the device
+  DevBuf<int> psys;                       // system of each particle in the caller's order (forests)
+  DevBuf<double> roots;                   // per system: root cube (cx, cy, cz, r)
   int order = 0, so = 0;
   double theta = 0;
   int dev = 0;
@@ -51,6 +56,10 @@ struct DevTree {
   DevBuf<double> cx, cy, cz;
   DevBuf<uint64_t> cid;                   // (1 << 3*level) | octant path
   DevBuf<int> ix, iy, iz;                 // integer cell coordinates at the cell's level
+  DevBuf<double> cr, crmax;               // half-width and rmax = sqrt(3 r r) (the reference's FP64 values)
+  DevBuf<float2> crf;                     // half-width as an FP32 (hi, lo) pair
+  DevBuf<float> cmargin;                  // walk: relative MAC band decided in FP64 for pairs this cell refines
+  DevBuf<int> csys;                       // system of the cell (forests of independent systems)
   DevBuf<int> pstart, pcount, parent, child_first;
   DevBuf<unsigned char> child_mask, clevel;
   DevBuf<int> leaf_cells;                 // leaf cell indices
@@ -86,7 +95,6 @@ struct DevTree {
   uint64_t build_serial = 0, tc_serial = ~0ull;  // tc_T belongs to the build with this serial
   int tc_order = -1, tc_so = -1;          // ... and to this expansion order and source order
   DevBuf<unsigned char> wdec;             // decision of each frontier pair
-  DevBuf<float> wmargin;                  // MAC band decided in FP64, per level
   DevBuf<char> tmp;                       // scan / sort / misc scratch
   DevBuf<uint32_t> d_eflags;
   DevBuf<double> d_root;                  // sums / maxima for the root box
@@ -97,8 +105,10 @@ struct DevTree {
   bool ev_ready = false;
 };
 
+// sys_off: nullptr for one system, else nsys + 1 host offsets of the systems'
+// particles in pos (a forest: one root cube and tree per system, one pass)
 int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
-                   cudaStream_t st);
+                   cudaStream_t st, const long *sys_off = nullptr, int nsys = 1);
 int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
                       cudaStream_t st);
 void fmm_tree_destroy(DevTree *t);

@@ -203,7 +203,7 @@ __device__ __forceinline__ void p2p_dipole(const float4 *sh, const float4 *sl, c
 __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
                                                           const int *pcount, const int *off_, const int *src,
                                                           const int *ix, const int *iy, const int *iz,
-                                                          const unsigned char *clevel, const float2 *levf,
+                                                          const unsigned char *clevel, const float2 *crf,
                                                           const float4 *phi4, const float4 *plo4,
                                                           const float4 *sdip, int so, double *Fnear) {
   __shared__ float4 sh[P2P_WARPS][32], sl[P2P_WARPS][32], sd[P2P_WARPS][32];
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
       const int B = src[k];
       const int b0 = pstart[B], nb = pcount[B];
       const int lb = clevel[B], L = max(la, lb);
-      const float2 sc = levf[L];
+      const float2 sc = crf[la >= lb ? A : B];  // half-width at the finer level L
       float oxh, oxl, oyh, oyl, ozh, ozl;
       offset2((iax << (L - la)) - ((2 * ix[B] + 1) << (L - lb)), sc, oxh, oxl);
       offset2((iay << (L - la)) - ((2 * iy[B] + 1) << (L - lb)), sc, oyh, oyl);
@@ -291,7 +291,7 @@ int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st) {
   if (mixed)
     fmm_note_launch(), k_p2p32<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->ix.p, t->iy.p, t->iz.p,
-        t->clevel.p, t->levf.p, t->phi4.p, t->plo4.p, t->sdip.p, so, t->Fnear.p);
+        t->clevel.p, t->crf.p, t->phi4.p, t->plo4.p, t->sdip.p, so, t->Fnear.p);
   else
     fmm_note_launch(), k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->px.p, t->py.p, t->pz.p,

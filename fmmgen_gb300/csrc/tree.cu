@@ -77,10 +77,11 @@ __global__ void k_root_final(const double *sums, const unsigned long long *mx, l
 // ---------------------------------------------------------------------------
 // per-particle octant keys (example/tree.cpp:94-98, 189-204)
 // ---------------------------------------------------------------------------
-__global__ void k_keys(const double *__restrict__ pos, long N, const double *root, uint64_t *keys,
-                       uint32_t *idx) {
+__global__ void k_keys(const double *__restrict__ pos, long N, const double *roots, const int *psys,
+                       uint64_t *keys, uint32_t *idx) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= N) return;
+  const double *root = roots + 4 * (psys ? psys[i] : 0);  // the particle's system's root cube
   double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
   double cx = root[0], cy = root[1], cz = root[2], r = root[3];
   uint64_t key = 0;
@@ -124,12 +125,98 @@ __device__ __forceinline__ int lower_digit(const uint64_t *keys, int lo, int hi,
   return lo;
 }
 
-__global__ void k_init_root_cell(const double *root, long N, double *cx, double *cy, double *cz, uint64_t *cid,
-                                 int *ix, int *iy, int *iz, int *pstart, int *pcount, int *parent,
-                                 int *child_first, unsigned char *child_mask, unsigned char *clevel) {
-  cx[0] = root[0]; cy[0] = root[1]; cz[0] = root[2];
-  cid[0] = 1; ix[0] = iy[0] = iz[0] = 0;
-  pstart[0] = 0; pcount[0] = (int)N; parent[0] = -1; child_first[0] = -1; child_mask[0] = 0; clevel[0] = 0;
+// half-width r of a cell, its rmax = sqrt(3 r r) as the reference computes it
+// (example/tree.cpp:15), and r as an FP32 (hi, lo) pair
+__device__ __forceinline__ void set_radius(int c, double r, double *cr, double *crmax, float2 *crf) {
+  cr[c] = r;
+  crmax[c] = __dsqrt_rn(__dmul_rn(__dmul_rn(3.0, r), r));
+  const float hi = (float)r;
+  crf[c] = make_float2(hi, (float)(r - (double)hi));
+}
+
+// Level 0: one root cell per system; in sorted order system s holds the
+// particles [sys_off[s], sys_off[s + 1]).
+__global__ void k_init_roots(int nsys, const double *roots, const long *sys_off, double *cx, double *cy,
+                             double *cz, uint64_t *cid, int *ix, int *iy, int *iz, int *pstart, int *pcount,
+                             int *parent, int *child_first, unsigned char *child_mask, unsigned char *clevel,
+                             double *cr, double *crmax, float2 *crf, int *csys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const double *rt = roots + 4 * s;
+  cx[s] = rt[0]; cy[s] = rt[1]; cz[s] = rt[2];
+  cid[s] = 1; ix[s] = iy[s] = iz[s] = 0;
+  pstart[s] = (int)sys_off[s]; pcount[s] = (int)(sys_off[s + 1] - sys_off[s]);
+  parent[s] = -1; child_first[s] = -1; child_mask[s] = 0; clevel[s] = 0;
+  set_radius(s, rt[3], cr, crmax, crf);
+  csys[s] = s;
+}
+
+// ---------------------------------------------------------------------------
+// forests: per-system root cubes (example/tree.cpp:139-187 for each system)
+// ---------------------------------------------------------------------------
+__global__ void k_fill_psys(const long *sys_off, int *psys) {
+  const int s = blockIdx.x;
+  for (long i = sys_off[s] + threadIdx.x; i < sys_off[s + 1]; i += blockDim.x) psys[i] = s;
+}
+// The reference's three sequential FP64 sums, one thread per (system, axis).
+__global__ void k_seg_sums(const double *pos, const long *sys_off, int nsys, double *sums) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * nsys) return;
+  const int s = t / 3, ax = t - 3 * s;
+  double acc = 0.0;
+  const long e = sys_off[s + 1];
+  for (long i = sys_off[s]; i < e; i++) acc = __dadd_rn(acc, pos[3 * i + ax]);
+  sums[t] = acc;
+}
+// max |x - mean| per system and axis (order-independent), one block per system
+__global__ void k_seg_absmax(const double *pos, const long *sys_off, const double *sums, unsigned long long *mx) {
+  const int s = blockIdx.x;
+  const long b = sys_off[s], e = sys_off[s + 1];
+  const double n = (double)(e - b);
+  const double ax = __ddiv_rn(sums[3 * s], n), ay = __ddiv_rn(sums[3 * s + 1], n), az = __ddiv_rn(sums[3 * s + 2], n);
+  double m0 = 0, m1 = 0, m2 = 0;
+  for (long i = b + threadIdx.x; i < e; i += blockDim.x) {
+    m0 = fmax(m0, fabs(__dsub_rn(pos[3 * i], ax)));
+    m1 = fmax(m1, fabs(__dsub_rn(pos[3 * i + 1], ay)));
+    m2 = fmax(m2, fabs(__dsub_rn(pos[3 * i + 2], az)));
+  }
+  for (int d = 16; d; d >>= 1) {
+    m0 = fmax(m0, __shfl_xor_sync(0xffffffffu, m0, d));
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, d));
+    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, d));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(&mx[3 * s], (unsigned long long)__double_as_longlong(m0));
+    atomicMax(&mx[3 * s + 1], (unsigned long long)__double_as_longlong(m1));
+    atomicMax(&mx[3 * s + 2], (unsigned long long)__double_as_longlong(m2));
+  }
+}
+__global__ void k_seg_root_final(int nsys, const long *sys_off, const double *sums, const unsigned long long *mx,
+                                 double *roots) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const double n = (double)(sys_off[s + 1] - sys_off[s]);
+  const double ax = __ddiv_rn(sums[3 * s], n), ay = __ddiv_rn(sums[3 * s + 1], n), az = __ddiv_rn(sums[3 * s + 2], n);
+  const double xm = __longlong_as_double((long long)mx[3 * s]);
+  const double ym = __longlong_as_double((long long)mx[3 * s + 1]);
+  const double zm = __longlong_as_double((long long)mx[3 * s + 2]);
+  roots[4 * s] = ax; roots[4 * s + 1] = ay; roots[4 * s + 2] = az;
+  roots[4 * s + 3] = __dmul_rn((xm > ym ? (xm > zm ? xm : zm) : (ym > zm ? ym : zm)), 1.001);
+}
+// sorted position -> system, for the stable sort by system after the key sort
+__global__ void k_sorted_sys(const uint32_t *perm, const int *psys, long N, uint32_t *ks, uint32_t *idx) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  ks[i] = (uint32_t)psys[perm[i]];
+  idx[i] = (uint32_t)i;
+}
+__global__ void k_apply_order(const uint32_t *idx, long N, const uint64_t *kin, const uint32_t *pin, uint64_t *kout,
+                              uint32_t *pout) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  kout[i] = kin[idx[i]];
+  pout[i] = pin[idx[i]];
 }
 
 __global__ void k_count_children(int lo, int hi, int level, long ncrit, const uint64_t *keys, const int *pstart,
@@ -157,18 +244,19 @@ __global__ void k_count_children(int lo, int hi, int level, long ncrit, const ui
   cnt[c - lo] = n;
 }
 
-__global__ void k_write_children(int lo, int hi, int level, const double *lev, const uint64_t *keys,
-                                 const uint32_t *off, double *cx, double *cy, double *cz, uint64_t *cid,
-                                 int *ix, int *iy, int *iz, int *pstart, int *pcount, int *parent,
-                                 int *child_first, const unsigned char *child_mask_in,
-                                 unsigned char *child_mask, unsigned char *clevel) {
+__global__ void k_write_children(int lo, int hi, int level, const uint64_t *keys, const uint32_t *off, double *cx,
+                                 double *cy, double *cz, uint64_t *cid, int *ix, int *iy, int *iz, int *pstart,
+                                 int *pcount, int *parent, int *child_first, const unsigned char *child_mask_in,
+                                 unsigned char *child_mask, unsigned char *clevel, double *cr, double *crmax,
+                                 float2 *crf, int *csys) {
   int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= hi) return;
   unsigned mask = child_mask_in[c];
   if (!mask) { child_first[c] = -1; return; }
   int first = hi + (int)off[c - lo];
   child_first[c] = first;
-  double r = lev[2 * (level + 1)];  // child half-width = parent r / 2.0
+  const double r = __ddiv_rn(cr[c], 2.0);  // child half-width = parent r / 2.0 (example/tree.cpp:95)
+  const int sys = csys[c];
   double px = cx[c], py = cy[c], pz = cz[c];
   int s = pstart[c], e = s + pcount[c];
   int b = s, j = first;
@@ -189,6 +277,8 @@ __global__ void k_write_children(int lo, int hi, int level, const double *lev, c
       child_first[j] = -1;
       child_mask[j] = 0;
       clevel[j] = (unsigned char)(level + 1);
+      set_radius(j, r, cr, crmax, crf);
+      csys[j] = sys;
       j++;
     }
     b = nb;
@@ -211,11 +301,11 @@ __global__ void k_leaf_compact(int ncells, long ncrit, const int *pcount, const 
 // dual-tree walk (example/calculate.cpp:81-133), breadth-first
 // ---------------------------------------------------------------------------
 struct WalkCells {
-  const double *cx, *cy, *cz, *lev;
+  const double *cx, *cy, *cz, *crmax;
   const unsigned char *mask, *clevel;
   const int *child_first;
   const int *ix, *iy, *iz;
-  const float *margin;  // per finer level: relative band around the MAC boundary decided in FP64
+  const float *margin;  // per cell: relative band around the MAC boundary decided in FP64
   float theta2;
 };
 
@@ -236,7 +326,7 @@ __device__ __forceinline__ int walk_decide(const WalkCells &W, int A, int B, dou
   const long long n2 = gx * gx + gy * gy + gz * gz;
   const long long base = (1ll << sa) + (1ll << sb);
   const float rho = (float)n2 * W.theta2 / (3.f * (float)(base * base));
-  const float m = W.margin[L];
+  const float m = W.margin[la >= lb ? A : B];  // the band of the finer cell's level
   bool mac;
   if (rho > 1.f + m) mac = true;
   else if (rho < 1.f - m) mac = false;
@@ -245,7 +335,7 @@ __device__ __forceinline__ int walk_decide(const WalkCells &W, int A, int B, dou
     double dy = __dsub_rn(W.cy[A], W.cy[B]);
     double dz = __dsub_rn(W.cz[A], W.cz[B]);
     double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-    double ra = W.lev[2 * la + 1], rb = W.lev[2 * lb + 1];
+    double ra = W.crmax[A], rb = W.crmax[B];
     mac = __dmul_rn(R, theta) > __dadd_rn(ra, rb);
   }
   if (mac) return 0;
@@ -255,15 +345,23 @@ __device__ __forceinline__ int walk_decide(const WalkCells &W, int A, int B, dou
   return 3;
 }
 
-// margin[l] for pairs whose finer level is l: FP32 evaluation error plus a bound
-// on how far FP64 centre rounding can move R relative to the level half-width
-__global__ void k_walk_margins(const double *root, const double *lev, double theta, float *margin) {
-  int l = threadIdx.x;
-  if (l > FMM_MAXLEVEL) return;
-  double cmax = fmax(fmax(fabs(root[0]), fabs(root[1])), fabs(root[2])) + root[3];
-  double s = lev[2 * l];
-  double m = 1e-5 + 64.0 * ldexp(1.0, -52) * cmax / s * fmax(1.0, theta);
-  margin[l] = s > 0 && m < 0.01 ? (float)m : 1e30f;  // 1e30: always decide in FP64
+// margin of each cell, for pairs in which it is the finer cell: FP32 evaluation
+// error plus a bound on how far FP64 centre rounding can move R relative to the
+// cell half-width (from its system's root cube)
+__global__ void k_cell_margins(int nc, const int *csys, const double *roots, const double *cr, double theta,
+                               float *margin) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const double *rt = roots + 4 * csys[c];
+  const double cmax = fmax(fmax(fabs(rt[0]), fabs(rt[1])), fabs(rt[2])) + rt[3];
+  const double s = cr[c];
+  const double m = 1e-5 + 64.0 * ldexp(1.0, -52) * cmax / s * fmax(1.0, theta);
+  margin[c] = s > 0 && m < 0.01 ? (float)m : 1e30f;  // 1e30: always decide in FP64
+}
+
+__global__ void k_root_pairs(int nsys, int *fa, int *fb) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) fa[s] = fb[s] = s;
 }
 
 __global__ void k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, U3 *cnt,
@@ -499,6 +597,7 @@ template <typename T> static int grow_keep(DevBuf<T> &b, size_t need, size_t use
 }
 
 static int tmp_reserve(DevTree *t, size_t bytes) { return fmm_reserve(t->tmp, bytes); }
+static int bits_for(long n);
 
 #define TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
 
@@ -514,11 +613,19 @@ static int build_lists(DevTree *t, cudaStream_t st);
 static int build_classes(DevTree *t, cudaStream_t st);
 
 int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
-                   cudaStream_t st) {
+                   cudaStream_t st, const long *sys_off, int nsys) {
   if (N < 1 || N >= (1L << 31) - 1 || ncrit < 1 || order < so + 1 || order > FMM_PMAX || so < 0 || so > 1 ||
-      !(theta > 0) || !pos)
+      !(theta > 0) || !pos || nsys < 1 || (nsys > 1 && !sys_off))
     return FMM_ERR_ARG;
+  if (sys_off) {
+    if (sys_off[0] != 0 || sys_off[nsys] != N) return FMM_ERR_ARG;
+    for (int k = 0; k < nsys; k++)
+      if (sys_off[k + 1] <= sys_off[k]) return FMM_ERR_ARG;  // every system holds particles
+  }
   t->N = N; t->ncrit = ncrit; t->order = order; t->so = so; t->theta = theta;
+  t->nsys = nsys;
+  if (sys_off) t->sys_off_h.assign(sys_off, sys_off + nsys + 1);
+  else t->sys_off_h = {0, N};
   FMM_CUDA_TRY(cudaGetDevice(&t->dev));
   if (!t->ev_ready) {
     for (int i = 0; i < 16; i++) FMM_CUDA_TRY(cudaEventCreate(&t->ev[i]));
@@ -532,36 +639,68 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
   TRY(rec(t, 0, st));
   TRY(fmm_reserve(t->d_eflags, 4));
   FMM_CUDA_TRY(cudaMemsetAsync(t->d_eflags.p, 0, sizeof(uint32_t), st));
-  // d_root: [0..2] sums, [3..5] maxima (u64 bits), [6..9] root box, [10..] level r/rmax
+  TRY(fmm_reserve(t->sys_off, (size_t)nsys + 1));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->sys_off.p, t->sys_off_h.data(), sizeof(long) * (nsys + 1),
+                               cudaMemcpyHostToDevice, st));
+  TRY(fmm_reserve(t->roots, 4 * (size_t)nsys));
+  // d_root: [0..2] sums, [3..5] maxima (u64 bits), [6..9] root box, [16..] level r/rmax
   TRY(fmm_reserve(t->d_root, 16 + 2 * (FMM_MAXLEVEL + 1)));
   double *dr = t->d_root.p;
-  FMM_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * 16, st));
-  TRY(tmp_reserve(t, fmm_seqsum_scratch(N)));
-  TRY(fmm_seqsum3(pos, N, dr, t->tmp.p, st));
-  unsigned nbm = std::min<unsigned>(fmm_blocks(N, 256), 152 * 8);
-  fmm_note_launch(), k_root_absmax<<<nbm, 256, 0, st>>>(pos, N, dr, (unsigned long long *)(dr + 3));
-  TRY(fmm_reserve(t->levf, FMM_MAXLEVEL + 1));
-  fmm_note_launch(), k_root_final<<<1, 1, 0, st>>>(dr, (const unsigned long long *)(dr + 3), N, dr + 6, dr + 16,
-                                                   t->levf.p);
+  if (nsys == 1) {
+    // one system: the exact sequential mean through fmm_seqsum3 (parallel)
+    FMM_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * 16, st));
+    TRY(tmp_reserve(t, fmm_seqsum_scratch(N)));
+    TRY(fmm_seqsum3(pos, N, dr, t->tmp.p, st));
+    unsigned nbm = std::min<unsigned>(fmm_blocks(N, 256), 152 * 8);
+    fmm_note_launch(), k_root_absmax<<<nbm, 256, 0, st>>>(pos, N, dr, (unsigned long long *)(dr + 3));
+    TRY(fmm_reserve(t->levf, FMM_MAXLEVEL + 1));
+    fmm_note_launch(), k_root_final<<<1, 1, 0, st>>>(dr, (const unsigned long long *)(dr + 3), N, t->roots.p,
+                                                     dr + 16, t->levf.p);
+  } else {
+    // a forest: each system's sums by one thread (systems run side by side)
+    TRY(fmm_reserve(t->psys, N));
+    fmm_note_launch(), k_fill_psys<<<nsys, 256, 0, st>>>(t->sys_off.p, t->psys.p);
+    TRY(tmp_reserve(t, sizeof(double) * 6 * (size_t)nsys + 64));
+    double *sums = (double *)t->tmp.p;
+    unsigned long long *mx = (unsigned long long *)(sums + 3 * (size_t)nsys);
+    FMM_CUDA_TRY(cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * 3 * nsys, st));
+    fmm_note_launch(), k_seg_sums<<<fmm_blocks(3 * (size_t)nsys, 128), 128, 0, st>>>(pos, t->sys_off.p, nsys, sums);
+    fmm_note_launch(), k_seg_absmax<<<nsys, 256, 0, st>>>(pos, t->sys_off.p, sums, mx);
+    fmm_note_launch(), k_seg_root_final<<<fmm_blocks(nsys, 128), 128, 0, st>>>(nsys, t->sys_off.p, sums, mx,
+                                                                                t->roots.p);
+  }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 1, st));
 
   // keys + stable sort
   TRY(fmm_reserve(t->keys, N)); TRY(fmm_reserve(t->keys2, N));
   TRY(fmm_reserve(t->perm, N)); TRY(fmm_reserve(t->perm2, N));
-  fmm_note_launch(), k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, dr + 6, t->keys.p, t->perm.p);
+  fmm_note_launch(), k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, t->roots.p, nsys > 1 ? t->psys.p : nullptr,
+                                                                 t->keys.p, t->perm.p);
   FMM_CUDA_TRY(cudaGetLastError());
   size_t nbh = fmm_rs_nblocks(N);
   size_t hist_n = 256 * nbh;
-  size_t tmp_bytes = hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 1024;
-  TRY(tmp_reserve(t, tmp_bytes));
+  const size_t sort_bytes = hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 1024;
+  TRY(tmp_reserve(t, sort_bytes + (nsys > 1 ? 16 * (size_t)N : 0)));
   uint32_t *hist = (uint32_t *)t->tmp.p;
   uint32_t *scantmp = hist + hist_n;
   TRY(fmm_radix_sort(t->keys.p, t->perm.p, t->keys2.p, t->perm2.p, N, 0, 3 * FMM_MAXLEVEL, hist, scantmp, st));
+  if (nsys > 1) {
+    // stable sort by system: (system, key) order, each system's particles contiguous
+    uint32_t *ks = (uint32_t *)(t->tmp.p + sort_bytes);
+    uint32_t *idx = ks + N, *ks2 = idx + N, *idx2 = ks2 + N;
+    fmm_note_launch(), k_sorted_sys<<<fmm_blocks(N, 256), 256, 0, st>>>(t->perm.p, t->psys.p, N, ks, idx);
+    TRY(fmm_radix_sort<uint32_t>(ks, idx, ks2, idx2, N, 0, bits_for(nsys), hist, scantmp, st));
+    fmm_note_launch(), k_apply_order<<<fmm_blocks(N, 256), 256, 0, st>>>(idx, N, t->keys.p, t->perm.p, t->keys2.p,
+                                                                         t->perm2.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    std::swap(t->keys, t->keys2);
+    std::swap(t->perm, t->perm2);
+  }
   TRY(fmm_reserve(t->px, N)); TRY(fmm_reserve(t->py, N)); TRY(fmm_reserve(t->pz, N));
   fmm_note_launch(), k_gather_pos<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, t->perm.p, N, t->px.p, t->py.p, t->pz.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  FMM_CUDA_TRY(cudaMemcpyAsync(&t->root, dr + 6, sizeof(RootBox), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaMemcpyAsync(&t->root, t->roots.p, sizeof(RootBox), cudaMemcpyDeviceToHost, st));  // system 0
   TRY(rec(t, 2, st));
 
   TRY(build_cells(t, st));
@@ -588,20 +727,23 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
 
 static int build_cells(DevTree *t, cudaStream_t st) {
   long N = t->N;
-  size_t cap = (size_t)(4 * N / std::max<long>(t->ncrit, 1)) + 1024;
+  const int nsys = t->nsys;
+  size_t cap = (size_t)(4 * N / std::max<long>(t->ncrit, 1)) + 1024 + nsys;
   TRY(fmm_reserve(t->cx, cap)); TRY(fmm_reserve(t->cy, cap)); TRY(fmm_reserve(t->cz, cap));
   TRY(fmm_reserve(t->cid, cap)); TRY(fmm_reserve(t->ix, cap)); TRY(fmm_reserve(t->iy, cap));
   TRY(fmm_reserve(t->iz, cap)); TRY(fmm_reserve(t->pstart, cap)); TRY(fmm_reserve(t->pcount, cap));
   TRY(fmm_reserve(t->parent, cap)); TRY(fmm_reserve(t->child_first, cap));
   TRY(fmm_reserve(t->child_mask, cap)); TRY(fmm_reserve(t->clevel, cap));
-  double *dr = t->d_root.p;
-  fmm_note_launch(), k_init_root_cell<<<1, 1, 0, st>>>(dr + 6, N, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
-                                    t->pstart.p, t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p,
-                                    t->clevel.p);
+  TRY(fmm_reserve(t->cr, cap)); TRY(fmm_reserve(t->crmax, cap)); TRY(fmm_reserve(t->crf, cap));
+  TRY(fmm_reserve(t->csys, cap));
+  fmm_note_launch(), k_init_roots<<<fmm_blocks(nsys, 128), 128, 0, st>>>(
+      nsys, t->roots.p, t->sys_off.p, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p, t->pstart.p,
+      t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p, t->clevel.p, t->cr.p, t->crmax.p, t->crf.p,
+      t->csys.p);
   FMM_CUDA_TRY(cudaGetLastError());
   t->level_off.assign(1, 0);
-  t->level_off.push_back(1);
-  int lo = 0, hi = 1, level = 0;
+  t->level_off.push_back(nsys);
+  int lo = 0, hi = nsys, level = 0;
   uint32_t *h_total = t->h_pinned;
   int rc = FMM_OK;
   while (true) {
@@ -626,11 +768,14 @@ static int build_cells(DevTree *t, cudaStream_t st) {
         (rc = grow_keep(t->iz, need_cells, used, st)) || (rc = grow_keep(t->pstart, need_cells, used, st)) ||
         (rc = grow_keep(t->pcount, need_cells, used, st)) || (rc = grow_keep(t->parent, need_cells, used, st)) ||
         (rc = grow_keep(t->child_first, need_cells, used, st)) ||
-        (rc = grow_keep(t->child_mask, need_cells, used, st)) || (rc = grow_keep(t->clevel, need_cells, used, st)))
+        (rc = grow_keep(t->child_mask, need_cells, used, st)) || (rc = grow_keep(t->clevel, need_cells, used, st)) ||
+        (rc = grow_keep(t->cr, need_cells, used, st)) || (rc = grow_keep(t->crmax, need_cells, used, st)) ||
+        (rc = grow_keep(t->crf, need_cells, used, st)) || (rc = grow_keep(t->csys, need_cells, used, st)))
       break;
     fmm_note_launch(), k_write_children<<<fmm_blocks(n, 128), 128, 0, st>>>(
-        lo, hi, level, dr + 16, t->keys.p, cnt, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p,
-        t->pstart.p, t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p, t->child_mask.p, t->clevel.p);
+        lo, hi, level, t->keys.p, cnt, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p, t->pstart.p,
+        t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p, t->child_mask.p, t->clevel.p, t->cr.p,
+        t->crmax.p, t->crf.p, t->csys.p);
     if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
     lo = hi;
     hi = hi + (int)nnew;
@@ -656,6 +801,10 @@ static int build_cells(DevTree *t, cudaStream_t st) {
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
   t->nleaves = (int)t->h_pinned[0];
+  TRY(fmm_reserve(t->cmargin, nc));
+  fmm_note_launch(), k_cell_margins<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->csys.p, t->roots.p, t->cr.p,
+                                                                          t->theta, t->cmargin.p);
+  FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
 
@@ -711,25 +860,24 @@ static int group_by_target(DevTree *t, DevBuf<int> &tgt_raw, DevBuf<int> &src_ra
 
 static int build_lists(DevTree *t, cudaStream_t st) {
   int nc = t->ncells;
-  TRY(fmm_reserve(t->wmargin, FMM_MAXLEVEL + 1));
-  fmm_note_launch(), k_walk_margins<<<1, 32, 0, st>>>(t->d_root.p + 6, t->d_root.p + 16, t->theta, t->wmargin.p);
-  WalkCells W{t->cx.p, t->cy.p, t->cz.p, t->d_root.p + 16, t->child_mask.p, t->clevel.p, t->child_first.p,
-              t->ix.p, t->iy.p, t->iz.p, t->wmargin.p, (float)(t->theta * t->theta)};
+  WalkCells W{t->cx.p, t->cy.p, t->cz.p, t->crmax.p, t->child_mask.p, t->clevel.p, t->child_first.p,
+              t->ix.p, t->iy.p, t->iz.p, t->cmargin.p, (float)(t->theta * t->theta)};
   // raw lists in walk order; the buffers keep their capacity between builds,
   // so a rebuild of a similar tree allocates nothing
   DevBuf<int> &m2l_src_raw = t->m2l_src_raw, &m2l_tgt_raw = t->m2l_tgt_raw;
   DevBuf<int> &p2p_tgt_raw = t->p2p_tgt_raw, &p2p_src_raw = t->p2p_src_raw;
-  size_t cap_pairs = (size_t)nc * 64 + 1024;
+  size_t cap_pairs = (size_t)nc * 64 + 1024 + t->nsys;
   TRY(fmm_reserve(t->fa, cap_pairs)); TRY(fmm_reserve(t->fb, cap_pairs));
   TRY(fmm_reserve(t->fa2, cap_pairs)); TRY(fmm_reserve(t->fb2, cap_pairs));
   TRY(fmm_reserve(m2l_src_raw, cap_pairs)); TRY(fmm_reserve(m2l_tgt_raw, cap_pairs));
   TRY(fmm_reserve(p2p_tgt_raw, cap_pairs)); TRY(fmm_reserve(p2p_src_raw, cap_pairs));
   int rc = FMM_OK;
   long nm2l = 0, np2p = 0;
-  uint32_t nf = 1;
+  // the walk starts from each system's (root, root) pair
+  uint32_t nf = (uint32_t)t->nsys;
   U3 *h_tot = (U3 *)t->h_pinned;
-  FMM_CUDA_TRY(cudaMemsetAsync(t->fa.p, 0, sizeof(int), st));
-  FMM_CUDA_TRY(cudaMemsetAsync(t->fb.p, 0, sizeof(int), st));
+  fmm_note_launch(), k_root_pairs<<<fmm_blocks(nf, 256), 256, 0, st>>>((int)nf, t->fa.p, t->fb.p);
+  FMM_CUDA_TRY(cudaGetLastError());
   while (nf > 0) {
     size_t need = (size_t)nf * sizeof(U3) + fmm_scan_tmp_elems<U3>(nf) * sizeof(U3) + 2 * sizeof(U3);
     if ((rc = tmp_reserve(t, need))) break;
@@ -914,7 +1062,9 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->tc_T); fmm_release(t->tc_Mh); fmm_release(t->tc_Ml); fmm_release(t->tc_mexp);
   fmm_release(t->d_tcerr);
   t->tc_serial = ~0ull;
-  fmm_release(t->wdec); fmm_release(t->wmargin);
+  fmm_release(t->wdec);
+  fmm_release(t->cr); fmm_release(t->crmax); fmm_release(t->crf); fmm_release(t->cmargin); fmm_release(t->csys);
+  fmm_release(t->sys_off); fmm_release(t->psys); fmm_release(t->roots);
   fmm_release(t->tmp); fmm_release(t->d_eflags); fmm_release(t->d_root);
   if (t->h_pinned) cudaFreeHost(t->h_pinned);
   t->h_pinned = nullptr;

@@ -47,9 +47,11 @@ def outputsize(potential=True, field=True):
 class Tree:
     """Device octree + interaction lists for fixed particle positions."""
 
-    def __init__(self, pos, S, ncrit, order, theta, source_order=0, stream=None):
+    def __init__(self, pos, S, ncrit, order, theta, source_order=0, stream=None, sys_off=None):
         if source_order not in (0, 1):
             raise ValueError("source_order must be 0 (charges) or 1 (dipoles)")
+        # a forest of independent systems when sys_off (nsys + 1 particle offsets) is given
+        self.sys_off = None if sys_off is None else np.ascontiguousarray(sys_off, dtype=np.int64)
         self.pos = _as_device(pos, (3,))
         self.N = self.pos.shape[0]
         self.S = _as_device(S, (sourcesize(source_order),)) if S is not None else None
@@ -64,8 +66,15 @@ class Tree:
         if pos is not None:
             self.pos = _as_device(pos, (3,))
             self.N = self.pos.shape[0]
-        check(lib().fmmgen_tree_build(C.c_void_p(self.pos.data_ptr()), self.N, self.ncrit, self.order, self.theta,
-                                      self.source_order, _stream_ptr(stream), C.byref(self._h)))
+        if self.sys_off is None:
+            check(lib().fmmgen_tree_build(C.c_void_p(self.pos.data_ptr()), self.N, self.ncrit, self.order,
+                                          self.theta, self.source_order, _stream_ptr(stream), C.byref(self._h)))
+        else:
+            if self.sys_off[-1] != self.N:
+                raise ValueError("the system offsets must end at N")
+            check(lib().fmmgen_forest_build(C.c_void_p(self.pos.data_ptr()), self.sys_off.ctypes.data,
+                                            len(self.sys_off) - 1, self.ncrit, self.order, self.theta,
+                                            self.source_order, _stream_ptr(stream), C.byref(self._h)))
         info = np.zeros(9, dtype=np.int64)
         check(lib().fmmgen_tree_info(self._h, info.ctypes.data))
         (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _,
@@ -112,6 +121,14 @@ class Tree:
         check(lib().fmmgen_tree_root(self._h, r.ctypes.data))
         return r
 
+    def systems(self):
+        """(root cubes [nsys][4], system of every cell in level-major order)."""
+        n = int(lib().fmmgen_tree_nsys(self._h))
+        roots = np.zeros((n, 4))
+        csys = np.zeros(self.ncells, dtype=np.int32)
+        check(lib().fmmgen_tree_export_systems(self._h, roots.ctypes.data, csys.ctypes.data))
+        return roots, csys
+
     def cells(self):
         nc, nl = self.ncells, self.nleaves
         cid = np.zeros(nc, np.uint64)
@@ -143,6 +160,17 @@ class Tree:
         check(lib().fmmgen_tree_times(self._h, b.ctypes.data, e.ctypes.data))
         return (dict(zip(["root", "keys_sort", "cells", "lists", "classes", "total"], b.tolist())),
                 dict(zip(["P2M", "M2M", "M2L", "P2P", "L2L", "L2P", "finalize", "total"], e.tolist())))
+
+
+def build_forest(pos, S, sizes, ncrit=64, order=4, theta=0.5, source_order=0, stream=None):
+    """Independent systems in one handle: system s is the next sizes[s] particles
+    of pos/S; each gets exactly the tree build_tree would give it alone, and the
+    build and evaluation phases run once over all systems."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    if sizes.ndim != 1 or len(sizes) < 1 or (sizes < 1).any():
+        raise ValueError("sizes must be a non-empty list of positive particle counts")
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return Tree(pos, S, ncrit, order, theta, source_order=source_order, stream=stream, sys_off=off)
 
 
 def build_tree(pos, S, N=None, ncrit=64, order=4, theta=0.5, source_order=0, stream=None):

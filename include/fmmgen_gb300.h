@@ -33,13 +33,14 @@ extern "C" {
 #define FMMGEN_ERR_ARG 1     /* invalid argument (order out of range, N < 1, ...) */
 #define FMMGEN_ERR_CUDA 2    /* CUDA runtime error; see fmmgen_last_error() */
 #define FMMGEN_ERR_DEPTH 3   /* tree would be deeper than 21 levels (>= ncrit coincident points) */
-#define FMMGEN_ERR_RANGE 4   /* interaction offsets beyond the M2L class table */
+#define FMMGEN_ERR_RANGE 4   /* an M2L offset beyond 2^18 finer-level half-widths (class key range) */
 #define FMMGEN_ERR_STATE 5   /* handle not built */
 
 /* precision modes of fmmgen_tree_compute_field_fmm */
 #define FMMGEN_PREC_FP64 0   /* every phase in FP64 */
 #define FMMGEN_PREC_MIXED 1  /* FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation;
-                                M2L on the tensor cores (3xTF32) for orders <= 9 */
+                                M2L on the tensor cores (3 FP16 products per term, FP32
+                                accumulation) for orders <= 9 */
 #define FMMGEN_PREC_MIXED_SIMT 2  /* as FMMGEN_PREC_MIXED with the M2L on the FP32 CUDA cores */
 
 const char *fmmgen_last_error(void);
@@ -100,6 +101,18 @@ typedef struct fmmgen_tree fmmgen_tree;
 int fmmgen_tree_build(const double *pos, long N, long ncrit, int order, double theta, int source_order,
                       void *stream, fmmgen_tree **tree);
 
+/* A forest of independent systems in one handle (no counterpart in the
+ * reference, whose Tree holds one system): system s owns the particles
+ * [sys_off[s], sys_off[s+1]) of pos (host array of nsys + 1 offsets,
+ * sys_off[0] = 0, sys_off[nsys] = N, every system non-empty).  Each system gets
+ * exactly the tree, root cube and interaction lists build_tree would give it
+ * alone; the build and every evaluation phase run once over all systems (one
+ * launch per phase, not per system).  fmmgen_tree_compute_field_fmm then
+ * evaluates all systems together (S and F over all N particles).  Same ncrit,
+ * order, theta and source order for every system. */
+int fmmgen_forest_build(const double *pos, const long *sys_off, int nsys, long ncrit, int order, double theta,
+                        int source_order, void *stream, fmmgen_tree **tree);
+
 /* Tree::compute_field_fmm (example/tree.cpp:243-271): F (device
  * [N][OUTPUTSIZE], caller's particle order) is overwritten with phi / E from
  * the sources S (device [N][SOURCESIZE], caller's particle order).  Does not
@@ -131,8 +144,13 @@ int fmmgen_root_box_noalloc(const double *pos, long N, double *root4, void *stre
 /* Introspection (host outputs; synchronises).
  * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions]. */
 int fmmgen_tree_info(fmmgen_tree *tree, long *info);
-/* Root cube [cx, cy, cz, r]. */
+/* Root cube [cx, cy, cz, r] (of system 0 in a forest). */
 int fmmgen_tree_root(fmmgen_tree *tree, double *root4);
+/* Systems of a handle (1 for fmmgen_tree_build), their root cubes
+ * [nsys][4] and the system of every cell (level-major order) -- either output
+ * may be NULL. */
+int fmmgen_tree_nsys(fmmgen_tree *tree);
+int fmmgen_tree_export_systems(fmmgen_tree *tree, double *roots4, int *cell_system);
 /* Per cell (level-major order): canonical id (1 << 3*level | octant path),
  * particle count (the reference's nleaf), centre [3]; leaf particle lists as
  * CSR over leaves in cell order (caller's particle indices). */
