@@ -13,7 +13,9 @@ direct sum on a 10,000-particle subset is reported.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config NAME]
 
 --config selects another configuration of the same path (10^4 charges at p=4;
-2x10^6 Plummer dipoles at p=6); the default is the headline above.
+2x10^6 Plummer dipoles at p=6; 4096 independent systems of 1,000-65,536
+charges, log-uniform sizes, p=6, solved as one forest per step); the default is
+the headline above.
 
 Multi-GPU: the path is replicated (independent systems per rank, no collective
 on the data path); `value` is the job total.
@@ -44,7 +46,17 @@ CONFIGS = {
     "uniform_10k_p4": (10_000, 4, 64, 0.5, 0, "uniform", True, True),
     # 2e6 dipoles in a Plummer sphere (scale 0.1, truncated at radius 1), p=6, potential and field
     "plummer_dipole_2m_p6": (2_000_000, 6, 64, 0.5, 1, "plummer", True, True),
+    # 4096 independent systems, sizes log-uniform in [1000, 65536], each uniform in its own unit cube,
+    # p=6, field output; N is the sum of the sizes
+    "batched_4096_p6": (0, 6, 64, 0.5, 0, "batched", False, True),
 }
+NSYS_BATCHED = 4096
+
+
+def batched_sizes(nsys, seed):
+    """Seeded system sizes, log-uniform in [1000, 65536]."""
+    rng = np.random.default_rng(seed + 7919)
+    return np.floor(np.exp(rng.uniform(np.log(1000.0), np.log(65536.0), nsys))).astype(np.int64)
 
 
 def args_parse():
@@ -59,6 +71,7 @@ def args_parse():
     ap.add_argument("--ncrit", type=int, default=None)
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--nsys", type=int, default=NSYS_BATCHED, help="systems of the batched configuration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
@@ -66,6 +79,10 @@ def args_parse():
                     help="run warmup + timed steps only (no e2e, FP64, direct sum, CPU baseline): for ncu captures")
     a = ap.parse_args()
     n, order, ncrit, theta, so, dist, pot, fld = CONFIGS[a.config]
+    a.sizes = None
+    if dist == "batched":
+        a.sizes = batched_sizes(a.nsys, a.seed)
+        n = int(a.sizes.sum())
     a.n = a.n or n
     a.order = a.order or order
     a.ncrit = a.ncrit or ncrit
@@ -107,7 +124,7 @@ def workload(a, seed):
     rng = np.random.default_rng(seed)
     if a.dist == "plummer":
         pos = plummer(rng, a.n)
-    else:
+    else:  # uniform; for the batched configuration each system in its own unit cube
         pos = rng.uniform(0.0, 1.0, (a.n, 3))
     if a.so == 0:
         S = rng.uniform(-1.0, 1.0, (a.n, 1))
@@ -118,7 +135,9 @@ def workload(a, seed):
 
 def config(a, world):
     kind = "Coulomb charges" if a.so == 0 else "dipoles"
-    where = "uniform in the unit cube" if a.dist == "uniform" else "in a Plummer sphere (a=0.1, r<=1)"
+    where = {"uniform": "uniform in the unit cube", "plummer": "in a Plummer sphere (a=0.1, r<=1)",
+             "batched": f"in {len(a.sizes) if a.sizes is not None else 0} independent systems (sizes log-uniform "
+                        f"in [1000, 65536], each uniform in its own unit cube), one forest"}[a.dist]
     out = "+".join(x for x, f in (("potential", a.potential), ("field", a.field)) if f)
     return {"workload": f"octree FMM, {a.n} {kind} {where}, p={a.order}, ncrit={a.ncrit}, theta={a.theta}, "
                         f"{out} output, tree+lists+evaluation per step",
@@ -186,9 +205,33 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline: the checker's restatement of the reference path on host cores
 # ---------------------------------------------------------------------------
+def sys_offsets(a):
+    return np.concatenate([[0], np.cumsum(a.sizes)]).astype(np.int64)
+
+
+def sampled_systems(a, k):
+    return np.unique(np.linspace(0, len(a.sizes) - 1, k).astype(np.int64))
+
+
 def cpu_sample(pos, q, a, stride):
     from oracle import oracle as orc
 
+    if a.sizes is not None:
+        # batched: the full build and evaluation of a spread of the systems, one at a time
+        off = sys_offsets(a)
+        tot_n, tot_t = 0, 0.0
+        idx = sampled_systems(a, 8)
+        for k in idx:
+            sl = slice(off[k], off[k + 1])
+            t0 = time.perf_counter()
+            ot = orc.OracleTree(pos[sl], q[sl], a.ncrit, a.order, a.theta, a.so)
+            t_build = time.perf_counter() - t0
+            _, ph = ot.evaluate(potential=a.potential, field=a.field, sample_stride=1)
+            tot_n += int(a.sizes[k])
+            tot_t += t_build + float(np.sum(ph))
+        sample = (f"oracle port (C, OpenMP) on this host: full tree build and evaluation of {len(idx)} of "
+                  f"{len(a.sizes)} systems one after another ({tot_n} particles)")
+        return tot_n / tot_t, tot_t * a.n / tot_n, sample, orc.num_threads()
     if a.n <= 100_000:
         stride = 1  # small systems run in full
     t0 = time.perf_counter()
@@ -270,7 +313,8 @@ def main():
     F = torch.empty((a.n, a.outsize), dtype=torch.float64, device=dev)
     L = fg.lib()
 
-    tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta, source_order=a.so)
+    tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta, source_order=a.so,
+                   sys_off=sys_offsets(a) if a.sizes is not None else None)
 
     def step(precision="mixed"):
         tree.rebuild(pos)
@@ -307,6 +351,7 @@ def main():
     with ClockSampler(local) as clk:
         dev_ms, wall = timed(a.steps, step, collect_phases=True)
     launches = L.fmmgen_launch_count() - n0
+    m2l_steps, m2l_mmas, m2l_exec_flops = tree.m2l_work()  # of the last timed (mixed) step
     t_max = dev_ms
     if pg:
         t = torch.tensor([dev_ms], device=dev)
@@ -349,12 +394,26 @@ def main():
     tree.S = q
 
     # ---- accuracy vs FP64 direct sum, and the plain FP64 GPU FMM ----
-    tg = torch.arange(0, a.n, max(1, a.n // 10000), device=dev)[:10000]
-    Fd = fg.direct(pos, q, targets=tg, source_order=a.so, potential=False, field=True)
+    if a.sizes is None:
+        tg = torch.arange(0, a.n, max(1, a.n // 10000), device=dev)[:10000]
+        Fd = fg.direct(pos, q, targets=tg, source_order=a.so, potential=False, field=True)
 
-    def err(Fx):
-        E = Fx[tg][:, -3:]  # the field columns, whether or not the potential is output too
-        return (torch.linalg.norm(E - Fd) / torch.linalg.norm(Fd)).item()
+        def err(Fx):
+            E = Fx[tg][:, -3:]  # the field columns, whether or not the potential is output too
+            return (torch.linalg.norm(E - Fd) / torch.linalg.norm(Fd)).item()
+    else:
+        # batched: each sampled system against its own FP64 direct sum on up to 1,000 of its particles
+        off = sys_offsets(a)
+        checks = []
+        for k in sampled_systems(a, 64):
+            b0, b1 = int(off[k]), int(off[k + 1])
+            tl = torch.arange(0, b1 - b0, max(1, (b1 - b0) // 1000), device=dev)[:1000]
+            Fs = fg.direct(pos[b0:b1], q[b0:b1], targets=tl, source_order=a.so, potential=False, field=True)
+            checks.append((b0, tl, Fs))
+
+        def err(Fx):
+            e = [(torch.linalg.norm(Fx[b0 + tl][:, -3:] - Fs) / torch.linalg.norm(Fs)).item() for b0, tl, Fs in checks]
+            return max(e)
 
     step("mixed")
     err_mixed = err(F)
@@ -396,11 +455,18 @@ def main():
                 "work": f"{'20 flop x P2P interactions' if dom == 'P2P' else '2*C(p+6,6) flop x M2L pairs'} "
                         f"per launch = {dom_flops:.3e} flop"}
     m2l_ms, _ = cand["M2L"]
-    roofline_m2l = {"kernel": "M2L", "bound": "tensor", "algorithmic_tflops": m2l_flops / (m2l_ms / 1e3) / 1e12
-                    if m2l_ms > 0 else 0.0, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-                    "frac": (m2l_flops / (m2l_ms / 1e3) / 1e12) / peaks["bf16_tflops"]
-                    if m2l_ms > 0 and peaks.get("bf16_tflops") else None,
-                    "note": "M2L runs on the FP32 pipe in this build; fraction is of the measured bf16 tensor peak"}
+    tpeak = peaks.get("bf16_tflops")  # dense 16-bit tensor peak (FP16 runs at the bf16 rate)
+    exec_tf = m2l_exec_flops / (m2l_ms / 1e3) / 1e12 if m2l_ms > 0 else 0.0
+    alg_tf = m2l_flops / (m2l_ms / 1e3) / 1e12 if m2l_ms > 0 else 0.0
+    roofline_m2l = {"kernel": "M2L (k_m2l_tc, tcgen05 kind::f16)" if m2l_steps else "M2L (CUDA cores)",
+                    "bound": "tensor", "achieved": exec_tf, "algorithmic_tflops": alg_tf, "peak": tpeak,
+                    "unit": "TFLOP/s", "frac": exec_tf / tpeak if tpeak else None,
+                    "algorithmic_frac": alg_tf / tpeak if tpeak else None,
+                    "class_steps": m2l_steps, "mma_instructions": m2l_mmas,
+                    "executed_flops_per_launch": m2l_exec_flops, "algorithmic_flops_per_launch": m2l_flops,
+                    "note": "executed = MMA flops issued (3 FP16 products per term, 128-row tiles over the union of "
+                            "the tile's classes, triangular N per 16-term chunk); algorithmic = 2*C(p+6,6) per pair; "
+                            "peak = measured bf16 dense (MEASURED_PEAKS.json)"}
 
     line = {"metric": metric_name(a), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

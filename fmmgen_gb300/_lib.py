@@ -63,6 +63,7 @@ _SIGS = {
     "fmmgen_tree_export_lists": (C.c_int, [_vp, _lp, _lp]),
     "fmmgen_tree_export_expansions": (C.c_int, [_vp, _dp, _dp]),
     "fmmgen_tree_times": (C.c_int, [_vp, _vp, _vp]),
+    "fmmgen_tree_m2l_work": (C.c_int, [_vp, _dp]),
 }
 
 

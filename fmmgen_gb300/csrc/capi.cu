@@ -342,6 +342,21 @@ extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, doubl
   return FMM_OK;
 }
 
+extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3) {
+  if (!tree || !tree->built || !out3) return ret(FMM_ERR_STATE);
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  DevTree &t = tree->t;
+  long long mmas = 0;
+  double flops = 0;
+  unsigned long long steps = 0;
+  if (t.h_pinned && fmm_m2l_tc_step_work(t.order, t.so, &mmas, &flops))
+    memcpy(&steps, t.h_pinned + FMM_PINNED_TCERR + 2, sizeof(steps));
+  out3[0] = (double)steps;
+  out3[1] = (double)steps * (double)mmas;
+  out3[2] = (double)steps * flops;
+  return FMM_OK;
+}
+
 extern "C" int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8) {
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   FMM_CUDA_TRY(cudaDeviceSynchronize());

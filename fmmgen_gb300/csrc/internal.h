@@ -86,7 +86,7 @@ struct DevTree {
   DevBuf<int> m2l_tgt_raw, m2l_src_raw;   // walk output in frontier order (kept between builds)
   DevBuf<int> p2p_tgt_raw, p2p_src_raw;
   uint32_t *h_pinned = nullptr;           // 64 pinned host bytes for count readbacks
-#define FMM_PINNED_TCERR 12               // h_pinned word holding the last tensor-core M2L error flags
+#define FMM_PINNED_TCERR 12               // h_pinned words 12..15: last tensor-core M2L error flags, class steps
   // tensor-core M2L operands (m2l_tc.cu)
   DevBuf<unsigned char> tc_T;             // split, swizzled operator records per class
   DevBuf<uint16_t> tc_Mh, tc_Ml;          // scaled, split source multipoles (FP16 bits)
@@ -113,6 +113,7 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
                       cudaStream_t st);
 void fmm_tree_destroy(DevTree *t);
 bool fmm_m2l_tc_supported(int p, int so);
+bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops);
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st);
 int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
                int potential, int field, double *F, cudaStream_t st);

@@ -72,7 +72,8 @@ struct TcParams {
   int cls_bytes, cls_scale, slot_bytes, nout;
   int nch[TC_MAXCH];              // MMA N of each K chunk
   int choff[TC_MAXCH + 1];        // byte offset of each chunk's (hi, lo) block in a class record
-  uint32_t *err;                  // bit 0: a gather-side wait timed out, bit 1: an MMA-side wait
+  uint32_t *err;                  // [0] bit 0: a gather-side wait timed out, bit 1: an MMA-side wait;
+                                  // [2..3] class steps issued (u64, for the executed-work count)
 };
 
 __device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -423,6 +424,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
     }
     cp_wait_all();
     if (!ok && tid == 0) atomicOr(P.err, 1u);
+    if (tid == 0) atomicAdd((unsigned long long *)(P.err + 2), (unsigned long long)u);
   } else if (lane == 0) {
     // ---------------- MMA issue (one thread) ----------------
     // Per-chunk instruction descriptors and operator offsets live in
@@ -637,6 +639,18 @@ bool fmm_m2l_tc_supported(int p, int so) {
   return tc_plan(p, so, pl);
 }
 
+// Executed tensor work of one class step of a 128-row tile: MMA instructions
+// and flops (3 products per K chunk, each 2 x 128 x 16 x N).
+bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops) {
+  TcPlan pl;
+  if (!tc_plan(p, so, pl)) return false;
+  long long n = 0;
+  for (int k = 0; k < pl.kch; k++) n += pl.nch[k];
+  *mmas = 3LL * pl.kch;
+  *flops = 3.0 * 2.0 * TC_ROWS * TC_CH * (double)n;
+  return true;
+}
+
 // M2L of the mixed-precision pass on the tensor cores: reads the FP32 scaled
 // multipoles M (row stride mstr) and writes every cell's FP32 scaled local
 // expansion L (row stride lstr).
@@ -664,12 +678,12 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   }
   const size_t nm = (size_t)nc * pl.kpad;
   if (fmm_reserve(t->tc_Mh, nm) || fmm_reserve(t->tc_Ml, nm) || fmm_reserve(t->tc_mexp, nc) ||
-      fmm_reserve(t->d_tcerr, 1))
+      fmm_reserve(t->d_tcerr, 4))
     return FMM_ERR_CUDA;
   fmm_note_launch(), k_tc_split<<<fmm_blocks((size_t)nc * 32, 256), 256, 0, st>>>(
       M, nc, mstr, pl.msize, pl.kpad, (__half *)t->tc_Mh.p, (__half *)t->tc_Ml.p, t->tc_mexp.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  FMM_CUDA_TRY(cudaMemsetAsync(t->d_tcerr.p, 0, sizeof(uint32_t), st));
+  FMM_CUDA_TRY(cudaMemsetAsync(t->d_tcerr.p, 0, 4 * sizeof(uint32_t), st));
 
   TcParams P;
   P.order = t->m2l_order.p;
@@ -711,7 +725,7 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   }
   if (rc) return rc;
   // timeout flags reach the host with the stream (read by fmmgen_tree_times)
-  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, sizeof(uint32_t),
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, 4 * sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, st));
   return FMM_OK;
 }

@@ -154,6 +154,12 @@ class Tree:
         check(lib().fmmgen_tree_export_expansions(self._h, M.ctypes.data, L.ctypes.data))
         return M, L
 
+    def m2l_work(self):
+        """Last tensor-core M2L: (class steps, MMA instructions, executed tensor flops)."""
+        w = np.zeros(3)
+        check(lib().fmmgen_tree_m2l_work(self._h, w.ctypes.data))
+        return tuple(float(x) for x in w)
+
     def times(self):
         b = np.zeros(6, np.float32)
         e = np.zeros(8, np.float32)

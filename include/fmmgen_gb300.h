@@ -165,6 +165,10 @@ int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, double *L);
 /* Phase times of the last build ([root, keys+sort, cells, lists, classes, total])
  * and evaluate ([P2M, M2M, M2L, P2P, L2L, L2P, finalize, total]) in ms. */
 int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8);
+/* Work of the last tensor-core M2L (no counterpart in the reference; for
+ * roofline accounting), host out3 = [class steps of 128-row tiles, tcgen05 MMA
+ * instructions, executed tensor flops]; zeros if none ran. */
+int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3);
 
 #ifdef __cplusplus
 }
