@@ -58,6 +58,7 @@ _SIGS = {
     "fmmgen_tree_info": (C.c_int, [_vp, _lp]),
     "fmmgen_tree_root": (C.c_int, [_vp, _dp]),
     "fmmgen_tree_nsys": (C.c_int, [_vp]),
+    "fmmgen_tree_set_graph": (C.c_int, [_vp, C.c_int]),
     "fmmgen_tree_export_systems": (C.c_int, [_vp, _dp, _vp]),
     "fmmgen_tree_export_cells": (C.c_int, [_vp, _lp, _lp, _dp, _lp, _lp]),
     "fmmgen_tree_export_lists": (C.c_int, [_vp, _lp, _lp]),

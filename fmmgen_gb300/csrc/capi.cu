@@ -46,6 +46,8 @@ void fmm_set_error_text(const char *msg) { g_err = msg; }
 
 static std::atomic<long long> g_launches{0};
 void fmm_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long fmm_launches() { return g_launches.load(std::memory_order_relaxed); }
+void fmm_add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 extern "C" {
 
@@ -220,6 +222,14 @@ int fmmgen_tree_info(fmmgen_tree *tree, long *info) {
   info[0] = t.ncells; info[1] = t.nleaves; info[2] = t.nm2l; info[3] = t.np2p;
   info[4] = t.nlevels; info[5] = t.nclasses; info[6] = t.N; info[7] = t.ncrit;
   info[8] = (long)t.p2p_interactions;
+  return FMM_OK;
+}
+
+int fmmgen_tree_set_graph(fmmgen_tree *tree, int enable) {
+  g_err.clear();
+  if (!tree) return ret(FMM_ERR_STATE);
+  tree->t.graph_on = enable != 0;
+  if (!enable) fmm_graph_release(&tree->t);
   return FMM_OK;
 }
 

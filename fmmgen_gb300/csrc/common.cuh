@@ -57,6 +57,8 @@ void fmm_set_cuda_error(cudaError_t e, const char *what, const char *file, int l
 void fmm_set_error_text(const char *msg);
 // Counts kernel launches made by this library (every launch site calls it).
 void fmm_note_launch();
+long long fmm_launches();            // kernels launched so far
+void fmm_add_launches(long long n);  // correction: kernels recorded in (not launched by) a graph capture, or replayed
 
 __device__ __forceinline__ unsigned fmm_lane() { return threadIdx.x & 31u; }
 

@@ -320,8 +320,15 @@ __global__ void k_finalize(const double *Fnear, const double *Ffar, const uint32
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
+// phase boundary i; while a graph is being recorded the record becomes a node
+// of the graph, so the replayed pass keeps its phase times
 static int rec(DevTree *t, int i, cudaStream_t st) {
-  FMM_CUDA_TRY(cudaEventRecord(t->ev[6 + i], st));
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FMM_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusActive)
+    FMM_CUDA_TRY(cudaEventRecordWithFlags(t->ev[6 + i], st, cudaEventRecordExternal));
+  else
+    FMM_CUDA_TRY(cudaEventRecord(t->ev[6 + i], st));
   return FMM_OK;
 }
 
@@ -389,10 +396,60 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   return FMM_OK;
 }
 
+static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, int field, int precision,
+                         cudaStream_t st);
+
+void fmm_graph_release(DevTree *t) {
+  if (t->gexec) cudaGraphExecDestroy(t->gexec);
+  if (t->graph) cudaGraphDestroy(t->graph);
+  t->gexec = nullptr;
+  t->graph = nullptr;
+  t->gkey = DevTree::GraphKey();
+}
+
+// Tree::compute_field_fmm (example/tree.cpp:243-271).  With the graph mode on,
+// the first pass after a build (or after a change of S, F or the switches)
+// runs normally -- reserving every buffer -- and is then recorded as a CUDA
+// graph on a private stream; later passes replay that graph on `st`, one launch.
 int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
                       cudaStream_t st) {
   if (!t || t->ncells == 0) return FMM_ERR_STATE;
   if (!S || !F || (!potential && !field) || precision < 0 || precision > 2) return FMM_ERR_ARG;
+  if (!t->graph_on) return evaluate_pass(t, S, F, potential, field, precision, st);
+  const DevTree::GraphKey key{S, F, potential, field, precision, t->build_serial};
+  const DevTree::GraphKey &k = t->gkey;
+  if (t->gexec && k.S == key.S && k.F == key.F && k.potential == key.potential && k.field == key.field &&
+      k.precision == key.precision && k.serial == key.serial) {
+    FMM_CUDA_TRY(cudaGraphLaunch(t->gexec, st));
+    fmm_add_launches(t->glaunches);
+    return FMM_OK;
+  }
+  TRY(evaluate_pass(t, S, F, potential, field, precision, st));
+  fmm_graph_release(t);
+  if (!t->gstream) FMM_CUDA_TRY(cudaStreamCreateWithFlags(&t->gstream, cudaStreamNonBlocking));
+  const long long n0 = fmm_launches();
+  FMM_CUDA_TRY(cudaStreamBeginCapture(t->gstream, cudaStreamCaptureModeRelaxed));
+  const int rc = evaluate_pass(t, S, F, potential, field, precision, t->gstream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(t->gstream, &g);
+  t->glaunches = fmm_launches() - n0;
+  fmm_add_launches(-t->glaunches);  // recorded, not launched
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (ce != cudaSuccess) {
+    fmm_set_cuda_error(ce, "graph capture", __FILE__, __LINE__);
+    return FMM_ERR_CUDA;
+  }
+  t->graph = g;
+  FMM_CUDA_TRY(cudaGraphInstantiate(&t->gexec, t->graph, 0));
+  t->gkey = key;
+  return FMM_OK;
+}
+
+static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, int field, int precision,
+                         cudaStream_t st) {
   const PlanSet *ps = fmm_get_plans(t->order, t->so);
   if (!ps) return FMM_ERR_CUDA;
   const bool mixed = precision != 0;
@@ -426,12 +483,14 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
 // Per-phase times of the last evaluate (needs the stream to have completed).
 void fmm_eval_times(DevTree *t) {
   float ms;
-  for (int i = 0; i < 7; i++) {
-    cudaEventElapsedTime(&ms, t->ev[6 + i], t->ev[6 + i + 1]);
+  for (int i = 0; i < 8; i++) {
+    const int a = i < 7 ? 6 + i : 6, b = i < 7 ? 7 + i : 13;
+    if (cudaEventElapsedTime(&ms, t->ev[a], t->ev[b]) != cudaSuccess) {
+      ms = -1.f;          // not recorded
+      cudaGetLastError();  // and leave no error behind for the next call
+    }
     t->phase_ms[i] = ms;
   }
-  cudaEventElapsedTime(&ms, t->ev[6], t->ev[13]);
-  t->phase_ms[7] = ms;
 }
 
 // ---------------------------------------------------------------------------

@@ -103,6 +103,19 @@ struct DevTree {
   float build_ms[6] = {0};                // root, keys+sort, levels, lists, classes, total
   cudaEvent_t ev[16];
   bool ev_ready = false;
+  // evaluation pass as a CUDA graph (fmmgen_tree_set_graph): replayed while
+  // the build, the arrays and the switches are those it was captured with
+  bool graph_on = false;
+  cudaStream_t gstream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphKey {
+    const double *S = nullptr;
+    double *F = nullptr;
+    int potential = -1, field = -1, precision = -1;
+    uint64_t serial = 0;
+  } gkey;
+  long long glaunches = 0;                // kernels in the graph
 };
 
 // sys_off: nullptr for one system, else nsys + 1 host offsets of the systems'
@@ -112,6 +125,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
 int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
                       cudaStream_t st);
 void fmm_tree_destroy(DevTree *t);
+void fmm_graph_release(DevTree *t);
 bool fmm_m2l_tc_supported(int p, int so);
 bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops);
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st);

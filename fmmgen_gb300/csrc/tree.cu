@@ -1042,6 +1042,9 @@ static int build_classes(DevTree *t, cudaStream_t st) {
 
 void fmm_tree_destroy(DevTree *t) {
   if (!t) return;
+  fmm_graph_release(t);
+  if (t->gstream) cudaStreamDestroy(t->gstream);
+  t->gstream = nullptr;
   fmm_release(t->keys); fmm_release(t->keys2); fmm_release(t->perm); fmm_release(t->perm2);
   fmm_release(t->px); fmm_release(t->py); fmm_release(t->pz);
   fmm_release(t->phi4); fmm_release(t->plo4); fmm_release(t->sdip); fmm_release(t->levf);

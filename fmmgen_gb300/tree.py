@@ -154,6 +154,12 @@ class Tree:
         check(lib().fmmgen_tree_export_expansions(self._h, M.ctypes.data, L.ctypes.data))
         return M, L
 
+    def set_graph(self, enable=True):
+        """Replay the evaluation pass as one CUDA graph launch while the build and
+        the arguments of compute_field_fmm stay the same."""
+        check(lib().fmmgen_tree_set_graph(self._h, int(bool(enable))))
+        return self
+
     def m2l_work(self):
         """Last tensor-core M2L: (class steps, MMA instructions, executed tensor flops)."""
         w = np.zeros(3)

@@ -120,6 +120,15 @@ int fmmgen_forest_build(const double *pos, const long *sys_off, int nsys, long n
 int fmmgen_tree_compute_field_fmm(fmmgen_tree *tree, const double *S, double *F, int potential, int field,
                                   int precision, void *stream);
 
+/* Graph mode (no counterpart in the reference): with enable != 0 the first
+ * fmmgen_tree_compute_field_fmm after a build -- or after S, F, the output
+ * switches or the precision change -- runs normally and is then recorded as a
+ * CUDA graph; later calls with the same build and arguments replay the whole
+ * evaluation pass as one graph launch on `stream`.  The recording uses a
+ * private stream, so `stream` may be the legacy default stream.  enable = 0
+ * drops the graph. */
+int fmmgen_tree_set_graph(fmmgen_tree *tree, int enable);
+
 /* Tree::compute_field_exact / evaluate_direct (example/calculate.cpp:252-264):
  * FP64 O(N^2) sum for the targets listed in `targets` (device, NULL = all N);
  * F is [ntargets][OUTPUTSIZE] in the order of `targets`. */
