@@ -14,8 +14,9 @@ direct sum on a 10,000-particle subset is reported.
 
 --config selects another configuration of the same path (10^4 charges at p=4;
 2x10^6 Plummer dipoles at p=6; 4096 independent systems of 1,000-65,536
-charges, log-uniform sizes, p=6, solved as one forest per step); the default is
-the headline above.
+charges, log-uniform sizes, p=6, solved as one forest per step; 8x10^6
+clustered charges at p_max=12 with learned per-pair M2L orders, the fixed
+p=12 pass timed beside it); the default is the headline above.
 
 Multi-GPU: the path is replicated (independent systems per rank, no collective
 on the data path); `value` is the job total.
@@ -49,6 +50,9 @@ CONFIGS = {
     # 4096 independent systems, sizes log-uniform in [1000, 65536], each uniform in its own unit cube,
     # p=6, field output; N is the sum of the sizes
     "batched_4096_p6": (0, 6, 64, 0.5, 0, "batched", False, True),
+    # learned per-pair M2L orders: 8e6 charges, half uniform in the unit cube and half in 64 Gaussian
+    # clusters (sigma 0.01), p_max=12, field output; the committed order model picks each pair's order
+    "learned_8m_p12": (8_000_000, 12, 128, 0.5, 0, "mixture", False, True),
 }
 NSYS_BATCHED = 4096
 
@@ -119,11 +123,24 @@ def plummer(rng, n, a=0.1, rmax=1.0):
     return np.concatenate(out)[:n]
 
 
+def mixture(n, seed, nclusters=64, sigma=0.01):
+    """Half uniform in the unit cube, half in nclusters isotropic Gaussian
+    clusters with centres uniform in the cube (the order model's training
+    distribution, fmmgen_gb300.learned.mixture_positions)."""
+    rng = np.random.default_rng(seed)
+    nu = n // 2
+    centres = rng.uniform(0, 1, (nclusters, 3))
+    which = rng.integers(0, nclusters, n - nu)
+    return np.concatenate([rng.uniform(0, 1, (nu, 3)), centres[which] + sigma * rng.standard_normal((n - nu, 3))])
+
+
 def workload(a, seed):
     """Seeded synthetic inputs of the configuration's shape (no dataset is involved)."""
     rng = np.random.default_rng(seed)
     if a.dist == "plummer":
         pos = plummer(rng, a.n)
+    elif a.dist == "mixture":
+        pos = mixture(a.n, seed + 104729)
     else:  # uniform; for the batched configuration each system in its own unit cube
         pos = rng.uniform(0.0, 1.0, (a.n, 3))
     if a.so == 0:
@@ -136,10 +153,13 @@ def workload(a, seed):
 def config(a, world):
     kind = "Coulomb charges" if a.so == 0 else "dipoles"
     where = {"uniform": "uniform in the unit cube", "plummer": "in a Plummer sphere (a=0.1, r<=1)",
+             "mixture": "half uniform in the unit cube, half in 64 Gaussian clusters (sigma=0.01)",
              "batched": f"in {len(a.sizes) if a.sizes is not None else 0} independent systems (sizes log-uniform "
                         f"in [1000, 65536], each uniform in its own unit cube), one forest"}[a.dist]
     out = "+".join(x for x, f in (("potential", a.potential), ("field", a.field)) if f)
-    return {"workload": f"octree FMM, {a.n} {kind} {where}, p={a.order}, ncrit={a.ncrit}, theta={a.theta}, "
+    orders = (f"p_max={a.order} with learned per-pair M2L orders (MLP 16-64-64-11, features + inference in "
+              f"every pass)" if a.dist == "mixture" else f"p={a.order}")
+    return {"workload": f"octree FMM, {a.n} {kind} {where}, {orders}, ncrit={a.ncrit}, theta={a.theta}, "
                         f"{out} output, tree+lists+evaluation per step",
             "name": a.config, "N": a.n, "order": a.order, "ncrit": a.ncrit, "theta": a.theta, "source_order": a.so,
             "precision": "mixed (FP32 sweeps/M2L/P2P, FP64 operator assembly and final accumulation)",
@@ -315,6 +335,12 @@ def main():
 
     tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta, source_order=a.so,
                    sys_off=sys_offsets(a) if a.sizes is not None else None)
+    model = None
+    if a.dist == "mixture":  # learned per-pair M2L orders: every pass predicts them from its multipoles
+        from fmmgen_gb300 import learned
+
+        model = learned.OrderModel.load()
+        model.attach(tree)
 
     def step(precision="mixed"):
         tree.rebuild(pos)
@@ -352,6 +378,7 @@ def main():
         dev_ms, wall = timed(a.steps, step, collect_phases=True)
     launches = L.fmmgen_launch_count() - n0
     m2l_steps, m2l_mmas, m2l_exec_flops = tree.m2l_work()  # of the last timed (mixed) step
+    m2l_orders = tree.m2l_orders() if model is not None else None
     t_max = dev_ms
     if pg:
         t = torch.tensor([dev_ms], device=dev)
@@ -359,6 +386,21 @@ def main():
         t_max = t.item()
     value = a.n * a.steps * world / (t_max / 1e3)
     ms_per_step = t_max / a.steps
+    # ---- eval-only (the reference's timed region, example/main.cpp:154-162): the tree is
+    # built once, then the evaluation pass is replayed from its recorded CUDA graph ----
+    tree.rebuild(pos)
+    tree.set_graph(True)
+    tree.compute_field_fmm(F, potential=a.potential, field=a.field, precision="mixed")  # runs, then records
+    eval_ms, _ = timed(a.steps, lambda: tree.compute_field_fmm(F, potential=a.potential, field=a.field,
+                                                                  precision="mixed"))
+    tree.set_graph(False)
+    eval_max = eval_ms
+    if pg:
+        t = torch.tensor([eval_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        eval_max = t.item()
+    eval_only = {"value": a.n * a.steps * world / (eval_max / 1e3), "unit": UNIT, "ms_per_step": eval_max / a.steps,
+                 "note": "P2M..L2P only, tree built once; the pass is replayed from its recorded CUDA graph"}
     if a.profile_only:
         if rank == 0:
             print(json.dumps({"profile_only": True, "value": value, "unit": UNIT, "ms_per_step": ms_per_step,
@@ -417,6 +459,25 @@ def main():
 
     step("mixed")
     err_mixed = err(F)
+    learned_info = None
+    if model is not None:
+        # the fixed-order fallback (p_max for every pair) timed and checked beside the learned pass
+        tree.set_order_model(None)
+        step("mixed")
+        err_fixed = err(F)
+        msf, _ = timed(2, lambda: step("mixed"), collect_phases=False)
+        _, ef = tree.times()
+        from fmmgen_gb300 import learned
+
+        terms = learned.m2l_terms(m2l_orders, a.so)
+        terms_fixed = tree.nm2l * learned.pair_terms(a.order, a.so)
+        learned_info = {"delta": model.delta, "m2l_multiply_adds": terms, "m2l_multiply_adds_fixed": terms_fixed,
+                        "order_histogram": {int(k): int(v) for k, v in
+                                            zip(*np.unique(m2l_orders, return_counts=True))},
+                        "fixed_pmax": {"value": a.n * 2 / (msf / 1e3), "ms_per_step": msf / 2,
+                                       "rel_field_err": err_fixed, "m2l_ms": ef.get("M2L")},
+                        "model": os.path.relpath(learned.MODEL_PATH, ROOT)}
+        model.attach(tree)
     fp64 = {}
     if not a.no_fp64:
         step("fp64")
@@ -438,6 +499,8 @@ def main():
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal at the max SM clock
     p2p_flops = (20.0 if a.so == 0 else 38.0) * tree.p2p_interactions
     m2l_flops = 2.0 * math.comb(a.order + 6, 6) * tree.nm2l
+    if learned_info:
+        m2l_flops = 2.0 * learned_info["m2l_multiply_adds"]  # at each pair's own order
     cand = {"P2P": (ph.get("P2P", 0.0), p2p_flops), "M2L": (ph.get("M2L", 0.0), m2l_flops)}
     dom = max(cand, key=lambda k: cand[k][0])
     dom_ms, dom_flops = cand[dom]
@@ -473,8 +536,9 @@ def main():
             "dtype": "f32+f64", "data": "synthetic (seeded positions and sources)",
             "config": config(a, world), "rel_field_err": err_mixed,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roofline, "roofline_m2l": roofline_m2l,
+            "gpu_launches": launches, "eval_only": eval_only, "roofline": roofline, "roofline_m2l": roofline_m2l,
             "fp64_plain": fp64, "speedup_vs_fp64": (value / world) / fp64["value"] if fp64 else None,
+            "learned_orders": learned_info,
             "phases_ms": {k: round(v, 3) for k, v in ph.items()},
             "tree": {"cells": tree.ncells, "leaves": tree.nleaves, "m2l_pairs": tree.nm2l, "p2p_pairs": tree.np2p,
                      "p2p_interactions": tree.p2p_interactions, "m2l_classes": tree.nclasses},

@@ -65,6 +65,18 @@ _SIGS = {
     "fmmgen_tree_export_expansions": (C.c_int, [_vp, _dp, _dp]),
     "fmmgen_tree_times": (C.c_int, [_vp, _vp, _vp]),
     "fmmgen_tree_m2l_work": (C.c_int, [_vp, _dp]),
+    "fmmgen_order_model_nparam": (C.c_int, []),
+    "fmmgen_order_nfeatures": (C.c_int, []),
+    "fmmgen_order_nclasses": (C.c_int, []),
+    "fmmgen_tree_order_features": (C.c_int, [_vp, C.c_double, _vp, _vp]),
+    "fmmgen_tree_order_labels": (C.c_int, [_vp, C.c_double, _vp, _vp, _vp]),
+    "fmmgen_tree_set_m2l_orders": (C.c_int, [_vp, _vp, _vp]),
+    "fmmgen_tree_set_order_model": (C.c_int, [_vp, _vp, C.c_float, C.c_double]),
+    "fmmgen_tree_export_m2l_orders": (C.c_int, [_vp, _vp]),
+    "fmmgen_mlp_predict": (C.c_int, [_vp, _vp, C.c_long, C.c_float, C.c_int, _vp, _vp]),
+    "fmmgen_mlp_train_work": (C.c_long, [C.c_int]),
+    "fmmgen_mlp_train_step": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp]),
+    "fmmgen_mlp_adam": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_float, _vp]),
 }
 
 

@@ -1,4 +1,5 @@
 // capi.cu -- the extern "C" boundary declared in include/fmmgen_gb300.h.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -366,6 +367,98 @@ extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3) {
   out3[2] = (double)steps * flops;
   return FMM_OK;
 }
+
+// ---- learned per-pair M2L orders -------------------------------------------
+extern "C" {
+int fmmgen_order_model_nparam(void) { return fmm_mlp_nparam(); }
+int fmmgen_order_nfeatures(void) { return 16; }
+int fmmgen_order_nclasses(void) { return 11; }
+
+int fmmgen_tree_order_features(fmmgen_tree *tree, double eps, float *feat, void *st) {
+  g_err.clear();
+  if (!tree || !tree->built || tree->last_precision < 0) return ret(FMM_ERR_STATE);
+  if ((!feat && tree->t.nm2l > 0) || !(eps > 0)) return ret(FMM_ERR_ARG);
+  return ret(fmm_order_features(&tree->t, eps, feat, S(st)));
+}
+
+int fmmgen_tree_order_labels(fmmgen_tree *tree, double eps, unsigned char *label, float *errq, void *st) {
+  g_err.clear();
+  if (!tree || !tree->built || tree->last_precision != FMMGEN_PREC_FP64) return ret(FMM_ERR_STATE);
+  if (!(eps > 0) || (!label && tree->t.nm2l > 0)) return ret(FMM_ERR_ARG);
+  return ret(fmm_order_labels(&tree->t, eps, label, errq, S(st)));
+}
+
+int fmmgen_tree_set_m2l_orders(fmmgen_tree *tree, const unsigned char *orders, void *st) {
+  g_err.clear();
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  fmm_graph_release(&t);  // a recorded pass holds the old M2L choice
+  if (!orders) {
+    t.ord_mode = t.model ? 2 : 0;
+    return FMM_OK;
+  }
+  int rc = fmm_reserve(t.m2l_ord, t.nm2l > 0 ? t.nm2l : 1);
+  if (rc) return ret(rc);
+  if (t.nm2l > 0)
+    FMM_CUDA_TRY(cudaMemcpyAsync(t.m2l_ord.p, orders, t.nm2l, cudaMemcpyDeviceToDevice, S(st)));
+  t.ord_mode = 1;
+  t.ord_serial = t.build_serial;
+  return FMM_OK;
+}
+
+int fmmgen_tree_set_order_model(fmmgen_tree *tree, const float *params, float delta, double eps) {
+  g_err.clear();
+  if (!tree) return ret(FMM_ERR_STATE);
+  if (params && (!(delta >= 0.f && delta < 1.f) || !(eps > 0))) return ret(FMM_ERR_ARG);
+  DevTree &t = tree->t;
+  fmm_graph_release(&t);
+  t.model = params;
+  t.model_delta = delta;
+  if (params) t.model_eps = eps;
+  t.ord_mode = params ? 2 : 0;
+  return FMM_OK;
+}
+
+int fmmgen_tree_export_m2l_orders(fmmgen_tree *tree, unsigned char *orders_host) {
+  g_err.clear();
+  if (!tree || !tree->built || tree->last_precision < 0) return ret(FMM_ERR_STATE);
+  DevTree &t = tree->t;
+  if (t.nm2l == 0) return FMM_OK;
+  if (!orders_host) return ret(FMM_ERR_ARG);
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  if (t.ord_mode == 0 || t.ord_serial != t.build_serial) {
+    memset(orders_host, t.order, t.nm2l);
+    return FMM_OK;
+  }
+  std::vector<unsigned char> o;
+  if (d2h(o, t.m2l_ord.p, t.nm2l)) return ret(FMM_ERR_CUDA);
+  for (long k = 0; k < t.nm2l; k++) orders_host[k] = (unsigned char)std::min(std::max((int)o[k], t.so + 1), t.order);
+  return FMM_OK;
+}
+
+int fmmgen_mlp_predict(const float *params, const float *X, long n, float delta, int qmax, unsigned char *orders,
+                       void *st) {
+  g_err.clear();
+  if (n < 0 || (n > 0 && (!params || !X || !orders)) || !(delta >= 0.f && delta < 1.f) || qmax < 2)
+    return ret(FMM_ERR_ARG);
+  return ret(fmm_mlp_predict(params, X, n, delta, qmax, orders, S(st)));
+}
+
+long fmmgen_mlp_train_work(int n) { return n > 0 ? 267L * n : 0; }
+
+int fmmgen_mlp_train_step(const float *params, const float *X, const unsigned char *y, int n, float *grad,
+                          float *loss, float *work, void *st) {
+  g_err.clear();
+  if (n <= 0 || !params || !X || !y || !grad || !loss || !work) return ret(FMM_ERR_ARG);
+  return ret(fmm_mlp_train_step(params, X, y, n, grad, loss, work, S(st)));
+}
+
+int fmmgen_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, void *st) {
+  g_err.clear();
+  if (!params || !grad || !m || !v || step < 1) return ret(FMM_ERR_ARG);
+  return ret(fmm_mlp_adam(params, grad, m, v, step, lr, S(st)));
+}
+}  // extern "C"
 
 extern "C" int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8) {
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);

@@ -218,6 +218,55 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l(Plan P, int ncells, int 
 }
 
 // ---------------------------------------------------------------------------
+// M2L with a per-pair order (learned order selection, learn.cu): pair k of
+// target A is applied at order q_k <= order, i.e. only the terms with
+// |n| + |m| <= q_k of the order-`order` contraction -- the leading blocks of D,
+// M and L in the degree-major layout, so the order-q_k plan runs on the same
+// rows.  One warp per target; lane l keeps outputs l, l + 32, ... in registers.
+// ---------------------------------------------------------------------------
+#define M2LV_R ((FMM_NTMAX + 31) / 32)
+struct PlanVar {
+  Plan p[FMM_PMAX + 1];
+};
+template <typename T>
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(PlanVar PV, int ncells, int so, int order,
+                                                            const int *off_, const int *src, const int *cls,
+                                                            const unsigned char *ord, const T *clsD,
+                                                            const unsigned char *clevel, const T *M, T *L, int mstr,
+                                                            int lstr, int dstr) {
+  __shared__ T sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX], sS[FMM_WARPS][FMM_NTMAX + 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int A = blockIdx.x * FMM_WARPS + w;
+  if (A >= ncells) return;
+  const int moff = fmm_nterms(so - 1), lsize = fmm_nterms(order - so);
+  T acc[M2LV_R];
+#pragma unroll
+  for (int r = 0; r < M2LV_R; r++) acc[r] = T(0);
+  const int la = clevel[A];
+  for (int k = off_[A]; k < off_[A + 1]; k++) {
+    const int q = min(max((int)ord[k], so + 1), order);
+    const Plan &P = PV.p[q];
+    const int nt = fmm_nterms(q), ms = nt - moff, ls = fmm_nterms(q - so);
+    const int B = src[k];
+    const T *D = clsD + (size_t)cls[k] * dstr;
+    const int dl = la - (int)clevel[B];
+    __syncwarp();
+    for (int i = lane; i < nt; i += 32) sA[w][i] = D[i];
+    for (int j = lane; j < ms; j += 32) sB[w][j] = M[(size_t)B * mstr + j] * exp2i<T>(dl * (int)c_mi[j + moff][3]);
+    for (int s = lane; s < P.nseg; s += 32) sS[w][s] = T(0);
+    __syncwarp();
+    engine_run<T>(P, sA[w], sB[w], sS[w], lane);
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < M2LV_R; r++)
+      if (lane + 32 * r < ls) acc[r] += engine_out<T>(P, sS[w], lane + 32 * r);
+  }
+#pragma unroll
+  for (int r = 0; r < M2LV_R; r++)
+    if (lane + 32 * r < lsize) L[(size_t)A * lstr + lane + 32 * r] = acc[r];
+}
+
+// ---------------------------------------------------------------------------
 // L2L for all cells of one level (example/calculate.cpp:219-234)
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -359,7 +408,29 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   m2l_reg_kernel kg[4];
   int kthreads[4];
   int ng = mixed && !tc ? m2l_reg_kernels(p, so, kg, kthreads) : 0;
-  if (tc) {
+  // with an order model, P2P runs first: the predicted orders read its near field
+  t->p2p_first = t->ord_mode == 2;
+  if (t->p2p_first) {
+    TRY(fmm_p2p_launch(t, mixed, S, st));
+    TRY(rec(t, 3, st));
+  }
+  if (t->ord_mode != 0) {
+    // per-pair orders: predicted now from this pass's multipoles, or given
+    if (t->ord_mode == 2) TRY(fmm_learned_orders(t, st));
+    else if (t->ord_serial != t->build_serial) {
+      fmm_set_error_text("per-pair M2L orders were set for an earlier build");
+      return FMM_ERR_STATE;
+    }
+    PlanVar PV;
+    for (int q = 0; q <= FMM_PMAX; q++) {
+      const PlanSet *pq = q >= so + 1 && q <= p ? fmm_get_plans(q, so) : nullptr;
+      PV.p[q] = pq ? pq->m2l : Plan();
+    }
+    fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        PV, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
+        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
+        lstr, dstr);
+  } else if (tc) {
     TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
   } else if (ng > 0) {
     for (int g = 0; g < ng; g++)
@@ -374,11 +445,15 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
         lstr, dstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
-  TRY(rec(t, 3, st));
-  // P2P (running it concurrently with M2L on a second stream was measured to
-  // give no gain: the two kernels slow each other down when co-resident)
-  TRY(fmm_p2p_launch(t, mixed, S, st));
-  TRY(rec(t, 4, st));
+  if (t->p2p_first) {
+    TRY(rec(t, 4, st));
+  } else {
+    TRY(rec(t, 3, st));
+    // P2P (running it concurrently with M2L on a second stream was measured to
+    // give no gain: the two kernels slow each other down when co-resident)
+    TRY(fmm_p2p_launch(t, mixed, S, st));
+    TRY(rec(t, 4, st));
+  }
   // L2L, top-down
   for (int l = 1; l < t->nlevels; l++) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
@@ -454,6 +529,7 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
   if (!ps) return FMM_ERR_CUDA;
   const bool mixed = precision != 0;
   const bool tc = precision == 1 && fmm_m2l_tc_supported(t->order, t->so);
+  t->last_prec = mixed ? 1 : 0;
   const int p = t->order, so = t->so;
   const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
   const size_t nc = t->ncells;
@@ -491,6 +567,7 @@ void fmm_eval_times(DevTree *t) {
     }
     t->phase_ms[i] = ms;
   }
+  if (t->p2p_first) std::swap(t->phase_ms[2], t->phase_ms[3]);  // the pass ran P2P, then M2L
 }
 
 // ---------------------------------------------------------------------------

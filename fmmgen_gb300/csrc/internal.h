@@ -116,6 +116,20 @@ struct DevTree {
     uint64_t serial = 0;
   } gkey;
   long long glaunches = 0;                // kernels in the graph
+  // per-pair M2L orders (learn.cu): explicit (fmmgen_tree_set_m2l_orders) or
+  // predicted by an order model during each evaluation
+  int ord_mode = 0;                       // 0: one order, 1: explicit orders, 2: order model
+  DevBuf<unsigned char> m2l_ord;          // order of each M2L pair, list order
+  uint64_t ord_serial = 0;                // the build m2l_ord belongs to
+  const float *model = nullptr;           // order-model parameters (device, caller-owned)
+  float model_delta = 0.f;
+  double model_eps = 1e-6;                // error target the model's features are scaled to
+  int last_prec = -1;                     // precision of the last evaluation (-1: none)
+  bool p2p_first = false;                 // the last pass ran P2P before M2L (phase times swap)
+  DevBuf<float> mnorm, feat;              // per-cell multipole degree norms; per-pair features
+  DevBuf<double> tscale, tpart;           // per system: sqrt(sum |E_near|^2 / M2L pairs); partial sums
+  DevBuf<int> sys_pairs;                  // per system: M2L pairs
+  DevBuf<int> ltgt;                       // target of each M2L pair (labels)
 };
 
 // sys_off: nullptr for one system, else nsys + 1 host offsets of the systems'
@@ -127,6 +141,16 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
 void fmm_tree_destroy(DevTree *t);
 void fmm_graph_release(DevTree *t);
 bool fmm_m2l_tc_supported(int p, int so);
+// learned per-pair orders (learn.cu)
+int fmm_mlp_nparam();
+int fmm_order_features(DevTree *t, double eps, float *feat, cudaStream_t st);
+int fmm_order_labels(DevTree *t, double eps, unsigned char *label, float *errq, cudaStream_t st);
+int fmm_mlp_predict(const float *params, const float *X, long n, float delta, int qmax, unsigned char *orders,
+                    cudaStream_t st);
+int fmm_mlp_train_step(const float *params, const float *X, const unsigned char *y, int n, float *grad, float *loss,
+                       float *work, cudaStream_t st);
+int fmm_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, cudaStream_t st);
+int fmm_learned_orders(DevTree *t, cudaStream_t st);
 bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops);
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st);
 int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,

@@ -1066,6 +1066,9 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->d_tcerr);
   t->tc_serial = ~0ull;
   fmm_release(t->wdec);
+  fmm_release(t->m2l_ord); fmm_release(t->mnorm); fmm_release(t->feat); fmm_release(t->tscale); fmm_release(t->tpart);
+  fmm_release(t->sys_pairs);
+  fmm_release(t->ltgt);
   fmm_release(t->cr); fmm_release(t->crmax); fmm_release(t->crf); fmm_release(t->cmargin); fmm_release(t->csys);
   fmm_release(t->sys_off); fmm_release(t->psys); fmm_release(t->roots);
   fmm_release(t->tmp); fmm_release(t->d_eflags); fmm_release(t->d_root);

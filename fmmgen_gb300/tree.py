@@ -160,6 +160,43 @@ class Tree:
         check(lib().fmmgen_tree_set_graph(self._h, int(bool(enable))))
         return self
 
+    # -- per-pair M2L orders (no counterpart in the reference) ----------------
+    def set_m2l_orders(self, orders=None, stream=None):
+        """Apply M2L pair k (export_lists order) at order orders[k] (clamped to
+        [source_order + 1, order]) in the evaluations of this build; None
+        returns to the one order."""
+        if orders is None:
+            check(lib().fmmgen_tree_set_m2l_orders(self._h, None, _stream_ptr(stream)))
+            return self
+        o = orders if isinstance(orders, torch.Tensor) else torch.as_tensor(np.asarray(orders))
+        o = o.to(device="cuda", dtype=torch.uint8).contiguous()
+        if o.numel() != self.nm2l:
+            raise ValueError("one order per M2L pair")
+        check(lib().fmmgen_tree_set_m2l_orders(self._h, C.c_void_p(o.data_ptr()), _stream_ptr(stream)))
+        (stream or torch.cuda.current_stream()).synchronize()  # the copy has read o
+        return self
+
+    def set_order_model(self, params=None, delta=0.0, eps=1e-6):
+        """Attach an order model (FP32 parameters on the device, see learned.py)
+        for the relative field error target eps: every evaluation predicts each
+        pair's order from its own multipoles and near field.  None detaches it."""
+        if params is None:
+            check(lib().fmmgen_tree_set_order_model(self._h, None, 0.0, 1.0))
+            self._order_params = None
+            return self
+        if not (isinstance(params, torch.Tensor) and params.is_cuda and params.dtype == torch.float32
+                and params.is_contiguous() and params.numel() == lib().fmmgen_order_model_nparam()):
+            raise ValueError("params must be a contiguous float32 CUDA tensor of the model's size")
+        check(lib().fmmgen_tree_set_order_model(self._h, C.c_void_p(params.data_ptr()), float(delta), float(eps)))
+        self._order_params = params  # kept alive while attached
+        return self
+
+    def m2l_orders(self):
+        """Host copy of the per-pair orders the last evaluation used."""
+        o = np.zeros(max(self.nm2l, 1), np.uint8)
+        check(lib().fmmgen_tree_export_m2l_orders(self._h, o.ctypes.data))
+        return o[: self.nm2l]
+
     def m2l_work(self):
         """Last tensor-core M2L: (class steps, MMA instructions, executed tensor flops)."""
         w = np.zeros(3)

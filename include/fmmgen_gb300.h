@@ -179,6 +179,60 @@ int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8);
  * instructions, executed tensor flops]; zeros if none ran. */
 int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3);
 
+/* ---- learned per-pair M2L orders (no counterpart in the reference, whose
+ * FMM applies one order to every pair) ----
+ * An M2L pair applied at order q < p keeps the terms |n| + |m| <= q of the
+ * order-p translation.  An order model is an MLP 16 -> 64 -> 64 -> 11 (ReLU,
+ * FP32 parameters W1[64][16], b1[64], W2[64][64], b2[64], W3[11][64], b3[11])
+ * whose 11 outputs are the logits of the orders 2..12.  Pairs are numbered in
+ * the order of fmmgen_tree_export_lists; every pointer below is device memory
+ * unless it says host. */
+int fmmgen_order_model_nparam(void);   /* 5963 */
+int fmmgen_order_nfeatures(void);      /* 16 */
+int fmmgen_order_nclasses(void);       /* 11: labels 0..10 are the orders 2..12 */
+/* The error budget of a pair B -> A for a relative L2 field error eps over
+ * its system: eps T_A, T_A = sqrt(sum_i |E_i|^2 / P) s_A^2 / sqrt(n_A) in the
+ * scaled units of A's local expansion, with E_i the near field (P2P part) of
+ * the system's particles in the last evaluate, P the system's M2L pairs, s_A
+ * and n_A A's half-width and particle count (the squared budget split equally
+ * over the pairs; A's error reaches all its particles).
+ * Features of every M2L pair from the multipoles and near field of the last
+ * evaluate, feat [nm2l][16]: lB - lA, log2(separation / s_A), log10 of the
+ * pair's share of its target's estimated far field, log10 of the part of
+ * degree 1..12 in the pair's estimate, log10 of the pair's estimated field at
+ * A over eps T_A. */
+int fmmgen_tree_order_features(fmmgen_tree *tree, double eps, float *feat, void *stream);
+/* Training labels (needs a last evaluate in FP64): for each pair the lowest
+ * order q in [2, p] whose truncation error bound in the target cell,
+ * sum_n max_cell |grad y^n / n!| |sum_{|n|+|m| > q} D_(n+m) M_m| (scaled
+ * units), stays within eps T_A; label = q - 2.  errq [nm2l][11] (may be NULL):
+ * the bound at q = 2..12 over eps T_A. */
+int fmmgen_tree_order_labels(fmmgen_tree *tree, double eps, unsigned char *label, float *errq, void *stream);
+/* Explicit per-pair orders (uint8 [nm2l], values clamped to [so + 1, p]) for
+ * the evaluations of this build; orders == NULL returns to the one order p. */
+int fmmgen_tree_set_m2l_orders(fmmgen_tree *tree, const unsigned char *orders, void *stream);
+/* Attach an order model (parameters stay caller-owned and must outlive its
+ * use): every evaluate then runs P2P before M2L, computes the features for
+ * the error target eps from its own multipoles and near field, and applies
+ * pair k at the lowest order whose cumulative predicted probability reaches
+ * 1 - delta.  params == NULL detaches it. */
+int fmmgen_tree_set_order_model(fmmgen_tree *tree, const float *params, float delta, double eps);
+/* Host copy of the per-pair orders the last evaluate used (uint8 [nm2l]);
+ * all p when it used one order. */
+int fmmgen_tree_export_m2l_orders(fmmgen_tree *tree, unsigned char *orders_host);
+/* Order-model inference on n feature rows: orders[k] in [2, qmax]. */
+int fmmgen_mlp_predict(const float *params, const float *X, long n, float delta, int qmax, unsigned char *orders,
+                       void *stream);
+/* One training step of the order model: mean cross-entropy of the logits
+ * against labels y (0..10) over n rows; grad [nparam] is overwritten with its
+ * gradient, *loss (device float) is incremented by its value.  work holds
+ * fmmgen_mlp_train_work(n) floats. */
+long fmmgen_mlp_train_work(int n);
+int fmmgen_mlp_train_step(const float *params, const float *X, const unsigned char *y, int n, float *grad,
+                          float *loss, float *work, void *stream);
+/* Adam update (beta1 0.9, beta2 0.999, eps 1e-8, bias-corrected, step >= 1). */
+int fmmgen_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -270,6 +270,7 @@ typedef struct {
     long *m2l; long nm2l, capm2l;   /* pairs (B=source, A=target) */
     long *p2p; long np2p, capp2p;   /* pairs (A=target, B=source) */
     int maxlevel;
+    unsigned char *m2l_ord;         /* per M2L pair (list order): its order, or NULL for `order` */
 } otree_t;
 
 static long add_cell(otree_t *t, double x, double y, double z, double r, long parent, int level) {
@@ -397,7 +398,26 @@ void or_tree_free(void *h) {
     otree_t *t = (otree_t *)h;
     if (!t) return;
     for (long c = 0; c < t->ncells; c++) free(t->cells[c].leaf);
-    free(t->cells); free(t->m2l); free(t->p2p); free(t);
+    free(t->cells); free(t->m2l); free(t->p2p); free(t->m2l_ord); free(t);
+}
+
+/* Per-pair M2L orders for the following evaluations (list order of
+ * or_tree_export_lists), clamped to [so + 1, order]; NULL: one order.  Pair
+ * k at order q applies fmmgen's order-q M2L operator, i.e. the terms
+ * |n| + |m| <= q of the order-`order` translation (the leading blocks of the
+ * degree-major M and L rows).  No counterpart in the reference. */
+void or_tree_set_m2l_orders(void *h, const unsigned char *orders) {
+    otree_t *t = (otree_t *)h;
+    free(t->m2l_ord);
+    t->m2l_ord = NULL;
+    if (!orders || t->nm2l == 0) return;
+    t->m2l_ord = (unsigned char *)malloc((size_t)t->nm2l);
+    for (long i = 0; i < t->nm2l; i++) {
+        int q = orders[i];
+        if (q < t->so + 1) q = t->so + 1;
+        if (q > t->order) q = t->order;
+        t->m2l_ord[i] = (unsigned char)q;
+    }
 }
 
 /* counts: [ncells, nleaves, nm2l, np2p, maxlevel] */
@@ -446,16 +466,22 @@ static double now_s(void) {
 
 /* Group pair list by target into CSR (stable: keeps list order per target). */
 static void csr_by_target(long npairs, const long *pairs, int tgt_slot, long ncells, long **off_out,
-                          long **src_out) {
+                          long **src_out, long **pair_out) {
     long *off = (long *)calloc(ncells + 1, sizeof(long));
     long *src = (long *)malloc(sizeof(long) * (npairs ? npairs : 1));
     for (long i = 0; i < npairs; i++) off[pairs[2 * i + tgt_slot] + 1]++;
     for (long c = 0; c < ncells; c++) off[c + 1] += off[c];
     long *fill = (long *)malloc(sizeof(long) * (ncells + 1));
     memcpy(fill, off, sizeof(long) * (ncells + 1));
-    for (long i = 0; i < npairs; i++) src[fill[pairs[2 * i + tgt_slot]]++] = pairs[2 * i + 1 - tgt_slot];
+    long *pidx = (long *)malloc(sizeof(long) * (npairs ? npairs : 1));
+    for (long i = 0; i < npairs; i++) {
+        long f = fill[pairs[2 * i + tgt_slot]]++;
+        src[f] = pairs[2 * i + 1 - tgt_slot];
+        pidx[f] = i;
+    }
     free(fill);
     *off_out = off; *src_out = src;
+    if (pair_out) *pair_out = pidx; else free(pidx);
 }
 
 /* Tree::compute_field_fmm (example/tree.cpp:243-271).  F is [N][outsize] in the
@@ -501,16 +527,17 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
                t->cells[p].z - t->cells[c].z, &M[(size_t)c * msize], &M[(size_t)p * msize], order, so);
     }
     double t2 = now_s();
-    long *moff, *msrc, *poff, *psrc;
-    csr_by_target(t->nm2l, t->m2l, 1, nc, &moff, &msrc);
-    csr_by_target(t->np2p, t->p2p, 0, nc, &poff, &psrc);
+    long *moff, *msrc, *mpair, *poff, *psrc;
+    csr_by_target(t->nm2l, t->m2l, 1, nc, &moff, &msrc, &mpair);
+    csr_by_target(t->np2p, t->p2p, 0, nc, &poff, &psrc, NULL);
     /* M2L (example/calculate.cpp:190-206), grouped by target instead of atomics */
 #pragma omp parallel for schedule(dynamic, 8)
     for (long A = 0; A < nc; A += sample_stride) {
         for (long k = moff[A]; k < moff[A + 1]; k++) {
             long B = msrc[k];
+            int q = t->m2l_ord ? t->m2l_ord[mpair[k]] : order;
             or_M2L(t->cells[A].x - t->cells[B].x, t->cells[A].y - t->cells[B].y,
-                   t->cells[A].z - t->cells[B].z, &M[(size_t)B * msize], &L[(size_t)A * lsize], order, so);
+                   t->cells[A].z - t->cells[B].z, &M[(size_t)B * msize], &L[(size_t)A * lsize], q, so);
         }
     }
     double t3 = now_s();
@@ -559,7 +586,7 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     if (times) memcpy(times, tt, sizeof(tt));
     if (Mout) memcpy(Mout, M, sizeof(double) * nc * msize);
     if (Lout) memcpy(Lout, L, sizeof(double) * nc * lsize);
-    free(M); free(L); free(moff); free(msrc); free(poff); free(psrc);
+    free(M); free(L); free(moff); free(msrc); free(mpair); free(poff); free(psrc);
     return 0;
 }
 

@@ -49,6 +49,7 @@ def lib():
         L.or_tree_info.argtypes = [C.c_void_p, _lp]
         L.or_tree_export_cells.argtypes = [C.c_void_p, _up, _lp, _dp, _lp, _lp, _lp, _lp]
         L.or_tree_export_lists.argtypes = [C.c_void_p, _up, _up]
+        L.or_tree_set_m2l_orders.argtypes = [C.c_void_p, C.c_void_p]
         L.or_tree_evaluate.restype = i
         L.or_tree_evaluate.argtypes = [C.c_void_p, _dp, i, i, l, C.c_void_p, C.c_void_p, _dp]
         L.or_direct.argtypes = [_dp, _dp, l, _lp, l, i, i, i, _dp]
@@ -148,6 +149,16 @@ class OracleTree:
         p2p = np.zeros(2 * max(self.np2p, 1), np.uint64)
         lib().or_tree_export_lists(self.h, m2l, p2p)
         return m2l[: 2 * self.nm2l].reshape(-1, 2), p2p[: 2 * self.np2p].reshape(-1, 2)
+
+    def set_m2l_orders(self, orders=None):
+        """Per-pair M2L orders in the order of lists() (None: the one order)."""
+        if orders is None:
+            lib().or_tree_set_m2l_orders(self.h, None)
+            return
+        o = np.ascontiguousarray(orders, dtype=np.uint8)
+        if o.shape != (self.nm2l,):
+            raise ValueError("one order per M2L pair")
+        lib().or_tree_set_m2l_orders(self.h, o.ctypes.data)
 
     def evaluate(self, potential=True, field=True, sample_stride=1, want_ML=False):
         F = np.zeros(self.N * outsize(potential, field))
