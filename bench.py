@@ -505,11 +505,14 @@ def main():
     dom = max(cand, key=lambda k: cand[k][0])
     dom_ms, dom_flops = cand[dom]
     traffic = None
-    try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = tr.get(dom, {}).get("bytes_per_launch")
-    except Exception:
-        pass
+    if a.config == "uniform_1m_p8" and a.n == 1_000_000:  # the workload the ncu capture ran
+        try:
+            for ln in open(os.path.join(ROOT, "profiles", "dram_traffic_uniform_1m_p8.txt")):
+                f = ln.split()
+                if len(f) == 2 and not ln.startswith("#") and f[0] == dom:
+                    traffic = float(f[1])
+        except OSError:
+            pass
     achieved = dom_flops / (dom_ms / 1e3) / 1e12 if dom_ms > 0 else 0.0
     roofline = {"kernel": dom, "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak, "traffic": traffic,

@@ -382,7 +382,11 @@ static int rec(DevTree *t, int i, cudaStream_t st) {
 }
 
 template <typename T>
-static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, bool tc, int mstr,
+static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed, int impl, int mstr, int lstr,
+                     int dstr, cudaStream_t st);
+
+template <typename T>
+static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, int impl, int mstr,
                     int lstr, int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so;
   const double *cr = t->cr.p;  // per-cell half-widths
@@ -402,49 +406,13 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 2, st));
-  // M2L: tensor cores (FP32 mixed pass, order <= 9), else register-resident
-  // generated kernels where this order has them (FP32), else the warp
-  // contraction engine
-  m2l_reg_kernel kg[4];
-  int kthreads[4];
-  int ng = mixed && !tc ? m2l_reg_kernels(p, so, kg, kthreads) : 0;
   // with an order model, P2P runs first: the predicted orders read its near field
   t->p2p_first = t->ord_mode == 2;
   if (t->p2p_first) {
     TRY(fmm_p2p_launch(t, mixed, S, st));
     TRY(rec(t, 3, st));
   }
-  if (t->ord_mode != 0) {
-    // per-pair orders: predicted now from this pass's multipoles, or given
-    if (t->ord_mode == 2) TRY(fmm_learned_orders(t, st));
-    else if (t->ord_serial != t->build_serial) {
-      fmm_set_error_text("per-pair M2L orders were set for an earlier build");
-      return FMM_ERR_STATE;
-    }
-    PlanVar PV;
-    for (int q = 0; q <= FMM_PMAX; q++) {
-      const PlanSet *pq = q >= so + 1 && q <= p ? fmm_get_plans(q, so) : nullptr;
-      PV.p[q] = pq ? pq->m2l : Plan();
-    }
-    fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        PV, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
-        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
-        lstr, dstr);
-  } else if (tc) {
-    TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
-  } else if (ng > 0) {
-    for (int g = 0; g < ng; g++)
-      fmm_note_launch(), kg[g]<<<(nc + kthreads[g] - 1) / kthreads[g], kthreads[g], 0, st>>>(
-          t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
-          (const float *)t->cls_Df.p, t->clevel.p,
-          (const float *)(const void *)M, (float *)(void *)L);
-  } else {
-    fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
-        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
-        lstr, dstr);
-  }
-  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, st));
   if (t->p2p_first) {
     TRY(rec(t, 4, st));
   } else {
@@ -468,6 +436,67 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
       t->pz.p, so, p, cr, L, t->Ffar.p, lstr);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 6, st));
+  return FMM_OK;
+}
+
+// M2L implementation of a pass: per-pair orders when set; else (mixed pass)
+// the tuned choice or, by default, tensor cores where the order allows
+// (p <= 9, precision "mixed"), else the generated CUDA-core kernels where this
+// order has them, else the warp contraction engine; FP64: the engine.
+enum { M2L_TC = 0, M2L_GEN = 1, M2L_ENGINE = 2 };
+bool fmm_m2l_gen_supported(int p, int so) {
+  m2l_reg_kernel kg[4];
+  int kt[4];
+  return m2l_reg_kernels(p, so, kg, kt) > 0;
+}
+static int m2l_impl(const DevTree *t, int precision) {
+  if (precision == 0) return M2L_ENGINE;
+  const bool tc_ok = fmm_m2l_tc_supported(t->order, t->so), gen_ok = fmm_m2l_gen_supported(t->order, t->so);
+  int impl = t->tune.impl;
+  if (impl < 0) impl = precision == 1 ? M2L_TC : M2L_GEN;
+  if (impl == M2L_TC && !tc_ok) impl = M2L_GEN;
+  if (impl == M2L_GEN && !gen_ok) impl = M2L_ENGINE;
+  return impl;
+}
+
+template <typename T>
+static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed, int impl, int mstr, int lstr,
+                     int dstr, cudaStream_t st) {
+  const int p = t->order, so = t->so, nc = t->ncells;
+  if (t->ord_mode != 0) {
+    // per-pair orders: predicted now from this pass's multipoles, or given
+    if (t->ord_mode == 2) TRY(fmm_learned_orders(t, st));
+    else if (t->ord_serial != t->build_serial) {
+      fmm_set_error_text("per-pair M2L orders were set for an earlier build");
+      return FMM_ERR_STATE;
+    }
+    PlanVar PV;
+    for (int q = 0; q <= FMM_PMAX; q++) {
+      const PlanSet *pq = q >= so + 1 && q <= p ? fmm_get_plans(q, so) : nullptr;
+      PV.p[q] = pq ? pq->m2l : Plan();
+    }
+    fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        PV, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
+        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
+        lstr, dstr);
+  } else if (mixed && impl == M2L_TC) {
+    TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
+  } else if (mixed && impl == M2L_GEN) {
+    m2l_reg_kernel kg[4];
+    int kthreads[4];
+    const int ng = m2l_reg_kernels(p, so, kg, kthreads);
+    for (int g = 0; g < ng; g++)
+      fmm_note_launch(), kg[g]<<<(nc + kthreads[g] - 1) / kthreads[g], kthreads[g], 0, st>>>(
+          t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
+          (const float *)t->cls_Df.p, t->clevel.p,
+          (const float *)(const void *)M, (float *)(void *)L);
+  } else {
+    fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
+        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
+        lstr, dstr);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
 
@@ -528,8 +557,9 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
   const PlanSet *ps = fmm_get_plans(t->order, t->so);
   if (!ps) return FMM_ERR_CUDA;
   const bool mixed = precision != 0;
-  const bool tc = precision == 1 && fmm_m2l_tc_supported(t->order, t->so);
+  const int impl = m2l_impl(t, precision);
   t->last_prec = mixed ? 1 : 0;
+  if (t->grouping_built != t->tune.grouping) TRY(fmm_m2l_cell_order(t, t->tune.grouping, st));
   const int p = t->order, so = t->so;
   const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
   const size_t nc = t->ncells;
@@ -544,16 +574,32 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
     TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
     TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
     TRY(fmm_stage_particles(t, S, st));
-    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, tc, mstr, lstr, dstr, st));
+    TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, impl, mstr, lstr, dstr, st));
   } else {
     TRY(fmm_reserve(t->M, nc * msize));
     TRY(fmm_reserve(t->L, nc * lsize));
-    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, false, (int)msize, (int)lsize, fmm_nterms(p), st));
+    TRY(run_pass<double>(t, ps, S, t->M.p, t->L.p, false, impl, (int)msize, (int)lsize, fmm_nterms(p), st));
   }
   fmm_note_launch(), k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N, potential, field, F);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 7, st));
   return FMM_OK;
+}
+
+// The M2L phase alone on the multipoles of the last pass (same precision
+// class): the autotuner's timed unit.
+int fmm_m2l_only(DevTree *t, int precision, cudaStream_t st) {
+  if (t->last_prec < 0 || (precision != 0) != (t->last_prec != 0) || t->ord_mode != 0) return FMM_ERR_STATE;
+  const PlanSet *ps = fmm_get_plans(t->order, t->so);
+  if (!ps) return FMM_ERR_CUDA;
+  if (t->grouping_built != t->tune.grouping) TRY(fmm_m2l_cell_order(t, t->tune.grouping, st));
+  const int p = t->order, so = t->so;
+  const int msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
+  const int impl = m2l_impl(t, precision);
+  if (precision != 0)
+    return m2l_phase<float>(t, ps, t->Mf.p, t->Lf.p, true, impl, fmm_stride4(msize), fmm_stride4(lsize),
+                            fmm_stride4(fmm_nterms(p)), st);
+  return m2l_phase<double>(t, ps, t->M.p, t->L.p, false, impl, msize, lsize, fmm_nterms(p), st);
 }
 
 // Per-phase times of the last evaluate (needs the stream to have completed).

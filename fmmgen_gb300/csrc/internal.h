@@ -66,7 +66,14 @@ struct DevTree {
   DevBuf<int> cell_leaf;                  // cell -> leaf ordinal or -1
   // interaction lists, grouped by target cell (CSR over cells)
   DevBuf<int> m2l_off, m2l_src, m2l_cls;  // per target: sorted by class
-  DevBuf<int> m2l_order;                  // cells in M2L processing order (level, interaction pattern)
+  DevBuf<int> m2l_order;                  // cells in M2L processing order (level, then the grouping below)
+  // M2L choices (set by fmmgen_tree_set_tune / the autotuner; -1 / 0: the default rules)
+  struct M2LTune {
+    int impl = -1;      // mixed pass: 0 tensor cores, 1 generated CUDA-core kernels, 2 contraction engine
+    int nslots = 0;     // tensor-core pipeline depth (row-gather slots), 0: as many as fit
+    int grouping = 0;   // cell order within a level: 0 by octant within the parent, 1 Morton
+  } tune;
+  int grouping_built = 0;                 // grouping m2l_order holds
   DevBuf<int> p2p_off, p2p_src;
   // M2L translation classes: operator vectors D^(k)(d/s_target), |k| <= order
   DevBuf<int> cls_key4;                   // [nclasses][4]: dlev, dx, dy, dz
@@ -141,6 +148,12 @@ int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int
 void fmm_tree_destroy(DevTree *t);
 void fmm_graph_release(DevTree *t);
 bool fmm_m2l_tc_supported(int p, int so);
+int fmm_m2l_tc_max_slots(int p, int so);       // 0 when the tensor-core M2L does not support (p, so)
+bool fmm_m2l_gen_supported(int p, int so);     // generated CUDA-core M2L kernels exist
+int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st);
+int fmm_m2l_only(DevTree *t, int precision, cudaStream_t st);  // the M2L phase alone (after a pass)
+int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand3, float *cand_ms,
+                 int *ncand, cudaStream_t st);
 // learned per-pair orders (learn.cu)
 int fmm_mlp_nparam();
 int fmm_order_features(DevTree *t, double eps, float *feat, cudaStream_t st);

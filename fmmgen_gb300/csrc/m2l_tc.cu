@@ -639,6 +639,11 @@ bool fmm_m2l_tc_supported(int p, int so) {
   return tc_plan(p, so, pl);
 }
 
+int fmm_m2l_tc_max_slots(int p, int so) {
+  TcPlan pl;
+  return tc_plan(p, so, pl) ? pl.nslots : 0;
+}
+
 // Executed tensor work of one class step of a 128-row tile: MMA instructions
 // and flops (3 products per K chunk, each 2 x 128 x 16 x N).
 bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops) {
@@ -702,7 +707,9 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   P.kpad = pl.kpad;
   P.kch = pl.kch;
   P.nkb = pl.nkb;
-  P.nslots = pl.nslots;
+  // pipeline depth: as many row-gather slots as fit, or fewer when tuned so
+  P.nslots = t->tune.nslots >= 2 ? std::min(pl.nslots, t->tune.nslots) : pl.nslots;
+  const int smem = 1024 + P.nslots * pl.slot_bytes + (int)sizeof(TcShared);
   P.cls_bytes = pl.cls_bytes;
   P.cls_scale = pl.cls_scale;
   P.slot_bytes = pl.slot_bytes;
@@ -713,14 +720,14 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   const int grid = std::min(P.ntiles, tc_sm_count());
   int rc;
   switch (pl.nout) {
-    case 16: rc = tc_launch<16>(P, pl.smem, grid, st); break;
-    case 32: rc = tc_launch<32>(P, pl.smem, grid, st); break;
-    case 48: rc = tc_launch<48>(P, pl.smem, grid, st); break;
-    case 64: rc = tc_launch<64>(P, pl.smem, grid, st); break;
-    case 96: rc = tc_launch<96>(P, pl.smem, grid, st); break;
-    case 128: rc = tc_launch<128>(P, pl.smem, grid, st); break;
-    case 176: rc = tc_launch<176>(P, pl.smem, grid, st); break;
-    case 224: rc = tc_launch<224>(P, pl.smem, grid, st); break;
+    case 16: rc = tc_launch<16>(P, smem, grid, st); break;
+    case 32: rc = tc_launch<32>(P, smem, grid, st); break;
+    case 48: rc = tc_launch<48>(P, smem, grid, st); break;
+    case 64: rc = tc_launch<64>(P, smem, grid, st); break;
+    case 96: rc = tc_launch<96>(P, smem, grid, st); break;
+    case 128: rc = tc_launch<128>(P, smem, grid, st); break;
+    case 176: rc = tc_launch<176>(P, smem, grid, st); break;
+    case 224: rc = tc_launch<224>(P, smem, grid, st); break;
     default: return FMM_ERR_ARG;
   }
   if (rc) return rc;

@@ -552,11 +552,12 @@ __global__ void k_class_lookup(const uint64_t *keys, long n, const uint64_t *tab
 // order, and the warps of the CUDA-core M2L read the same operator rows.
 // Cells are stored level by level in parent order, so a stable sort on
 // (level, octant) alone keeps the parents in Morton order.
-__global__ void k_order_keys(int nc, const uint64_t *cid, const unsigned char *clevel, uint64_t *key,
+// grouping 1 keeps plain Morton order within a level (the key is the level alone).
+__global__ void k_order_keys(int nc, const uint64_t *cid, const unsigned char *clevel, int grouping, uint64_t *key,
                              uint32_t *idx) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  key[c] = ((uint64_t)clevel[c] << 56) | ((cid[c] & 7u) << 48);
+  key[c] = ((uint64_t)clevel[c] << 56) | (grouping == 0 ? (cid[c] & 7u) << 48 : 0u);
   idx[c] = (uint32_t)c;
 }
 
@@ -1022,7 +1023,13 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_class_derivs<<<fmm_blocks(ncls, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(t->cls_key4.p, (int)ncls, p, t->cls_D.p,
                                                                          t->cls_Df.p, t->d_cls_same.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  // the M2L processing order (level, interaction pattern)
+  return fmm_m2l_cell_order(t, t->tune.grouping, st);
+}
+
+// The M2L processing order of the cells (t->m2l_order): level, then by octant
+// within the parent (grouping 0) or Morton order (grouping 1).
+int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st) {
+  const int nc = t->ncells;
   size_t nbh = fmm_rs_nblocks(nc);
   size_t hist_n = 256 * nbh;
   TRY(tmp_reserve(t, (size_t)nc * 20 + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 256));
@@ -1033,10 +1040,11 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   uint32_t *hist = (uint32_t *)q; q += hist_n * 4;
   uint32_t *stmp2 = (uint32_t *)q;
   TRY(fmm_reserve(t->m2l_order, nc));
-  fmm_note_launch(), k_order_keys<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->cid.p, t->clevel.p, k1,
+  fmm_note_launch(), k_order_keys<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->cid.p, t->clevel.p, grouping, k1,
                                                                         (uint32_t *)t->m2l_order.p);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(fmm_radix_sort<uint64_t>(k1, (uint32_t *)t->m2l_order.p, k2, v2, nc, 48, 64, hist, stmp2, st));
+  t->grouping_built = grouping;
   return FMM_OK;
 }
 

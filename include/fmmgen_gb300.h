@@ -179,6 +179,24 @@ int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8);
  * instructions, executed tensor flops]; zeros if none ran. */
 int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3);
 
+/* ---- M2L choices and their autotuner (no counterpart in the reference) ----
+ * impl: -1 the default rules (tensor cores for "mixed" where p <= 9, else the
+ * generated CUDA-core kernels where the order has them, else the warp
+ * contraction engine), 0 tensor cores, 1 generated CUDA-core kernels,
+ * 2 contraction engine (mixed passes; FP64 passes always use the engine).
+ * nslots: tensor-core pipeline depth (row-gather slots), 0 = as many as fit.
+ * grouping: order of a level's cells in M2L tiles and warps, 0 by octant
+ * within the parent, 1 Morton.  Unsupported choices are rejected. */
+int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping);
+int fmmgen_tree_get_tune(fmmgen_tree *tree, int *impl3);
+/* Autotuner: one pass over S at `precision` (for the multipoles), then the
+ * M2L phase alone timed `reps` times per candidate (implementation x pipeline
+ * depth x grouping that this order supports); the handle keeps the candidate
+ * with the lowest median.  cand3 [max_cand][3] (impl, nslots, grouping) and
+ * cand_ms [max_cand] receive the table (either may be NULL), *ncand its size. */
+int fmmgen_tree_autotune(fmmgen_tree *tree, const double *S, int precision, int reps, int max_cand, int *cand3,
+                         float *cand_ms, int *ncand, void *stream);
+
 /* ---- learned per-pair M2L orders (no counterpart in the reference, whose
  * FMM applies one order to every pair) ----
  * An M2L pair applied at order q < p keeps the terms |n| + |m| <= q of the
