@@ -77,6 +77,7 @@ def args_parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--nsys", type=int, default=NSYS_BATCHED, help="systems of the batched configuration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default M2L rules (no autotuner run)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
     ap.add_argument("--profile-only", action="store_true",
@@ -335,6 +336,14 @@ def main():
 
     tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta, source_order=a.so,
                    sys_off=sys_offsets(a) if a.sizes is not None else None)
+    autotune = None
+    if not a.no_autotune and a.dist != "mixture":
+        # the M2L autotuner, once before the warm-up (outside every timed region)
+        r = tree.autotune(precision="mixed", reps=3)
+        autotune = {"chosen": r["best"], "candidates_ms": [
+            [c["impl"], c["nslots"], c["grouping"], round(c["ms"], 3)] for c in r["table"]],
+            "legend": "impl 0 tensor cores / 1 generated CUDA-core / 2 contraction engine; nslots = tensor-core "
+                      "pipeline depth; grouping 0 by octant / 1 Morton; M2L phase median ms"}
     model = None
     if a.dist == "mixture":  # learned per-pair M2L orders: every pass predicts them from its multipoles
         from fmmgen_gb300 import learned
@@ -541,7 +550,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "eval_only": eval_only, "roofline": roofline, "roofline_m2l": roofline_m2l,
             "fp64_plain": fp64, "speedup_vs_fp64": (value / world) / fp64["value"] if fp64 else None,
-            "learned_orders": learned_info,
+            "learned_orders": learned_info, "m2l_autotune": autotune,
             "phases_ms": {k: round(v, 3) for k, v in ph.items()},
             "tree": {"cells": tree.ncells, "leaves": tree.nleaves, "m2l_pairs": tree.nm2l, "p2p_pairs": tree.np2p,
                      "p2p_interactions": tree.p2p_interactions, "m2l_classes": tree.nclasses},

@@ -559,6 +559,7 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
   const bool mixed = precision != 0;
   const int impl = m2l_impl(t, precision);
   t->last_prec = mixed ? 1 : 0;
+  t->pass_potential = potential != 0;
   if (t->grouping_built != t->tune.grouping) TRY(fmm_m2l_cell_order(t, t->tune.grouping, st));
   const int p = t->order, so = t->so;
   const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);

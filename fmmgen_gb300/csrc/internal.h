@@ -133,6 +133,7 @@ struct DevTree {
   double model_eps = 1e-6;                // error target the model's features are scaled to
   int last_prec = -1;                     // precision of the last evaluation (-1: none)
   bool p2p_first = false;                 // the last pass ran P2P before M2L (phase times swap)
+  bool pass_potential = true;             // the pass outputs the potential (the P2P sums it only then)
   DevBuf<float> mnorm, feat;              // per-cell multipole degree norms; per-pair features
   DevBuf<double> tscale, tpart;           // per system: sqrt(sum |E_near|^2 / M2L pairs); partial sums
   DevBuf<int> sys_pairs;                  // per system: M2L pairs

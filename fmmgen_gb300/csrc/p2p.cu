@@ -104,8 +104,11 @@ __global__ void k_stage_particles(const int *leaf_cells, int nleaves, const int 
 // from integer cell coordinates, so the displacement keeps ~1e-7 relative
 // accuracy even for very close pairs.  Each source leaf's contribution is
 // summed in FP32 and folded into a Kahan-compensated FP32 total; the final
-// per-particle near + far sum is FP64 (k_finalize).  1/R is the hardware
-// approximation refined by one Newton step.
+// per-particle near + far sum is FP64 (k_finalize).  1/R of a charge pair is
+// the hardware approximation (relative error ~1e-7, the size of the FP32
+// displacement's own rounding); the dipole kernel, whose terms carry 1/R^5,
+// refines it with one Newton step.  The potential is summed only when it is
+// an output.
 __device__ __forceinline__ float rsqrt_approx(float x) {
   float y;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -135,7 +138,7 @@ __device__ __forceinline__ void add2(float ah, float al, float oh, float ol, flo
   tl = ((ah - (th - bv)) + (oh - bv)) + (al + ol);
 }
 
-template <bool SELF>
+template <bool SELF, bool POT>
 __device__ __forceinline__ void coulomb_one(const float4 &q, const float4 &ql, bool self, float txh, float txl,
                                             float tyh, float tyl, float tzh, float tzl, float &phi, float &ex,
                                             float &ey, float &ez) {
@@ -143,11 +146,11 @@ __device__ __forceinline__ void coulomb_one(const float4 &q, const float4 &ql, b
   const float dy = (tyh - q.y) + (tyl - ql.y);
   const float dz = (tzh - q.z) + (tzl - ql.z);
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-  float rinv = rsqrt_nr(r2);
+  float rinv = rsqrt_approx(r2);
   if (SELF) rinv = self ? 0.f : rinv;  // l2 != l1
   const float qr = q.w * rinv;
   const float qr3 = qr * (rinv * rinv);
-  phi += qr;
+  if (POT) phi += qr;
   ex = fmaf(qr3, dx, ex);
   ey = fmaf(qr3, dy, ey);
   ez = fmaf(qr3, dz, ez);
@@ -156,7 +159,7 @@ __device__ __forceinline__ void coulomb_one(const float4 &q, const float4 &ql, b
 // Sources first, first + step, ... < cnt of the staged chunk.  With one lane
 // per target (step 1) the loop runs in blocks of 8 with constant shared-memory
 // offsets, so nothing but the interaction itself sits in the loop body.
-template <bool SELF>
+template <bool SELF, bool POT>
 __device__ __forceinline__ void p2p_coulomb(const float4 *sh, const float4 *sl, int first, int cnt, int step,
                                             int selfj, float txh, float txl, float tyh, float tyl, float tzh,
                                             float tzl, float &phi, float &ex, float &ey, float &ez) {
@@ -165,15 +168,16 @@ __device__ __forceinline__ void p2p_coulomb(const float4 *sh, const float4 *sl, 
     for (; jj + 8 <= cnt; jj += 8) {
 #pragma unroll
       for (int u = 0; u < 8; u++)
-        coulomb_one<SELF>(sh[jj + u], sl[jj + u], jj + u == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+        coulomb_one<SELF, POT>(sh[jj + u], sl[jj + u], jj + u == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey,
+                               ez);
     }
     for (; jj < cnt; jj++)
-      coulomb_one<SELF>(sh[jj], sl[jj], jj == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+      coulomb_one<SELF, POT>(sh[jj], sl[jj], jj == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
     return;
   }
 #pragma unroll 4
   for (int jj = first; jj < cnt; jj += step)
-    coulomb_one<SELF>(sh[jj], sl[jj], jj == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+    coulomb_one<SELF, POT>(sh[jj], sl[jj], jj == selfj, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
 }
 
 template <bool SELF>
@@ -200,6 +204,7 @@ __device__ __forceinline__ void p2p_dipole(const float4 *sh, const float4 *sl, c
   }
 }
 
+template <bool POT>
 __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
                                                           const int *pcount, const int *off_, const int *src,
                                                           const int *ix, const int *iy, const int *iz,
@@ -251,9 +256,10 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
         const int cnt = min(32, nb - sb);
         if (so == 0) {
           if (B == A)
-            p2p_coulomb<true>(sh[w], sl[w], slice, cnt, f, i - (b0 + sb), txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+            p2p_coulomb<true, POT>(sh[w], sl[w], slice, cnt, f, i - (b0 + sb), txh, txl, tyh, tyl, tzh, tzl, phi, ex,
+                                   ey, ez);
           else
-            p2p_coulomb<false>(sh[w], sl[w], slice, cnt, f, -1, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+            p2p_coulomb<false, POT>(sh[w], sl[w], slice, cnt, f, -1, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
         } else {
           if (B == A)
             p2p_dipole<true>(sh[w], sl[w], sd[w], slice, cnt, f, i - (b0 + sb), txh, txl, tyh, tyl, tzh, tzl, phi,
@@ -288,14 +294,16 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
 // ---------------------------------------------------------------------------
 int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st) {
   const int nl = t->nleaves, so = t->so;
-  if (mixed)
-    fmm_note_launch(), k_p2p32<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
+  if (mixed) {
+    auto k = t->pass_potential || so ? k_p2p32<true> : k_p2p32<false>;
+    fmm_note_launch(), k<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->ix.p, t->iy.p, t->iz.p,
         t->clevel.p, t->crf.p, t->phi4.p, t->plo4.p, t->sdip.p, so, t->Fnear.p);
-  else
+  } else {
     fmm_note_launch(), k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->px.p, t->py.p, t->pz.p,
         t->perm.p, S, so, t->Fnear.p);
+  }
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
