@@ -341,9 +341,11 @@ def main():
         # the M2L autotuner, once before the warm-up (outside every timed region)
         r = tree.autotune(precision="mixed", reps=3)
         autotune = {"chosen": r["best"], "candidates_ms": [
-            [c["impl"], c["nslots"], c["grouping"], round(c["ms"], 3)] for c in r["table"]],
+            [c["impl"], c["nslots"], c["grouping"], c["overlap"], round(c["ms"], 3)] for c in r["table"]],
             "legend": "impl 0 tensor cores / 1 generated CUDA-core / 2 contraction engine; nslots = tensor-core "
-                      "pipeline depth; grouping 0 by octant / 1 Morton; M2L phase median ms"}
+                      "pipeline depth; grouping 0 by octant / 1 Morton; overlap 1 / 2 = M2L and P2P side by side "
+                      "(P2P blocks of 4 / 2 warps); "
+                      "M2L + P2P median ms"}
     model = None
     if a.dist == "mixture":  # learned per-pair M2L orders: every pass predicts them from its multipoles
         from fmmgen_gb300 import learned

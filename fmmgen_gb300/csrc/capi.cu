@@ -370,11 +370,12 @@ extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3) {
 
 // ---- M2L choices and the autotuner -------------------------------------------
 extern "C" {
-int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping) {
+int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping, int overlap) {
   g_err.clear();
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   DevTree &t = tree->t;
-  if (impl < -1 || impl > 2 || nslots < 0 || grouping < 0 || grouping > 1) return ret(FMM_ERR_ARG);
+  if (impl < -1 || impl > 2 || nslots < 0 || grouping < 0 || grouping > 1 || overlap < 0 || overlap > 2)
+    return ret(FMM_ERR_ARG);
   if (impl == 0 && !fmm_m2l_tc_supported(t.order, t.so)) {
     fmm_set_error_text("the tensor-core M2L does not support this order / source order");
     return ret(FMM_ERR_ARG);
@@ -387,23 +388,25 @@ int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping) 
   t.tune.impl = impl;
   t.tune.nslots = nslots;
   t.tune.grouping = grouping;
+  t.tune.overlap = overlap;
   return FMM_OK;
 }
 
-int fmmgen_tree_get_tune(fmmgen_tree *tree, int *impl3) {
-  if (!tree || !tree->built || !impl3) return ret(FMM_ERR_STATE);
-  impl3[0] = tree->t.tune.impl;
-  impl3[1] = tree->t.tune.nslots;
-  impl3[2] = tree->t.tune.grouping;
+int fmmgen_tree_get_tune(fmmgen_tree *tree, int *tune4) {
+  if (!tree || !tree->built || !tune4) return ret(FMM_ERR_STATE);
+  tune4[0] = tree->t.tune.impl;
+  tune4[1] = tree->t.tune.nslots;
+  tune4[2] = tree->t.tune.grouping;
+  tune4[3] = tree->t.tune.overlap;
   return FMM_OK;
 }
 
-int fmmgen_tree_autotune(fmmgen_tree *tree, const double *Sv, int precision, int reps, int max_cand, int *cand3,
+int fmmgen_tree_autotune(fmmgen_tree *tree, const double *Sv, int precision, int reps, int max_cand, int *cand4,
                          float *cand_ms, int *ncand, void *st) {
   g_err.clear();
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   if (!Sv || precision < 0 || precision > 2 || reps < 1 || max_cand < 0) return ret(FMM_ERR_ARG);
-  const int rc = fmm_autotune(&tree->t, Sv, precision, reps, max_cand, cand3, cand_ms, ncand, S(st));
+  const int rc = fmm_autotune(&tree->t, Sv, precision, reps, max_cand, cand4, cand_ms, ncand, S(st));
   if (rc == FMM_OK) tree->last_precision = precision;
   return ret(rc);
 }

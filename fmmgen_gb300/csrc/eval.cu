@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(32 * L2P_WARPS) k_l2p(const int *leaf_cells, i
 }
 
 // P2P and the FP32 staging live in p2p.cu
-int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st);
+int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st, bool narrow = false);
 int fmm_stage_particles(DevTree *t, const double *S, cudaStream_t st);
 
 // F[caller index][outsize] = near + far, in FP64
@@ -386,6 +386,10 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
                      int dstr, cudaStream_t st);
 
 template <typename T>
+static int m2l_p2p(DevTree *t, const PlanSet *ps, const double *S, const T *M, T *L, bool mixed, int impl, int mstr,
+                   int lstr, int dstr, cudaStream_t st);
+
+template <typename T>
 static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, int impl, int mstr,
                     int lstr, int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so;
@@ -412,15 +416,11 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
     TRY(fmm_p2p_launch(t, mixed, S, st));
     TRY(rec(t, 3, st));
   }
-  TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, st));
   if (t->p2p_first) {
+    TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, st));
     TRY(rec(t, 4, st));
   } else {
-    TRY(rec(t, 3, st));
-    // P2P (running it concurrently with M2L on a second stream was measured to
-    // give no gain: the two kernels slow each other down when co-resident)
-    TRY(fmm_p2p_launch(t, mixed, S, st));
-    TRY(rec(t, 4, st));
+    TRY(m2l_p2p<T>(t, ps, S, M, L, mixed, impl, mstr, lstr, dstr, st));
   }
   // L2L, top-down
   for (int l = 1; l < t->nlevels; l++) {
@@ -457,6 +457,42 @@ static int m2l_impl(const DevTree *t, int precision) {
   if (impl == M2L_TC && !tc_ok) impl = M2L_GEN;
   if (impl == M2L_GEN && !gen_ok) impl = M2L_ENGINE;
   return impl;
+}
+
+static int side_stream(DevTree *t) {
+  if (t->s_hi) return FMM_OK;
+  int lo = 0, hi = 0;
+  FMM_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  FMM_CUDA_TRY(cudaStreamCreateWithPriority(&t->s_hi, cudaStreamNonBlocking, hi));
+  FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming));
+  FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming));
+  return FMM_OK;
+}
+
+// M2L, then P2P (phase records 3 and 4).  With the overlap switch and the
+// tensor-core M2L, the M2L runs on a highest-priority side stream -- its
+// persistent CTAs take one SM each first -- and the P2P blocks run beside it
+// in the registers and shared memory the M2L CTA leaves free (one 4-warp block
+// per SM), so the P2P's FP32 work fills issue slots of the latency-bound MMA
+// pipeline; record 3 marks the M2L's end, record 4 the join.
+template <typename T>
+static int m2l_p2p(DevTree *t, const PlanSet *ps, const double *S, const T *M, T *L, bool mixed, int impl, int mstr,
+                   int lstr, int dstr, cudaStream_t st) {
+  if (!(t->tune.overlap && mixed && impl == M2L_TC && t->nm2l > 0)) {
+    TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, st));
+    TRY(rec(t, 3, st));
+    TRY(fmm_p2p_launch(t, mixed, S, st));
+    return rec(t, 4, st);
+  }
+  TRY(side_stream(t));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_fork, st));
+  FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_fork, 0));
+  TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, t->s_hi));
+  TRY(rec(t, 3, t->s_hi));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_join, t->s_hi));
+  TRY(fmm_p2p_launch(t, mixed, S, st, t->tune.overlap == 2));
+  FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
+  return rec(t, 4, st);
 }
 
 template <typename T>
@@ -587,9 +623,9 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
   return FMM_OK;
 }
 
-// The M2L phase alone on the multipoles of the last pass (same precision
-// class): the autotuner's timed unit.
-int fmm_m2l_only(DevTree *t, int precision, cudaStream_t st) {
+// The M2L and P2P phases alone on the multipoles and staged particles of the
+// last pass (same precision class): the autotuner's timed unit.
+int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st) {
   if (t->last_prec < 0 || (precision != 0) != (t->last_prec != 0) || t->ord_mode != 0) return FMM_ERR_STATE;
   const PlanSet *ps = fmm_get_plans(t->order, t->so);
   if (!ps) return FMM_ERR_CUDA;
@@ -598,9 +634,9 @@ int fmm_m2l_only(DevTree *t, int precision, cudaStream_t st) {
   const int msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
   const int impl = m2l_impl(t, precision);
   if (precision != 0)
-    return m2l_phase<float>(t, ps, t->Mf.p, t->Lf.p, true, impl, fmm_stride4(msize), fmm_stride4(lsize),
-                            fmm_stride4(fmm_nterms(p)), st);
-  return m2l_phase<double>(t, ps, t->M.p, t->L.p, false, impl, msize, lsize, fmm_nterms(p), st);
+    return m2l_p2p<float>(t, ps, S, t->Mf.p, t->Lf.p, true, impl, fmm_stride4(msize), fmm_stride4(lsize),
+                          fmm_stride4(fmm_nterms(p)), st);
+  return m2l_p2p<double>(t, ps, S, t->M.p, t->L.p, false, impl, msize, lsize, fmm_nterms(p), st);
 }
 
 // Per-phase times of the last evaluate (needs the stream to have completed).

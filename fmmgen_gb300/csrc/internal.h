@@ -72,7 +72,11 @@ struct DevTree {
     int impl = -1;      // mixed pass: 0 tensor cores, 1 generated CUDA-core kernels, 2 contraction engine
     int nslots = 0;     // tensor-core pipeline depth (row-gather slots), 0: as many as fit
     int grouping = 0;   // cell order within a level: 0 by octant within the parent, 1 Morton
+    int overlap = 0;    // tensor-core M2L on a high-priority side stream, P2P beside it on the SMs' spare
+                        // room in blocks of 4 (1) or 2 (2) warps
   } tune;
+  cudaStream_t s_hi = nullptr;            // the side stream (highest priority)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int grouping_built = 0;                 // grouping m2l_order holds
   DevBuf<int> p2p_off, p2p_src;
   // M2L translation classes: operator vectors D^(k)(d/s_target), |k| <= order
@@ -152,8 +156,8 @@ bool fmm_m2l_tc_supported(int p, int so);
 int fmm_m2l_tc_max_slots(int p, int so);       // 0 when the tensor-core M2L does not support (p, so)
 bool fmm_m2l_gen_supported(int p, int so);     // generated CUDA-core M2L kernels exist
 int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st);
-int fmm_m2l_only(DevTree *t, int precision, cudaStream_t st);  // the M2L phase alone (after a pass)
-int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand3, float *cand_ms,
+int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st);  // M2L + P2P alone (after a pass)
+int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand4, float *cand_ms,
                  int *ncand, cudaStream_t st);
 // learned per-pair orders (learn.cu)
 int fmm_mlp_nparam();

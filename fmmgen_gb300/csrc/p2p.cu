@@ -204,17 +204,17 @@ __device__ __forceinline__ void p2p_dipole(const float4 *sh, const float4 *sl, c
   }
 }
 
-template <bool POT>
-__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
+template <bool POT, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_p2p32(const int *leaf_cells, int nleaves, const int *pstart,
                                                           const int *pcount, const int *off_, const int *src,
                                                           const int *ix, const int *iy, const int *iz,
                                                           const unsigned char *clevel, const float2 *crf,
                                                           const float4 *phi4, const float4 *plo4,
                                                           const float4 *sdip, int so, double *Fnear) {
-  __shared__ float4 sh[P2P_WARPS][32], sl[P2P_WARPS][32], sd[P2P_WARPS][32];
+  __shared__ float4 sh[WARPS][32], sl[WARPS][32], sd[WARPS][32];
   const unsigned FULL = 0xffffffffu;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int leaf = blockIdx.x * P2P_WARPS + w;
+  const int leaf = blockIdx.x * WARPS + w;
   if (leaf >= nleaves) return;
   const int A = leaf_cells[leaf];
   const int a0 = pstart[A], na = pcount[A];
@@ -292,11 +292,16 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p32(const int *leaf_cells,
 // ---------------------------------------------------------------------------
 // launchers used by eval.cu
 // ---------------------------------------------------------------------------
-int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st) {
+int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st, bool narrow) {
   const int nl = t->nleaves, so = t->so;
   if (mixed) {
-    auto k = t->pass_potential || so ? k_p2p32<true> : k_p2p32<false>;
-    fmm_note_launch(), k<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
+    // narrow blocks (2 warps) when running beside the tensor-core M2L: three
+    // fit in the registers its CTA leaves free, against one of 4 warps
+    const bool pot = t->pass_potential || so;
+    const int wp = narrow ? 2 : P2P_WARPS;
+    auto k = narrow ? (pot ? k_p2p32<true, 2> : k_p2p32<false, 2>)
+                    : (pot ? k_p2p32<true, P2P_WARPS> : k_p2p32<false, P2P_WARPS>);
+    fmm_note_launch(), k<<<fmm_blocks(nl, wp), 32 * wp, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->ix.p, t->iy.p, t->iz.p,
         t->clevel.p, t->crf.p, t->phi4.p, t->plo4.p, t->sdip.p, so, t->Fnear.p);
   } else {

@@ -1051,6 +1051,11 @@ int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st) {
 void fmm_tree_destroy(DevTree *t) {
   if (!t) return;
   fmm_graph_release(t);
+  if (t->ev_fork) cudaEventDestroy(t->ev_fork);
+  if (t->ev_join) cudaEventDestroy(t->ev_join);
+  if (t->s_hi) cudaStreamDestroy(t->s_hi);
+  t->ev_fork = t->ev_join = nullptr;
+  t->s_hi = nullptr;
   if (t->gstream) cudaStreamDestroy(t->gstream);
   t->gstream = nullptr;
   fmm_release(t->keys); fmm_release(t->keys2); fmm_release(t->perm); fmm_release(t->perm2);

@@ -5,40 +5,43 @@
 //   implementation: tensor cores (p <= 9), generated CUDA-core kernels
 //                   (orders that have them), warp contraction engine;
 //   tensor-core pipeline depth: 2 .. the row-gather slots that fit in shared memory;
+//   tensor cores alone, or overlapped with the P2P (in 4- or 2-warp blocks);
 //   grouping of the cells into tiles / warps: by octant within the parent, or Morton.
-// One evaluation pass computes the multipoles; then the M2L phase alone is
-// timed `reps` times per candidate with CUDA events on the caller's stream and
-// the candidate with the lowest median is kept on the handle.
+// One evaluation pass computes the multipoles and stages the particles; then
+// the M2L and P2P phases alone are timed `reps` times per candidate with CUDA
+// events on the caller's stream and the candidate with the lowest median is
+// kept on the handle.
 #include <algorithm>
 #include <vector>
 #include "internal.h"
 
 #define TRY_(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
 
-int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand3, float *cand_ms,
+int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand4, float *cand_ms,
                  int *ncand, cudaStream_t st) {
   if (t->ord_mode != 0) return FMM_ERR_STATE;  // per-pair orders use their own kernel
   if (reps < 1) reps = 1;
   // the candidates
   struct Cand {
-    int impl, nslots, grouping;
+    int impl, nslots, grouping, overlap;
   };
   std::vector<Cand> cands;
   const int maxs = fmm_m2l_tc_max_slots(t->order, t->so);
   const bool gen = fmm_m2l_gen_supported(t->order, t->so);
   for (int g = 0; g < 2; g++) {
     if (precision != 0) {
-      for (int s = 2; s <= maxs; s++) cands.push_back({0, s, g});
-      if (gen) cands.push_back({1, 0, g});
+      for (int ov = 0; ov < 3; ov++)
+        for (int s = 2; s <= maxs; s++) cands.push_back({0, s, g, ov});
+      if (gen) cands.push_back({1, 0, g, 0});
     }
-    cands.push_back({2, 0, g});
+    cands.push_back({2, 0, g, 0});
   }
-  // one pass for the multipoles (potential only into a scratch output)
+  // one pass for the multipoles (the field into a scratch output)
   double *F = nullptr;
-  FMM_CUDA_TRY(cudaMalloc((void **)&F, sizeof(double) * (size_t)std::max(t->N, 1L)));
+  FMM_CUDA_TRY(cudaMalloc((void **)&F, sizeof(double) * 3 * (size_t)std::max(t->N, 1L)));
   const DevTree::M2LTune keep = t->tune;
   t->tune = DevTree::M2LTune();
-  int rc = fmm_tree_evaluate(t, S, F, 1, 0, precision, st);
+  int rc = fmm_tree_evaluate(t, S, F, 0, 1, precision, st);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = FMM_ERR_CUDA;
   int best = -1;
@@ -48,11 +51,12 @@ int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_c
     t->tune.impl = cands[c].impl;
     t->tune.nslots = cands[c].nslots;
     t->tune.grouping = cands[c].grouping;
-    rc = fmm_m2l_only(t, precision, st);  // warm-up (and the grouping's cell order)
+    t->tune.overlap = cands[c].overlap;
+    rc = fmm_m2l_p2p_only(t, S, precision, st);  // warm-up (and the grouping's cell order)
     std::vector<float> ms;
     for (int r = 0; r < reps && !rc; r++) {
       if (cudaEventRecord(e0, st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
-      rc = fmm_m2l_only(t, precision, st);
+      rc = fmm_m2l_p2p_only(t, S, precision, st);
       if (rc) break;
       float x = 0.f;
       if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
@@ -80,15 +84,17 @@ int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_c
   t->tune.impl = cands[best].impl;
   t->tune.nslots = cands[best].nslots;
   t->tune.grouping = cands[best].grouping;
+  t->tune.overlap = cands[best].overlap;
   fmm_graph_release(t);
   if (t->grouping_built != t->tune.grouping) TRY_(fmm_m2l_cell_order(t, t->tune.grouping, st));
   const int n = (int)cands.size();
   if (ncand) *ncand = n;
   for (int c = 0; c < std::min(n, max_cand); c++) {
-    if (cand3) {
-      cand3[3 * c] = cands[c].impl;
-      cand3[3 * c + 1] = cands[c].impl == 0 ? cands[c].nslots : 0;
-      cand3[3 * c + 2] = cands[c].grouping;
+    if (cand4) {
+      cand4[4 * c] = cands[c].impl;
+      cand4[4 * c + 1] = cands[c].impl == 0 ? cands[c].nslots : 0;
+      cand4[4 * c + 2] = cands[c].grouping;
+      cand4[4 * c + 3] = cands[c].overlap;
     }
     if (cand_ms) cand_ms[c] = med[c];
   }

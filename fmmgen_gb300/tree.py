@@ -163,32 +163,34 @@ class Tree:
     # -- M2L choices and the autotuner (no counterpart in the reference) -------
     M2L_IMPLS = {-1: "default", 0: "tensor cores", 1: "generated CUDA-core kernels", 2: "contraction engine"}
 
-    def set_tune(self, impl=-1, nslots=0, grouping=0):
+    def set_tune(self, impl=-1, nslots=0, grouping=0, overlap=0):
         """M2L implementation (-1 default rules, 0 tensor cores, 1 generated
         CUDA-core kernels, 2 contraction engine), tensor-core pipeline depth
-        (0: as deep as fits) and cell grouping (0 by octant, 1 Morton)."""
-        check(lib().fmmgen_tree_set_tune(self._h, int(impl), int(nslots), int(grouping)))
+        (0: as deep as fits), cell grouping (0 by octant, 1 Morton) and
+        overlap (1 / 2: tensor-core M2L and P2P side by side on the SMs, the
+        P2P in blocks of 4 / 2 warps)."""
+        check(lib().fmmgen_tree_set_tune(self._h, int(impl), int(nslots), int(grouping), int(overlap)))
         return self
 
     def get_tune(self):
-        v = np.zeros(3, np.int32)
+        v = np.zeros(4, np.int32)
         check(lib().fmmgen_tree_get_tune(self._h, v.ctypes.data))
-        return dict(impl=int(v[0]), nslots=int(v[1]), grouping=int(v[2]))
+        return dict(impl=int(v[0]), nslots=int(v[1]), grouping=int(v[2]), overlap=int(v[3]))
 
     def autotune(self, S=None, precision="mixed", reps=3, stream=None):
-        """Time the M2L phase for every supported (implementation, pipeline
-        depth, grouping) and keep the fastest on this handle; returns the
-        chosen setting and the table of median times (ms)."""
+        """Time the M2L + P2P phases for every supported (implementation,
+        pipeline depth, overlap, grouping) and keep the fastest on this handle;
+        returns the chosen setting and the table of median times (ms)."""
         if S is not None:
             self.S = _as_device(S, (sourcesize(self.source_order),))
         if self.S is None:
             raise ValueError("no sources")
-        cand = np.zeros((32, 3), np.int32)
-        ms = np.zeros(32, np.float32)
+        cand = np.zeros((64, 4), np.int32)
+        ms = np.zeros(64, np.float32)
         n = C.c_int(0)
-        check(lib().fmmgen_tree_autotune(self._h, C.c_void_p(self.S.data_ptr()), PRECISIONS[precision], int(reps), 32,
+        check(lib().fmmgen_tree_autotune(self._h, C.c_void_p(self.S.data_ptr()), PRECISIONS[precision], int(reps), 64,
                                          cand.ctypes.data, ms.ctypes.data, C.byref(n), _stream_ptr(stream)))
-        table = [dict(impl=int(c[0]), nslots=int(c[1]), grouping=int(c[2]), ms=float(m))
+        table = [dict(impl=int(c[0]), nslots=int(c[1]), grouping=int(c[2]), overlap=int(c[3]), ms=float(m))
                  for c, m in zip(cand[: n.value], ms[: n.value])]
         return dict(best=self.get_tune(), table=table)
 

@@ -186,15 +186,19 @@ int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3);
  * 2 contraction engine (mixed passes; FP64 passes always use the engine).
  * nslots: tensor-core pipeline depth (row-gather slots), 0 = as many as fit.
  * grouping: order of a level's cells in M2L tiles and warps, 0 by octant
- * within the parent, 1 Morton.  Unsupported choices are rejected. */
-int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping);
-int fmmgen_tree_get_tune(fmmgen_tree *tree, int *impl3);
-/* Autotuner: one pass over S at `precision` (for the multipoles), then the
- * M2L phase alone timed `reps` times per candidate (implementation x pipeline
- * depth x grouping that this order supports); the handle keeps the candidate
- * with the lowest median.  cand3 [max_cand][3] (impl, nslots, grouping) and
- * cand_ms [max_cand] receive the table (either may be NULL), *ncand its size. */
-int fmmgen_tree_autotune(fmmgen_tree *tree, const double *S, int precision, int reps, int max_cand, int *cand3,
+ * within the parent, 1 Morton.  overlap: 1 (2) runs the tensor-core M2L on a
+ * highest-priority side stream with the P2P beside it on the same SMs, in
+ * blocks of 4 (2) warps.
+ * Unsupported choices are rejected. */
+int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping, int overlap);
+int fmmgen_tree_get_tune(fmmgen_tree *tree, int *tune4);
+/* Autotuner: one pass over S at `precision` (for the multipoles and the staged
+ * particles), then the M2L and P2P phases alone timed `reps` times per
+ * candidate (implementation x pipeline depth x overlap x grouping that this
+ * order supports); the handle keeps the candidate with the lowest median.
+ * cand4 [max_cand][4] (impl, nslots, grouping, overlap) and cand_ms [max_cand]
+ * receive the table (either may be NULL), *ncand its size. */
+int fmmgen_tree_autotune(fmmgen_tree *tree, const double *S, int precision, int reps, int max_cand, int *cand4,
                          float *cand_ms, int *ncand, void *stream);
 
 /* ---- learned per-pair M2L orders (no counterpart in the reference, whose

@@ -32,11 +32,11 @@ def test_autotune_candidates(fg, p, so):
     assert (0 in impls) == (p <= 9)  # tensor cores where the order allows
     assert all(c["ms"] > 0 for c in table)
     best = min(table, key=lambda c: c["ms"])
-    assert r["best"] == {"impl": best["impl"], "nslots": best["nslots"], "grouping": best["grouping"]}
+    assert r["best"] == {k: best[k] for k in ("impl", "nslots", "grouping", "overlap")}
     F = t.compute_field_fmm(precision="mixed").cpu().numpy()
     assert rel(F, ref) < 2e-6
     for c in table:
-        t.set_tune(c["impl"], c["nslots"], c["grouping"])
+        t.set_tune(c["impl"], c["nslots"], c["grouping"], c["overlap"])
         assert rel(t.compute_field_fmm(precision="mixed").cpu().numpy(), ref) < 2e-6, c
 
 
@@ -62,7 +62,20 @@ def test_set_tune_rejects_unsupported(fg):
     with pytest.raises(fg.FMMError):
         t.set_tune(5)
     t.set_tune(2, 0, 1)
-    assert t.get_tune() == {"impl": 2, "nslots": 0, "grouping": 1}
+    assert t.get_tune() == {"impl": 2, "nslots": 0, "grouping": 1, "overlap": 0}
+
+
+def test_overlap_gives_the_same_fields(fg):
+    n = 80000
+    pos, S = system(14, n)
+    t = fg.build_tree(pos, S, n, 64, 8, 0.5)
+    t.set_tune(0, 0, 0, 0)
+    ref = t.compute_field_fmm(precision="mixed").cpu().numpy()
+    for ov in (1, 2, 1):
+        t.set_tune(0, 0, 0, ov)
+        assert np.array_equal(t.compute_field_fmm(precision="mixed").cpu().numpy(), ref)
+    b, e = t.times()
+    assert e["M2L"] > 0 and e["P2P"] >= 0
 
 
 def test_tune_under_graph_replay(fg):
@@ -70,9 +83,9 @@ def test_tune_under_graph_replay(fg):
     pos, S = system(13, n)
     t = fg.build_tree(pos, S, n, 64, 8, 0.5).set_graph(True)
     F = torch.empty((n, 4), dtype=torch.float64, device="cuda")
-    for impl, grouping in ((0, 0), (1, 1), (0, 1)):
-        t.set_tune(impl, 0, grouping)
-        ref = fg.build_tree(pos, S, n, 64, 8, 0.5).set_tune(impl, 0, grouping).compute_field_fmm(
+    for impl, grouping, ov in ((0, 0, 0), (1, 1, 0), (0, 1, 1), (0, 0, 2)):
+        t.set_tune(impl, 0, grouping, ov)
+        ref = fg.build_tree(pos, S, n, 64, 8, 0.5).set_tune(impl, 0, grouping, ov).compute_field_fmm(
             precision="mixed").cpu().numpy()
         for _ in range(2):
             t.compute_field_fmm(F, precision="mixed")
