@@ -104,6 +104,10 @@ struct DevTree {
   DevBuf<int> tc_mexp;                    // per cell: scale exponent of its multipole row
   DevBuf<uint32_t> d_tcerr;               // kernel timeout flags
   uint64_t build_serial = 0, tc_serial = ~0ull;  // tc_T belongs to the build with this serial
+  DevBuf<int> tc_sched_off;               // class-step schedule of the tensor-core M2L tiles
+  DevBuf<unsigned> tc_sched_cls, tc_sched_mask;
+  uint64_t sched_serial = ~0ull, sched_version = ~0ull;  // ... of this build and cell order
+  uint64_t order_version = 0;             // incremented whenever m2l_order is rewritten
   int tc_order = -1, tc_so = -1;          // ... and to this expansion order and source order
   DevBuf<unsigned char> wdec;             // decision of each frontier pair
   DevBuf<char> tmp;                       // scan / sort / misc scratch

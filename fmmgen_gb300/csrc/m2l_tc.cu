@@ -25,23 +25,30 @@
 //
 // Tiles take 128 cells of one level and one octant-within-parent, parents in
 // Morton order: those cells have near-identical interaction lists, so a tile
-// visits ~1.4x the classes of one list.
+// visits ~1.4x the classes of one list.  The class steps of every tile (the
+// sorted union of its rows' classes, and which rows have a source in each) are
+// computed once per build (k_tc_sched): the kernel's warps then follow that
+// schedule independently, coupled only through mbarriers.
 //
-// Per CTA (one per SM, persistent), 9 warps:
-//  * warps 0-7 gather the 128 source rows of each (class, 64-term K-block)
-//    step into a stage slot with cp.async, in the 128-byte swizzled K-major
-//    layout, and arrive on the slot's mbarrier when their copies land
+// Per CTA (one per SM, persistent), 13 warps:
+//  * warps 0-3 gather the source rows of each (class, 64-term K-block) step
+//    into a stage slot with cp.async, in the 128-byte swizzled K-major layout,
+//    and arrive on the slot's mbarrier when their copies land
 //    (cp.async.mbarrier.arrive); thread 0 also fetches the class's pre-split
-//    operator chunks (32-byte swizzled) with a bulk copy.  The same warps fold
-//    each finished class step out of tensor memory (warps w and w+4 take the
-//    two column halves of lane quarter w % 4) and store the tile's rows;
-//  * warp 8 allocates 512 tensor-memory columns (two accumulators) and one of
+//    operator chunks (32-byte swizzled) and column scales with bulk copies.  A
+//    row without a source in the class is not copied: its accumulator row
+//    holds garbage that the fold leaves out;
+//  * warps 4-11 fold each finished class step out of tensor memory (warps w
+//    and w+4 take the two column halves of lane quarter w % 4) and store the
+//    tile's rows;
+//  * warp 12 allocates 512 tensor-memory columns (two accumulators) and one of
 //    its lanes issues the MMAs.
 // Stage slots and accumulators circulate through mbarriers; every wait is
 // bounded and reports a timeout through an error flag instead of hanging.
 #include <algorithm>
 #include <cstddef>
 #include <cuda_fp16.h>
+#include <vector>
 #include "internal.h"
 
 namespace {
@@ -52,8 +59,12 @@ constexpr int TC_KB = 64;         // terms per K-block: one 128-byte swizzle row
 constexpr int TC_A_BYTES = TC_ROWS * 128;  // one operand half (hi or lo) of a K-block
 constexpr int TC_MAXCH = 16;      // K chunks (p <= 9: at most 14)
 constexpr int TC_MAXKB = 4;
-constexpr int TC_GATHER = 256;    // gather / epilogue threads (warps 0-7)
-constexpr int TC_THREADS = TC_GATHER + 32;
+constexpr int TC_GWARPS = 4;      // gather warps 0-3
+constexpr int TC_FWARPS = 8;      // fold warps 4-11
+constexpr int TC_MWARP = TC_GWARPS + TC_FWARPS;  // warp 12: tensor memory + MMA issue
+constexpr int TC_GATHER = 32 * TC_GWARPS;
+constexpr int TC_FOLD = 32 * TC_FWARPS;
+constexpr int TC_THREADS = 32 * (TC_MWARP + 1);
 constexpr int TC_MAXSLOTS = 4;
 constexpr int TC_ACC_COLS = 256;  // tensor-memory columns per accumulator
 constexpr int TC_EBIAS = 14;      // operands are scaled to [2^14, 2^15) in magnitude
@@ -64,6 +75,9 @@ struct TcParams {
   const int *order;               // cells in M2L processing order
   int ncells, ntiles;
   const int *off, *src, *cls;     // class-sorted M2L lists (CSR over targets)
+  const int *sched_off;           // [ntiles + 1] class steps of each tile
+  const unsigned *sched_cls;      // [steps] class of the step
+  const unsigned *sched_mask;     // [steps][4] rows (bit lane of word quarter) with a source in it
   const __half *Mh, *Ml;          // scaled, split source multipoles, row stride kpad
   const int *mexp;                // per cell: row scale exponent (M~ = 2^mexp (Mh + Ml))
   const unsigned char *T;         // per class: split, swizzled operator chunks, then column scales
@@ -168,6 +182,19 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
   for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 16 consecutive accumulator columns in one load-and-wait statement
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
 // x = 2^e (hi + lo) with hi, lo FP16 and |x 2^-e| in [2^14, 2^15) for the
 // largest |x| of its row or column (e from that maximum)
 __device__ __forceinline__ int scale_exp(float amax) {
@@ -188,18 +215,16 @@ namespace {
 struct TcShared {
   alignas(16) float colf[2][TC_ACC_COLS];  // column scales 2^g of the class in each accumulator (bulk-copy
                                            // destination: 16-byte aligned)
-  uint64_t full[TC_MAXSLOTS];   // slot filled: 256 cp.async arrivals + thread 0's expect_tx arrival
+  uint64_t full[TC_MAXSLOTS];   // slot filled: 128 cp.async arrivals + thread 0's expect_tx arrival
   uint64_t empty[TC_MAXSLOTS];  // slot consumed: MMA commit
   uint64_t accfull[2];          // class step accumulated: MMA commit
-  uint64_t accempty[2];         // accumulator folded out: 256 epilogue arrivals
+  uint64_t accempty[2];         // accumulator folded out: 256 fold arrivals
   uint64_t colfull[2];          // column scales of the class in each accumulator landed (bulk copy)
   uint64_t drain;               // every MMA complete (before tensor memory is released)
   int hdr[TC_MAXSLOTS];         // K-block of the slot's step; -1: end of work
   uint32_t ch_idesc[TC_MAXCH];  // per K chunk: instruction descriptor (N of the chunk)
   uint32_t ch_boff[TC_MAXCH];   // per K chunk: offset of its hi block in the slot's operator area, >> 4
   uint32_t ch_nlo[TC_MAXCH];    // per K chunk: offset of its lo block from its hi block, >> 4
-  unsigned smin[2][8];          // per-warp partial minima (double-buffered)
-  uint32_t wok[2];              // outcome of a wait thread 0 did for the gather group
   uint32_t tmem;                // tensor-memory base address
 };
 
@@ -208,54 +233,43 @@ struct TcShared {
 static_assert(offsetof(TcShared, colf) % 16 == 0 && sizeof(TcShared::colf[0]) % 16 == 0, "colf alignment");
 static_assert(offsetof(TcShared, full) % 8 == 0 && offsetof(TcShared, drain) % 8 == 0, "mbarrier alignment");
 
-__device__ __forceinline__ void gather_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
-// minimum over the 256 gather threads
-__device__ __forceinline__ unsigned gather_min(unsigned v, TcShared *cs, uint32_t &par) {
-  v = __reduce_min_sync(0xffffffffu, v);
-  unsigned *b = cs->smin[par & 1];
-  par++;
-  if ((threadIdx.x & 31) == 0) b[threadIdx.x >> 5] = v;
-  gather_bar();
-  unsigned m = b[0];
-#pragma unroll
-  for (int i = 1; i < 8; i++) m = min(m, b[i]);
-  return m;
-}
-
-// Thread 0 waits on the mbarrier; the outcome reaches the whole gather group
-// through the named barrier, so every gather thread takes the same branch.
-__device__ __forceinline__ bool gather_wait(uint32_t bar, uint32_t parity, TcShared *cs, uint32_t &par) {
-  uint32_t *w = &cs->wok[par & 1];
-  par++;
-  if (threadIdx.x == 0) *w = mbar_wait(bar, parity) ? 1u : 0u;
-  gather_bar();
-  return *w != 0;
+// Bounded wait of a whole warp: lane 0 waits, the outcome reaches every lane.
+__device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok = 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity) ? 1u : 0u;
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
 // Add class step v's accumulator (this thread's lane, HALF columns from col0),
 // times its row scale 2^e and the class's column scales, into the FP32 running
-// sums, and hand the accumulator back to the MMA issuer.
+// sums -- rows with a source in the step only -- and hand the accumulator back
+// to the MMA issuer.
 template <int HALF>
-__device__ __forceinline__ bool fold(float *acc, uint32_t tlane, int col0, uint32_t v, int e, uint32_t accfull0,
-                                     uint32_t accempty0, uint32_t colfull0, TcShared *cs, uint32_t &wpar) {
+__device__ __forceinline__ bool fold(float *acc, uint32_t tlane, int col0, uint32_t v, int e, bool mine,
+                                     uint32_t accfull0, uint32_t accempty0, uint32_t colfull0, TcShared *cs) {
   const uint32_t b = v & 1;
-  uint32_t *w = &cs->wok[wpar & 1];
-  wpar++;
-  if (threadIdx.x == 0)
-    *w = mbar_wait(colfull0 + 8 * b, (v >> 1) & 1) && mbar_wait(accfull0 + 8 * b, (v >> 1) & 1) ? 1u : 0u;
-  gather_bar();
-  if (!*w) return false;
+  if (!warp_wait(colfull0 + 8 * b, (v >> 1) & 1) || !warp_wait(accfull0 + 8 * b, (v >> 1) & 1)) return false;
   tc_fence_after();
   __syncwarp();  // tcgen05.ld is warp-collective
   const float rowf = ldexpf(1.f, e);
   const float *cf = cs->colf[b] + col0;
+  // columns in loads of 16, then 8 (one wait each)
+  constexpr int N16 = HALF / 16, N8 = (HALF % 16) / 8;
 #pragma unroll
-  for (int c0 = 0; c0 < HALF; c0 += 8) {
+  for (int j = 0; j < N16; j++) {
+    float t[16];
+    tmem_ld16(tlane + b * TC_ACC_COLS + 16 * j, t);  // warp-collective: every lane loads
+    if (mine)  // a row without a source in the step holds garbage: left out
+#pragma unroll
+      for (int i = 0; i < 16; i++) acc[16 * j + i] = fmaf(t[i], rowf * cf[16 * j + i], acc[16 * j + i]);
+  }
+  if (N8) {
+    constexpr int c0 = 16 * N16;
     float t[8];
     tmem_ld8(tlane + b * TC_ACC_COLS + c0, t);
+    if (mine)
 #pragma unroll
-    for (int i = 0; i < 8; i++) acc[c0 + i] = fmaf(t[i], rowf * cf[c0 + i], acc[c0 + i]);
+      for (int i = 0; i < 8; i++) acc[c0 + i] = fmaf(t[i], rowf * cf[c0 + i], acc[c0 + i]);
   }
   tc_fence_before();
   mbar_arrive(accempty0 + 8 * b);
@@ -282,18 +296,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
   }
   if (tid == 0) {
     for (int i = 0; i < P.nslots; i++) {
-      mbar_init(full0 + 8 * i, TC_GATHER + 1);
+      mbar_init(full0 + 8 * i, TC_GATHER + 1);  // every gather thread + thread 0's expect_tx
       mbar_init(empty0 + 8 * i, 1);
     }
     for (int i = 0; i < 2; i++) {
       mbar_init(accfull0 + 8 * i, 1);
-      mbar_init(accempty0 + 8 * i, TC_GATHER);
+      mbar_init(accempty0 + 8 * i, TC_FOLD);
       mbar_init(colfull0 + 8 * i, 1);
     }
     mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 8) {
+  if (warp == TC_MWARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&cs->tmem)),
                  "r"(2 * TC_ACC_COLS)
                  : "memory");
@@ -304,12 +318,96 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
   tc_fence_after();
   const uint32_t tmem = cs->tmem;
 
-  if (warp < 8) {
-    // ---------------- gather + fold + store ----------------
-    const int quarter = warp & 3, half = warp >> 2;
+  if (warp < TC_GWARPS) {
+    // ---------------- gather ----------------
+    const int quarter = warp;
     const int row = 32 * quarter + lane;  // tile row whose list this thread walks
+    uint32_t g = 0, u = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < P.ntiles && ok; tile += gridDim.x) {
+      const int rr = tile * TC_ROWS + row;
+      const int A = rr < P.ncells ? P.order[rr] : -1;
+      int k = 0, kend = 0;
+      if (A >= 0) {
+        k = P.off[A];
+        kend = P.off[A + 1];
+      }
+      // the row's next source, loaded a step before it is needed
+      int hsrc = k < kend ? P.src[k] : 0;
+      const int s1 = P.sched_off[tile + 1];
+      for (int st = P.sched_off[tile]; st < s1; st++, u++) {
+        const unsigned c = P.sched_cls[st];
+        const bool mine = (P.sched_mask[4 * st + quarter] >> lane) & 1u;
+        const int mysrc = mine ? hsrc : -1;
+        if (mine) {
+          k++;
+          hsrc = k < kend ? P.src[k] : 0;
+        }
+        for (int kb = 0; kb < P.nkb; kb++) {
+          const int slot = (int)(g % (uint32_t)P.nslots);
+          const uint32_t use = g / (uint32_t)P.nslots;
+          if (!warp_wait(empty0 + 8 * slot, (use & 1) ^ 1)) { ok = false; break; }
+          const uint32_t sa = base + (uint32_t)slot * P.slot_bytes;
+          const int qn = min(8, (P.kpad - TC_KB * kb) >> 3);  // valid 16-byte chunks of the K-block
+#pragma unroll
+          for (int jj = 0; jj < 8; jj++) {
+            const int rl = 4 * jj + (lane >> 3), q = lane & 7;  // 4 rows x 8 chunks per instruction
+            const int r = 32 * quarter + rl;
+            const int sr = __shfl_sync(0xffffffffu, mysrc, rl);
+            if (sr >= 0 && q < qn) {
+              const size_t e = (size_t)sr * P.kpad + TC_KB * kb + 8 * q;
+              const uint32_t o = (uint32_t)r * 128u + ((uint32_t)(q ^ (r & 7)) << 4);
+              cp16(sa + o, P.Mh + e, 16u);
+              cp16(sa + TC_A_BYTES + o, P.Ml + e, 16u);
+            }
+          }
+          if (tid == 0) {
+            cs->hdr[slot] = kb;
+            const unsigned char *rec = P.T + (size_t)c * P.cls_bytes;
+            const uint32_t b0 = P.choff[4 * kb], b1 = P.choff[min(4 * kb + 4, P.kch)];
+            mbar_arrive_tx(full0 + 8 * slot, b1 - b0);
+            bulk_g2s(sa + 2 * TC_A_BYTES, rec + b0, b1 - b0, full0 + 8 * slot);
+            if (kb == 0) {
+              // the class's column scales, for the fold of this step, into
+              // buffer u & 1 once the fold of step u - 2 has read it
+              const uint32_t cb = colfull0 + 8 * (u & 1), sc = 4u * (uint32_t)P.nout;
+              if (!mbar_wait(accempty0 + 8 * (u & 1), ((u >> 1) & 1) ^ 1)) ok = false;
+              fence_async_smem();
+              mbar_arrive_tx(cb, sc);
+              bulk_g2s(su32(cs->colf[u & 1]), rec + P.cls_scale, sc, cb);
+            }
+          }
+          cp_arrive(full0 + 8 * slot);
+          g++;
+        }
+        if (!__all_sync(0xffffffffu, ok)) ok = false;
+        if (!ok) break;
+      }
+    }
+    // end of work: one more slot carrying only the end mark
+    if (ok) {
+      const int slot = (int)(g % (uint32_t)P.nslots);
+      const uint32_t use = g / (uint32_t)P.nslots;
+      if (warp_wait(empty0 + 8 * slot, (use & 1) ^ 1)) {
+        if (tid == 0) {
+          cs->hdr[slot] = -1;
+          mbar_arrive(full0 + 8 * slot);
+        }
+        mbar_arrive(full0 + 8 * slot);
+      } else {
+        ok = false;
+      }
+    }
+    cp_wait_all();
+    if (!ok && lane == 0) atomicOr(P.err, 1u);
+    if (tid == 0) atomicAdd((unsigned long long *)(P.err + 2), (unsigned long long)u);
+  } else if (warp < TC_MWARP) {
+    // ---------------- fold + store ----------------
+    const int fw = warp - TC_GWARPS;
+    const int quarter = warp & 3, half = fw >> 2;  // tensor-memory lanes 32 (warp % 4) .. + 31
+    const int row = 32 * quarter + lane;
     const uint32_t tlane = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(half * HALF);
-    uint32_t g = 0, u = 0, par = 0, wpar = 0;
+    uint32_t u = 0;
     bool ok = true;
     float acc[HALF];
     for (int tile = blockIdx.x; tile < P.ntiles && ok; tile += gridDim.x) {
@@ -322,111 +420,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
         k = P.off[A];
         kend = P.off[A + 1];
       }
-      // the current list entry and the next one, loaded a class step before
-      // they are needed so that no global-load latency sits in the step loop
-      unsigned head = k < kend ? (unsigned)P.cls[k] : TC_NONE;
       int hsrc = k < kend ? P.src[k] : 0;
-      unsigned nhead = k + 1 < kend ? (unsigned)P.cls[k + 1] : TC_NONE;
-      int nsrc = k + 1 < kend ? P.src[k + 1] : 0;
-      unsigned c = gather_min(head, cs, par);
-      int e_last = 0;  // row scale exponent of the step issued last
-      if (c == TC_NONE) {  // no M2L into this tile
-        if (Lrow)
-          for (int i = 0; i < ncol; i++) Lrow[i] = 0.f;
-        continue;
-      }
 #pragma unroll
       for (int i = 0; i < HALF; i++) acc[i] = 0.f;
-      uint32_t steps = 0;
-      while (true) {
-        const bool mine = head == c;
-        const int mysrc = mine ? hsrc : -1;
-        const int e_this = mine ? P.mexp[hsrc] : 0;  // first used by the fold one step later
+      const int s1 = P.sched_off[tile + 1];
+      for (int st = P.sched_off[tile]; st < s1; st++, u++) {
+        const bool mine = (P.sched_mask[4 * st + quarter] >> lane) & 1u;
+        const int e = mine ? P.mexp[hsrc] : 0;
         if (mine) {
-          head = nhead;
-          hsrc = nsrc;
           k++;
-          nhead = k + 1 < kend ? (unsigned)P.cls[k + 1] : TC_NONE;
-          nsrc = k + 1 < kend ? P.src[k + 1] : 0;
+          hsrc = k < kend ? P.src[k] : 0;
         }
-        const unsigned cnext = gather_min(head, cs, par);
-        for (int kb = 0; kb < P.nkb; kb++) {
-          const int slot = (int)(g % (uint32_t)P.nslots);
-          const uint32_t use = g / (uint32_t)P.nslots;
-          if (!gather_wait(empty0 + 8 * slot, (use & 1) ^ 1, cs, wpar)) { ok = false; break; }
-          const uint32_t sa = base + (uint32_t)slot * P.slot_bytes;
-          const int qn = min(8, (P.kpad - TC_KB * kb) >> 3);  // valid 16-byte chunks of the K-block
-#pragma unroll
-          for (int jj = 0; jj < 4; jj++) {
-            const int rl = 16 * half + 4 * jj + (lane >> 3), q = lane & 7;
-            const int r = 32 * quarter + rl;
-            const int s = __shfl_sync(0xffffffffu, mysrc, rl);
-            if (q < qn) {
-              const size_t e = (size_t)(s < 0 ? 0 : s) * P.kpad + TC_KB * kb + 8 * q;
-              const uint32_t o = (uint32_t)r * 128u + ((uint32_t)(q ^ (r & 7)) << 4);
-              const uint32_t nb = s < 0 ? 0u : 16u;  // zero fill: no source of this class
-              cp16(sa + o, P.Mh + e, nb);
-              cp16(sa + TC_A_BYTES + o, P.Ml + e, nb);
-            }
-          }
-          if (tid == 0) {
-            cs->hdr[slot] = kb;
-            const unsigned char *rec = P.T + (size_t)c * P.cls_bytes;
-            const uint32_t b0 = P.choff[4 * kb], b1 = P.choff[min(4 * kb + 4, P.kch)];
-            mbar_arrive_tx(full0 + 8 * slot, b1 - b0);
-            bulk_g2s(sa + 2 * TC_A_BYTES, rec + b0, b1 - b0, full0 + 8 * slot);
-            if (kb == 0) {  // the class's column scales, for the fold of this step
-              const uint32_t sc = 4u * (uint32_t)P.nout, cb = colfull0 + 8 * (u & 1);
-              fence_async_smem();  // the folds' reads of this buffer precede its overwrite
-              mbar_arrive_tx(cb, sc);
-              bulk_g2s(su32(cs->colf[u & 1]), rec + P.cls_scale, sc, cb);
-            }
-          }
-          cp_arrive(full0 + 8 * slot);
-          g++;
-        }
-        if (!ok) break;
-        // fold the previous class step while the MMAs of this one run
-        if (steps > 0 &&
-            !fold<HALF>(acc, tlane, half * HALF, u - 1, e_last, accfull0, accempty0, colfull0, cs, wpar)) {
+        if (!fold<HALF>(acc, tlane, half * HALF, u, e, mine, accfull0, accempty0, colfull0, cs)) {
           ok = false;
           break;
         }
-        e_last = e_this;
-        steps++;
-        u++;
-        if (cnext == TC_NONE) break;
-        c = cnext;
       }
       if (!ok) break;
-      if (!fold<HALF>(acc, tlane, half * HALF, u - 1, e_last, accfull0, accempty0, colfull0, cs, wpar)) {
-        ok = false;
-        break;
-      }
       if (Lrow)
 #pragma unroll
         for (int i = 0; i < HALF; i++)
           if (i < ncol) Lrow[i] = acc[i];
     }
-    // end of work: one more slot carrying only the end mark
-    if (ok) {
-      const int slot = (int)(g % (uint32_t)P.nslots);
-      const uint32_t use = g / (uint32_t)P.nslots;
-      if (gather_wait(empty0 + 8 * slot, (use & 1) ^ 1, cs, wpar)) {
-        if (tid == 0) {
-          cs->hdr[slot] = -1;
-          mbar_arrive(full0 + 8 * slot);
-        }
-        mbar_arrive(full0 + 8 * slot);
-      } else {
-        ok = false;
-      }
-    }
-    cp_wait_all();
-    if (!ok && tid == 0) atomicOr(P.err, 1u);
-    if (tid == 0) atomicAdd((unsigned long long *)(P.err + 2), (unsigned long long)u);
+    if (!ok && lane == 0) atomicOr(P.err, 1u);
   } else if (lane == 0) {
-    // ---------------- MMA issue (one thread) ----------------
+    // ---------------- MMA issue (one thread of warp 12) ----------------
     // Per-chunk instruction descriptors and operator offsets live in
     // registers (compile-time indices below), so nothing but descriptor
     // arithmetic sits between consecutive MMAs.
@@ -495,7 +513,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
   __syncwarp();
   tc_fence_before();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == TC_MWARP) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_ACC_COLS)
                  : "memory");
@@ -594,6 +612,42 @@ __global__ void k_tc_operators(const double *D64, const int *key4, int ncls, TcP
   }
 }
 
+// Class steps of every tile (one block of 128 threads per tile, thread = row):
+// the sorted union of the rows' class-sorted lists.  Counting pass (cls_out
+// null): count[tile] = steps; writing pass: the class of each step and, per
+// warp quarter of the tile, the rows with a source in it.
+__global__ void __launch_bounds__(TC_ROWS) k_tc_sched(const int *order, int ncells, const int *off, const int *cls,
+                                                      int *count, const int *sched_off, unsigned *cls_out,
+                                                      unsigned *mask_out) {
+  __shared__ unsigned wmin[TC_ROWS / 32];
+  const int tile = blockIdx.x, r = threadIdx.x, w = r >> 5, lane = r & 31;
+  const int rr = tile * TC_ROWS + r;
+  const int A = rr < ncells ? order[rr] : -1;
+  int k = A >= 0 ? off[A] : 0;
+  const int kend = A >= 0 ? off[A + 1] : 0;
+  int st = cls_out ? sched_off[tile] : 0, n = 0;
+  while (true) {
+    const unsigned h = k < kend ? (unsigned)cls[k] : TC_NONE;
+    const unsigned m = __reduce_min_sync(0xffffffffu, h);
+    if (lane == 0) wmin[w] = m;
+    __syncthreads();
+    unsigned c = wmin[0];
+#pragma unroll
+    for (int i = 1; i < TC_ROWS / 32; i++) c = min(c, wmin[i]);
+    __syncthreads();  // wmin is rewritten next round
+    if (c == TC_NONE) break;
+    const unsigned bal = __ballot_sync(0xffffffffu, h == c);
+    if (cls_out) {
+      if (r == 0) cls_out[st] = c;
+      if (lane == 0) mask_out[4 * st + w] = bal;
+    }
+    st++;
+    n++;
+    if (h == c) k++;
+  }
+  if (!cls_out && r == 0) count[tile] = n;
+}
+
 // Source multipoles as 2^e (hi + lo), hi and lo FP16 rows of kpad terms, e per
 // cell from the row's largest magnitude (one warp per cell).
 __global__ void k_tc_split(const float *M, int ncells, int mstr, int msize, int kpad, __half *Mh, __half *Ml,
@@ -667,6 +721,32 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
     FMM_CUDA_TRY(cudaMemset2DAsync(L, sizeof(float) * lstr, 0, sizeof(float) * pl.lsize, nc, st));
     return FMM_OK;
   }
+  // class-step schedule of the tiles: once per build and cell order
+  const int ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
+  if (t->sched_serial != t->build_serial || t->sched_version != t->order_version) {
+    if (fmm_reserve(t->tc_sched_off, ntiles + 1)) return FMM_ERR_CUDA;
+    int *cnt = t->tc_sched_off.p + 1;
+    fmm_note_launch(), k_tc_sched<<<ntiles, TC_ROWS, 0, st>>>(t->m2l_order.p, nc, t->m2l_off.p, t->m2l_cls.p, cnt,
+                                                             nullptr, nullptr, nullptr);
+    FMM_CUDA_TRY(cudaGetLastError());
+    std::vector<int> h(ntiles + 1);
+    FMM_CUDA_TRY(cudaMemcpyAsync(h.data() + 1, cnt, sizeof(int) * ntiles, cudaMemcpyDeviceToHost, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    h[0] = 0;
+    for (int i = 0; i < ntiles; i++) h[i + 1] += h[i];
+    const int nsteps = h[ntiles];
+    FMM_CUDA_TRY(cudaMemcpyAsync(t->tc_sched_off.p, h.data(), sizeof(int) * (ntiles + 1), cudaMemcpyHostToDevice, st));
+    if (fmm_reserve(t->tc_sched_cls, nsteps > 0 ? nsteps : 1) ||
+        fmm_reserve(t->tc_sched_mask, 4 * (size_t)(nsteps > 0 ? nsteps : 1)))
+      return FMM_ERR_CUDA;
+    fmm_note_launch(), k_tc_sched<<<ntiles, TC_ROWS, 0, st>>>(t->m2l_order.p, nc, t->m2l_off.p, t->m2l_cls.p,
+                                                             nullptr, t->tc_sched_off.p, t->tc_sched_cls.p,
+                                                             t->tc_sched_mask.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));  // h is read by the copy above
+    t->sched_serial = t->build_serial;
+    t->sched_version = t->order_version;
+  }
   // operator records: once per build
   if (t->tc_serial != t->build_serial) {
     const size_t bytes = (size_t)t->nclasses * pl.cls_bytes;
@@ -693,10 +773,13 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   TcParams P;
   P.order = t->m2l_order.p;
   P.ncells = nc;
-  P.ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
+  P.ntiles = ntiles;
   P.off = t->m2l_off.p;
   P.src = t->m2l_src.p;
   P.cls = t->m2l_cls.p;
+  P.sched_off = t->tc_sched_off.p;
+  P.sched_cls = t->tc_sched_cls.p;
+  P.sched_mask = t->tc_sched_mask.p;
   P.Mh = (const __half *)t->tc_Mh.p;
   P.Ml = (const __half *)t->tc_Ml.p;
   P.mexp = t->tc_mexp.p;

@@ -1045,6 +1045,7 @@ int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st) {
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(fmm_radix_sort<uint64_t>(k1, (uint32_t *)t->m2l_order.p, k2, v2, nc, 48, 64, hist, stmp2, st));
   t->grouping_built = grouping;
+  t->order_version++;
   return FMM_OK;
 }
 
@@ -1077,6 +1078,8 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->p2p_tgt_raw); fmm_release(t->p2p_src_raw);
   fmm_release(t->tc_T); fmm_release(t->tc_Mh); fmm_release(t->tc_Ml); fmm_release(t->tc_mexp);
   fmm_release(t->d_tcerr);
+  fmm_release(t->tc_sched_off); fmm_release(t->tc_sched_cls); fmm_release(t->tc_sched_mask);
+  t->sched_serial = ~0ull;
   t->tc_serial = ~0ull;
   fmm_release(t->wdec);
   fmm_release(t->m2l_ord); fmm_release(t->mnorm); fmm_release(t->feat); fmm_release(t->tscale); fmm_release(t->tpart);
