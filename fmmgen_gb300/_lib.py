@@ -53,6 +53,7 @@ _SIGS = {
                                       C.POINTER(C.c_void_p)]),
     "fmmgen_tree_compute_field_fmm": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_gpu_direct": (C.c_int, [_dp, _dp, C.c_long, _lp, C.c_long, C.c_int, C.c_int, C.c_int, _dp, _vp]),
+    "fmmgen_tree_compute_field_bh": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_int, _vp]),
     "fmmgen_tree_free": (C.c_int, [_vp]),
     "fmmgen_root_box_noalloc": (C.c_int, [_dp, C.c_long, _dp, _vp]),
     "fmmgen_tree_info": (C.c_int, [_vp, _lp]),

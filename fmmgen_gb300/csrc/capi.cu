@@ -202,6 +202,13 @@ int fmmgen_tree_compute_field_fmm(fmmgen_tree *tree, const double *Sv, double *F
   return ret(rc);
 }
 
+int fmmgen_tree_compute_field_bh(fmmgen_tree *tree, const double *Sv, double *F, int potential, int field,
+                                  void *st) {
+  g_err.clear();
+  if (!tree || !tree->built) return ret(FMM_ERR_STATE);
+  return ret(fmm_tree_evaluate_bh(&tree->t, Sv, F, potential, field, S(st)));
+}
+
 int fmmgen_gpu_direct(const double *pos, const double *Sv, long N, const long *targets, long ntargets, int so,
                       int potential, int field, double *F, void *stream) {
   g_err.clear();

@@ -639,6 +639,195 @@ int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st
   return m2l_p2p<double>(t, ps, S, t->M.p, t->L.p, false, impl, msize, lsize, fmm_nterms(p), st);
 }
 
+// ---------------------------------------------------------------------------
+// Barnes-Hut (Tree::compute_field_bh, example/tree.cpp:273-293)
+// ---------------------------------------------------------------------------
+// D[idx(n)] = d^n (1/|y|) at y, |n| <= q, in one thread, degree by degree:
+//   |n| |y|^2 D_n = -(2|n| - 1) sum_a n_a y_a D_(n - e_a) - (|n| - 1) sum_a n_a (n_a - 1) D_(n - 2 e_a)
+__device__ __forceinline__ void thread_derivs(double yx, double yy, double yz, int q, double *D) {
+  const double ir2 = 1.0 / (yx * yx + yy * yy + yz * yz);
+  D[0] = sqrt(ir2);
+  int i = 1;
+  for (int d = 1; d <= q; d++) {
+    const double rd = 1.0 / d, a1 = -(2 * d - 1) * ir2 * rd, a2 = -(d - 1) * ir2 * rd;
+    for (int nx = d; nx >= 0; nx--)
+      for (int ny = d - nx; ny >= 0; ny--, i++) {
+        const int nz = d - nx - ny;
+        double s1 = 0, s2 = 0;
+        if (nx) {
+          s1 += nx * yx * D[fmm_idx3(nx - 1, ny, nz)];
+          if (nx > 1) s2 += nx * (nx - 1) * D[fmm_idx3(nx - 2, ny, nz)];
+        }
+        if (ny) {
+          s1 += ny * yy * D[fmm_idx3(nx, ny - 1, nz)];
+          if (ny > 1) s2 += ny * (ny - 1) * D[fmm_idx3(nx, ny - 2, nz)];
+        }
+        if (nz) {
+          s1 += nz * yz * D[fmm_idx3(nx, ny, nz - 1)];
+          if (nz > 1) s2 += nz * (nz - 1) * D[fmm_idx3(nx, ny, nz - 2)];
+        }
+        D[i] = a1 * s1 + a2 * s2;
+      }
+  }
+}
+
+// One thread per particle (sorted order), FP64: evaluate_M2P_and_P2P
+// (example/calculate.cpp:266-314) from the particle's root with an explicit
+// stack.  A child c of an open cell is opened when r_c > theta |x_i - c_c|,
+// else its multipole acts through M2P -- the potential of fmmgen's M2P
+// (fmmgen/generator.py:174-206) and its exact gradient as the field,
+//   phi = (1/s) sum_m D_m(y) M~_m,  E = -(1/s^2) sum_m D_(m+e)(y) M~_m,  y = (x_i - c_c) / s,
+// in the scaled multipoles M~ = M / s^|m| -- and a leaf's particles through
+// P2P.  NTQ holds the derivatives to order p + 1.
+#define BH_THREADS 128
+#define BH_STACK (8 * 22)
+template <int NTQ>
+__global__ void __launch_bounds__(BH_THREADS) k_bh64(long N, int nsys, const long *sys_off, const double *px,
+                                                     const double *py, const double *pz, const uint32_t *perm,
+                                                     const double *S, int so, int p, double theta,
+                                                     const double *cx, const double *cy, const double *cz,
+                                                     const double *cr, const int *child_first,
+                                                     const unsigned char *child_mask, const int *pstart,
+                                                     const int *pcount, const double *M, int msize, int potential,
+                                                     int field, double *F, uint32_t *eflag) {
+  const long i = blockIdx.x * (long)BH_THREADS + threadIdx.x;
+  if (i >= N) return;
+  int root = 0;
+  if (nsys > 1) {  // the system holding sorted particle i: sys_off[s] <= i < sys_off[s + 1]
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sys_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    root = lo;
+  }
+  const double xi = px[i], yi = py[i], zi = pz[i];
+  const int moff = fmm_nterms(so - 1);
+  double phi = 0, ex = 0, ey = 0, ez = 0;
+  double D[NTQ];
+  int stack[BH_STACK];
+  int sp = 0;
+  stack[sp++] = root;
+  while (sp > 0) {
+    const int c0 = stack[--sp];
+    const unsigned mask = child_mask[c0];
+    if (mask) {
+      int c = child_first[c0];
+      for (int o = 0; o < 8; o++) {
+        if (!((mask >> o) & 1u)) continue;
+        const double dx = xi - cx[c], dy = yi - cy[c], dz = zi - cz[c];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double s = cr[c];
+        if (s > theta * r) {
+          if (sp < BH_STACK) stack[sp++] = c;
+          else atomicOr(eflag, 1u);  // deeper than the stack: reported, not walked
+        } else {
+          const double is = 1.0 / s;
+          thread_derivs(dx * is, dy * is, dz * is, p + 1, D);
+          const double *Mc = M + (size_t)c * msize;
+          double v = 0, gx = 0, gy = 0, gz = 0;
+          int j = moff;  // multipole terms in the degree-major layout
+          for (int d = so; d <= p; d++)
+            for (int mx = d; mx >= 0; mx--)
+              for (int my = d - mx; my >= 0; my--, j++) {
+                const int mz = d - mx - my;
+                const double w = Mc[j - moff];
+                v += D[j] * w;
+                gx += D[fmm_idx3(mx + 1, my, mz)] * w;
+                gy += D[fmm_idx3(mx, my + 1, mz)] * w;
+                gz += D[fmm_idx3(mx, my, mz + 1)] * w;
+              }
+          phi += v * is;
+          const double is2 = is * is;
+          ex -= gx * is2;
+          ey -= gy * is2;
+          ez -= gz * is2;
+        }
+        c++;
+      }
+    } else {
+      const int j0 = pstart[c0], j1 = j0 + pcount[c0];
+      for (int j = j0; j < j1; j++) {
+        if (j == i) continue;
+        const double dx = xi - px[j], dy = yi - py[j], dz = zi - pz[j];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        const double rinv = 1.0 / sqrt(r2), r3 = rinv * rinv * rinv;
+        const uint32_t oj = perm[j];
+        if (so == 0) {
+          const double q = S[oj];
+          phi += q * rinv;
+          ex += q * r3 * dx;
+          ey += q * r3 * dy;
+          ez += q * r3 * dz;
+        } else {
+          const double sx = S[3 * (size_t)oj], sy = S[3 * (size_t)oj + 1], sz = S[3 * (size_t)oj + 2];
+          const double sr = sx * dx + sy * dy + sz * dz;
+          const double r5 = 3.0 * sr * r3 * rinv * rinv;
+          phi -= sr * r3;
+          ex += sx * r3 - r5 * dx;
+          ey += sy * r3 - r5 * dy;
+          ez += sz * r3 - r5 * dz;
+        }
+      }
+    }
+  }
+  const int outsize = (potential ? 1 : 0) + (field ? 3 : 0);
+  double *f = F + (size_t)perm[i] * outsize;
+  int k = 0;
+  if (potential) f[k++] = phi;
+  if (field) {
+    f[k] = ex;
+    f[k + 1] = ey;
+    f[k + 2] = ez;
+  }
+}
+
+// Tree::compute_field_bh (example/tree.cpp:273-293): FP64 P2M and M2M, then
+// the walk of every particle.
+int fmm_tree_evaluate_bh(DevTree *t, const double *S, double *F, int potential, int field, cudaStream_t st) {
+  if (!t || t->ncells == 0) return FMM_ERR_STATE;
+  if (!S || !F || (!potential && !field)) return FMM_ERR_ARG;
+  const PlanSet *ps = fmm_get_plans(t->order, t->so);
+  if (!ps) return FMM_ERR_CUDA;
+  const int p = t->order, so = t->so;
+  const int msize = fmm_nterms(p) - fmm_nterms(so - 1);
+  const double *cr = t->cr.p;
+  TRY(fmm_reserve(t->M, (size_t)t->ncells * msize));
+  TRY(fmm_reserve(t->d_eflags, 1));
+  FMM_CUDA_TRY(cudaMemsetAsync(t->d_eflags.p, 0, sizeof(uint32_t), st));
+  fmm_note_launch(), k_p2m<double><<<fmm_blocks(t->nleaves, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+      t->leaf_cells.p, t->nleaves, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p,
+      t->py.p, t->pz.p, t->perm.p, S, so, p, cr, t->M.p, msize);
+  for (int l = t->nlevels - 2; l >= 0; l--) {
+    int lo = t->level_off[l], hi = t->level_off[l + 1];
+    fmm_note_launch(), k_m2m<double><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr,
+        t->M.p, msize);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
+  const unsigned nb = (unsigned)((t->N + BH_THREADS - 1) / BH_THREADS);
+#define BH_ARGS                                                                                              \
+  t->N, t->nsys, t->nsys > 1 ? t->sys_off.p : nullptr, t->px.p, t->py.p, t->pz.p, t->perm.p, S, so, p,       \
+      t->theta, t->cx.p, t->cy.p, t->cz.p, cr, t->child_first.p, t->child_mask.p, t->pstart.p, t->pcount.p, \
+      t->M.p, msize, potential, field, F, t->d_eflags.p
+  const int q = p + 1;
+  if (q <= 4) fmm_note_launch(), k_bh64<35><<<nb, BH_THREADS, 0, st>>>(BH_ARGS);
+  else if (q <= 6) fmm_note_launch(), k_bh64<84><<<nb, BH_THREADS, 0, st>>>(BH_ARGS);
+  else if (q <= 9) fmm_note_launch(), k_bh64<220><<<nb, BH_THREADS, 0, st>>>(BH_ARGS);
+  else fmm_note_launch(), k_bh64<560><<<nb, BH_THREADS, 0, st>>>(BH_ARGS);
+#undef BH_ARGS
+  FMM_CUDA_TRY(cudaGetLastError());
+  uint32_t fl = 0;
+  FMM_CUDA_TRY(cudaMemcpyAsync(&fl, t->d_eflags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  if (fl) {
+    fmm_set_error_text("Barnes-Hut walk deeper than its stack");
+    return FMM_ERR_DEPTH;
+  }
+  t->last_prec = 0;  // the FP64 multipoles of this pass are in t->M
+  return FMM_OK;
+}
+
 // Per-phase times of the last evaluate (needs the stream to have completed).
 void fmm_eval_times(DevTree *t) {
   float ms;

@@ -154,6 +154,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
                    cudaStream_t st, const long *sys_off = nullptr, int nsys = 1);
 int fmm_tree_evaluate(DevTree *t, const double *S, double *F, int potential, int field, int precision,
                       cudaStream_t st);
+int fmm_tree_evaluate_bh(DevTree *t, const double *S, double *F, int potential, int field, cudaStream_t st);
 void fmm_tree_destroy(DevTree *t);
 void fmm_graph_release(DevTree *t);
 bool fmm_m2l_tc_supported(int p, int so);

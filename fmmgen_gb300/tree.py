@@ -111,6 +111,26 @@ class Tree:
             return F
         return Fd
 
+    def compute_field_bh(self, F=None, S=None, potential=True, field=True, stream=None):
+        """Tree::compute_field_bh (example/tree.cpp:273-293): Barnes-Hut with the
+        tree's order and theta, in FP64; returns F like compute_field_fmm."""
+        if S is not None:
+            self.S = _as_device(S, (sourcesize(self.source_order),))
+        if self.S is None:
+            raise ValueError("no sources")
+        os_ = outputsize(potential, field)
+        host_out = F is not None and not (isinstance(F, torch.Tensor) and F.is_cuda)
+        Fd = F if (F is not None and not host_out) else torch.empty((self.N, os_), dtype=torch.float64,
+                                                                     device=self.pos.device)
+        if Fd.dtype != torch.float64 or not Fd.is_contiguous() or Fd.numel() != self.N * os_:
+            raise ValueError("F must be a contiguous float64 [N][OUTPUTSIZE] array")
+        check(lib().fmmgen_tree_compute_field_bh(self._h, C.c_void_p(self.S.data_ptr()), C.c_void_p(Fd.data_ptr()),
+                                                 int(potential), int(field), _stream_ptr(stream)))
+        if host_out:
+            F[...] = Fd.reshape(np.shape(F)).cpu().numpy() if isinstance(F, np.ndarray) else Fd.cpu()
+            return F
+        return Fd
+
     def compute_field_exact(self, F=None, targets=None, potential=True, field=True, stream=None):
         return direct(self.pos, self.S, targets=targets, source_order=self.source_order, potential=potential,
                       field=field, F=F, stream=stream)

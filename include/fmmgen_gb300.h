@@ -153,6 +153,15 @@ int fmmgen_root_box_noalloc(const double *pos, long N, double *root4, void *stre
 /* Introspection (host outputs; synchronises).
  * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions]. */
 int fmmgen_tree_info(fmmgen_tree *tree, long *info);
+/* Tree::compute_field_bh (example/tree.cpp:273-293): FP64 P2M and M2M, then
+ * for every particle the walk of evaluate_M2P_and_P2P
+ * (example/calculate.cpp:266-314) from its system's root: a child c of an
+ * opened cell is opened when r_c > theta |x_i - c_c|, else its multipole acts
+ * through M2P (fmmgen's M2P potential with its exact gradient as the field --
+ * the generated field is wrong), and a leaf's particles through P2P.  S and F
+ * as in fmmgen_tree_compute_field_fmm; F is overwritten. */
+int fmmgen_tree_compute_field_bh(fmmgen_tree *tree, const double *S, double *F, int potential, int field,
+                                 void *stream);
 /* Root cube [cx, cy, cz, r] (of system 0 in a forest). */
 int fmmgen_tree_root(fmmgen_tree *tree, double *root4);
 /* Systems of a handle (1 for fmmgen_tree_build), their root cubes

@@ -218,6 +218,32 @@ void or_L2P(double x, double y, double z, const double *L, double *F, int order,
     if (field) { F[o] += ex; F[o + 1] += ey; F[o + 2] += ez; }
 }
 
+/* M2P_p: the Barnes-Hut far field of a multipole at (x,y,z) = particle - cell
+ * (fmmgen/generator.py:174-206): phi = V = sum_{so<=|m|<=order} D_m M[m] (the
+ * n = 0 output of M2L_p) and E = -grad V = -sum_m D_{m+e} M[m], the exact
+ * gradient (derivatives to order + 1).  The generator's own field is not the
+ * gradient of its potential (the same substitution defect as its P2P); this
+ * is the physical field. */
+void or_M2P(double x, double y, double z, const double *M, double *F, int order, int so, int potential,
+            int field) {
+    mi_init();
+    double D[1140];
+    or_derivs(x, y, z, order + 1, D);
+    long off = or_nterms(so - 1), cnt = or_nterms(order);
+    double phi = 0, ex = 0, ey = 0, ez = 0;
+    for (long j = off; j < cnt; j++) {
+        mi_t m = g_mi[j];
+        double v = M[j - off];
+        phi += D[j] * v;
+        ex -= D[idx3(m.x + 1, m.y, m.z)] * v;
+        ey -= D[idx3(m.x, m.y + 1, m.z)] * v;
+        ez -= D[idx3(m.x, m.y, m.z + 1)] * v;
+    }
+    int o = 0;
+    if (potential) F[o++] += phi;
+    if (field) { F[o] += ex; F[o + 1] += ey; F[o + 2] += ez; }
+}
+
 /* P2P: Coulomb  phi += q/R, E += q r/R^3 (example/operators.cpp:54-66);
  * dipole (source_order=1, S = degree-1 M coefficients):
  *   phi += -S.r/R^3, E += S/R^3 - 3 (S.r) r / R^5  (fmmgen/generator.py:257-288 potential). */
@@ -484,6 +510,41 @@ static void csr_by_target(long npairs, const long *pairs, int tgt_slot, long nce
     if (pair_out) *pair_out = pidx; else free(pidx);
 }
 
+/* P2M (as point-source M2M, example/calculate.cpp:135-161) and M2M, children
+ * before parents (example/calculate.cpp:163-187), into M (zeroed, creation
+ * order); returns the P2M seconds through *tp2m. */
+static void or_tree_multipoles_t(otree_t *t, double *M, double *tp2m) {
+    int order = t->order, so = t->so;
+    int ssize = so == 0 ? 1 : 3;
+    long msize = or_msize(order, so);
+    long nc = t->ncells, ncrit = t->ncrit;
+    double t0 = now_s();
+    /* P2M as point-source M2M (example/calculate.cpp:135-161) */
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long c = 0; c < nc; c++) {
+        const ocell_t *cc = &t->cells[c];
+        if (cc->nleaf >= ncrit) continue;
+        double Mt[1140];
+        for (long i = 0; i < cc->nleaf; i++) {
+            long l = cc->leaf[i];
+            memset(Mt, 0, sizeof(double) * msize);
+            for (int k = 0; k < ssize; k++) Mt[k] = t->S[ssize * l + k];
+            or_M2M(cc->x - t->pos[3 * l], cc->y - t->pos[3 * l + 1], cc->z - t->pos[3 * l + 2], Mt,
+                   &M[(size_t)c * msize], order, so);
+        }
+    }
+    double t1 = now_s();
+    if (tp2m) *tp2m = t1 - t0;
+    /* M2M, children before parents (example/calculate.cpp:163-187) */
+    for (long c = nc - 1; c > 0; c--) {
+        long p = t->cells[c].parent;
+        or_M2M(t->cells[p].x - t->cells[c].x, t->cells[p].y - t->cells[c].y,
+               t->cells[p].z - t->cells[c].z, &M[(size_t)c * msize], &M[(size_t)p * msize], order, so);
+    }
+}
+
+static void or_tree_multipoles(otree_t *t, double *M) { or_tree_multipoles_t(t, M, NULL); }
+
 /* Tree::compute_field_fmm (example/tree.cpp:243-271).  F is [N][outsize] in the
  * caller's particle order, overwritten.  M/L buffers are returned through
  * Mout/Lout when non-NULL (cells x Msize / Lsize, creation order).
@@ -505,27 +566,9 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     memset(F, 0, sizeof(double) * N * outsize);
     double tt[6] = {0};
     double t0 = now_s();
-    /* P2M as point-source M2M (example/calculate.cpp:135-161) */
-#pragma omp parallel for schedule(dynamic, 16)
-    for (long c = 0; c < nc; c++) {
-        const ocell_t *cc = &t->cells[c];
-        if (cc->nleaf >= ncrit) continue;
-        double Mt[1140];
-        for (long i = 0; i < cc->nleaf; i++) {
-            long l = cc->leaf[i];
-            memset(Mt, 0, sizeof(double) * msize);
-            for (int k = 0; k < ssize; k++) Mt[k] = t->S[ssize * l + k];
-            or_M2M(cc->x - t->pos[3 * l], cc->y - t->pos[3 * l + 1], cc->z - t->pos[3 * l + 2], Mt,
-                   &M[(size_t)c * msize], order, so);
-        }
-    }
-    double t1 = now_s();
-    /* M2M, children before parents (example/calculate.cpp:163-187) */
-    for (long c = nc - 1; c > 0; c--) {
-        long p = t->cells[c].parent;
-        or_M2M(t->cells[p].x - t->cells[c].x, t->cells[p].y - t->cells[c].y,
-               t->cells[p].z - t->cells[c].z, &M[(size_t)c * msize], &M[(size_t)p * msize], order, so);
-    }
+    double tp2m = 0;
+    or_tree_multipoles_t(t, M, &tp2m);
+    double t1 = t0 + tp2m;
     double t2 = now_s();
     long *moff, *msrc, *mpair, *poff, *psrc;
     csr_by_target(t->nm2l, t->m2l, 1, nc, &moff, &msrc, &mpair);
@@ -588,6 +631,51 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     if (Lout) memcpy(Lout, L, sizeof(double) * nc * lsize);
     free(M); free(L); free(moff); free(msrc); free(mpair); free(poff); free(psrc);
     return 0;
+}
+
+/* evaluate_M2P_and_P2P (example/calculate.cpp:266-314) for particle i from
+ * cell p: a child c of a non-leaf cell is opened when r_c > theta |x_i - c_c|,
+ * else its multipole acts through M2P; a leaf's particles act through P2P. */
+static void bh_walk(const otree_t *t, const double *M, long p, long i, double *F, int outsize, int potential,
+                    int field) {
+    const ocell_t *cp = &t->cells[p];
+    long msize = or_msize(t->order, t->so);
+    int ssize = t->so == 0 ? 1 : 3;
+    if (cp->nleaf >= t->ncrit) {
+        for (int o = 0; o < 8; o++) {
+            if (!(cp->nchild & (1u << o))) continue;
+            long c = cp->child[o];
+            const ocell_t *cc = &t->cells[c];
+            double dx = t->pos[3 * i] - cc->x, dy = t->pos[3 * i + 1] - cc->y, dz = t->pos[3 * i + 2] - cc->z;
+            double r = sqrt(dx * dx + dy * dy + dz * dz);
+            if (cc->r > t->theta * r)
+                bh_walk(t, M, c, i, F, outsize, potential, field);
+            else
+                or_M2P(dx, dy, dz, &M[(size_t)c * msize], &F[outsize * i], t->order, t->so, potential, field);
+        }
+    } else {
+        for (long l = 0; l < cp->nleaf; l++) {
+            long j = cp->leaf[l];
+            if (j == i) continue;
+            or_P2P(t->pos[3 * i] - t->pos[3 * j], t->pos[3 * i + 1] - t->pos[3 * j + 1],
+                   t->pos[3 * i + 2] - t->pos[3 * j + 2], &t->S[ssize * j], &F[outsize * i], t->so, potential,
+                   field);
+        }
+    }
+}
+
+/* Tree::compute_field_bh (example/tree.cpp:273-293) with the physical M2P field. */
+void or_tree_evaluate_bh(void *h, double *F, int potential, int field) {
+    otree_t *t = (otree_t *)h;
+    mi_init();
+    int outsize = (potential ? 1 : 0) + (field ? 3 : 0);
+    long msize = or_msize(t->order, t->so), nc = t->ncells;
+    double *M = (double *)calloc((size_t)nc * msize, sizeof(double));
+    memset(F, 0, sizeof(double) * t->N * outsize);
+    or_tree_multipoles(t, M);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long i = 0; i < t->N; i++) bh_walk(t, M, 0, i, F, outsize, potential, field);
+    free(M);
 }
 
 /* evaluate_direct (example/calculate.cpp:252-264) for a subset of targets:

@@ -50,6 +50,8 @@ def lib():
         L.or_tree_export_cells.argtypes = [C.c_void_p, _up, _lp, _dp, _lp, _lp, _lp, _lp]
         L.or_tree_export_lists.argtypes = [C.c_void_p, _up, _up]
         L.or_tree_set_m2l_orders.argtypes = [C.c_void_p, C.c_void_p]
+        L.or_M2P.argtypes = [d, d, d, _dp, _dp, i, i, i, i]
+        L.or_tree_evaluate_bh.argtypes = [C.c_void_p, _dp, i, i]
         L.or_tree_evaluate.restype = i
         L.or_tree_evaluate.argtypes = [C.c_void_p, _dp, i, i, l, C.c_void_p, C.c_void_p, _dp]
         L.or_direct.argtypes = [_dp, _dp, l, _lp, l, i, i, i, _dp]
@@ -97,6 +99,10 @@ def L2P(x, y, z, L, F, order, so=0, potential=True, field=True):
 
 def P2P(x, y, z, S, F, so=0, potential=True, field=True):
     lib().or_P2P(x, y, z, S, F, so, int(potential), int(field))
+
+
+def M2P(x, y, z, M, F, order, so=0, potential=True, field=True):
+    lib().or_M2P(x, y, z, M, F, order, so, int(potential), int(field))
 
 
 def derivs(x, y, z, p):
@@ -160,6 +166,12 @@ class OracleTree:
             raise ValueError("one order per M2L pair")
         lib().or_tree_set_m2l_orders(self.h, o.ctypes.data)
 
+    def evaluate_bh(self, potential=True, field=True):
+        """Tree::compute_field_bh with a physical M2P field (or_M2P)."""
+        F = np.zeros(self.N * outsize(potential, field))
+        lib().or_tree_evaluate_bh(self.h, F, int(potential), int(field))
+        return F.reshape(self.N, -1)
+
     def evaluate(self, potential=True, field=True, sample_stride=1, want_ML=False):
         F = np.zeros(self.N * outsize(potential, field))
         times = np.zeros(6)
@@ -222,6 +234,9 @@ def ref(so=0):
         L.ref_export_lists.argtypes = [C.c_void_p, _up, _up]
         L.ref_evaluate.restype = d
         L.ref_evaluate.argtypes = [C.c_void_p, _dp]
+        L.ref_evaluate_bh.restype = d
+        L.ref_evaluate_bh.argtypes = [C.c_void_p, _dp]
+        L.ref_M2P.argtypes = [d, d, d, _dp, _dp, i]
         L.ref_cell_M.argtypes = [C.c_void_p, _dp]
         L.ref_cell_L.argtypes = [C.c_void_p, _dp]
         L.ref_P2M.argtypes = [d, d, d, d, _dp, i]
@@ -276,6 +291,13 @@ class RefTree:
     def evaluate(self):
         F = np.zeros(self.N * 4)
         sec = self.L.ref_evaluate(self.h, F)
+        return F.reshape(self.N, 4), sec
+
+    def evaluate_bh(self):
+        """Tree::compute_field_bh; only the potential column is meaningful (the
+        generated M2P's field is not the gradient of its potential)."""
+        F = np.zeros(self.N * 4)
+        sec = self.L.ref_evaluate_bh(self.h, F)
         return F.reshape(self.N, 4), sec
 
     def ML(self):

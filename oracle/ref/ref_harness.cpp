@@ -143,6 +143,18 @@ double ref_evaluate(void *p, double *F) {
   return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// Tree::compute_field_bh (example/tree.cpp:273-293): the generated M2P's
+// potential is right, its field is not the gradient of that potential (the
+// generator defect the P2P restatement works around), so only the potential
+// of this pass is a pin.
+double ref_evaluate_bh(void *p, double *F) {
+  Handle *h = static_cast<Handle *>(p);
+  auto t0 = std::chrono::steady_clock::now();
+  h->tree.compute_field_bh(F);
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
 void ref_cell_M(void *p, double *out) {
   Handle *h = static_cast<Handle *>(p);
   memcpy(out, h->tree.M.data(), sizeof(double) * h->tree.M.size());
@@ -158,6 +170,7 @@ void ref_M2M(double x, double y, double z, double *M, double *Ms, int order) { M
 void ref_M2L(double x, double y, double z, double *M, double *L, int order) { M2L(x, y, z, M, L, order); }
 void ref_L2L(double x, double y, double z, double *L, double *Ls, int order) { L2L(x, y, z, L, Ls, order); }
 void ref_L2P(double x, double y, double z, double *L, double *F, int order) { L2P(x, y, z, L, F, order); }
+void ref_M2P(double x, double y, double z, double *M, double *F, int order) { M2P(x, y, z, M, F, order); }
 void ref_P2P_generated(double x, double y, double z, double *S, double *F) {
   fmmgen_generated_P2P(x, y, z, S, F);
 }

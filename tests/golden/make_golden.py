@@ -7,6 +7,9 @@ The values come from the reference's own code: fmmgen's generated operators
 interact_dehnen_lazy / compute_field_fmm, linked by oracle/ref/ref_harness.cpp.
 The one restated piece is P2P (the generated field is zero at HEAD); its
 potential is checked against the generated P2P here before anything is saved.
+Barnes-Hut fixtures (compute_field_bh, M2P) keep potentials only: the
+generated M2P's field is not the gradient of its potential.
+`--bh` writes only the Barnes-Hut fixtures.
 """
 import hashlib
 import os
@@ -131,6 +134,51 @@ def make_trees():
         print(f"tree_{name}.npz: cells {rt.ncells} leaves {rt.nleaves} m2l {len(m2l)} p2p {len(p2p)}")
 
 
+BH_CASES = {  # name: (N, ncrit, order, theta, source_order, generator)
+    "uniform10k": (10000, 64, 4, 0.5, 0, "uniform"),
+    "clustered": (5000, 16, 6, 0.5, 0, "clusters"),
+    "dipole_plummer": (3000, 32, 5, 0.5, 1, "plummer"),
+}
+
+
+def make_bh():
+    """Barnes-Hut: the reference's compute_field_bh potentials (its M2P field is
+    not the gradient of its potential, so only the potential is kept) and the
+    generated M2P's potential at every order."""
+    for seed, (name, (N, ncrit, p, theta, so, gen)) in enumerate(BH_CASES.items()):
+        rng = np.random.default_rng(100 + seed)
+        pos = {"uniform": lambda: rng.uniform(0, 1, (N, 3)), "plummer": lambda: plummer(rng, N),
+               "clusters": lambda: clusters(rng, N)}[gen]()
+        S = rng.uniform(-1, 1, (N, 1)) if so == 0 else rng.standard_normal((N, 3))
+        rt = O.RefTree(pos, S, ncrit, p, theta, so)
+        F, _ = rt.evaluate_bh()
+        np.savez_compressed(os.path.join(HERE, f"bh_{name}.npz"), N=np.int64(N), ncrit=np.int64(ncrit),
+                            order=np.int64(p), theta=np.float64(theta), source_order=np.int64(so), pos=pos, S=S,
+                            phi=F[:, 0])
+        print(f"bh_{name}.npz: N {N} p {p}")
+    rng = np.random.default_rng(77)
+    out = {}
+    for so, (pmin, pmax) in ((0, (1, 8)), (1, (2, 6))):
+        R = O.ref(so)
+        for p in range(pmin, pmax + 1):
+            K = 5
+            d = rng.uniform(-1, 1, (K, 3))
+            d *= rng.uniform(1.5, 3.0, (K, 1)) / np.linalg.norm(d, axis=1, keepdims=True)
+            M = rng.standard_normal((K, O.msize(p, so)))
+            phi = np.zeros(K)
+            for k in range(K):
+                F = np.zeros(4)
+                R.ref_M2P(*d[k], np.ascontiguousarray(M[k]), F, p)
+                phi[k] = F[0]
+            out[f"so{so}_p{p}_d"], out[f"so{so}_p{p}_M"], out[f"so{so}_p{p}_phi"] = d, M, phi
+    np.savez_compressed(os.path.join(HERE, "m2p_potential.npz"), **out)
+    print("m2p_potential.npz")
+
+
 if __name__ == "__main__":
-    make_ops()
-    make_trees()
+    if "--bh" in sys.argv:
+        make_bh()
+    else:
+        make_ops()
+        make_trees()
+        make_bh()
