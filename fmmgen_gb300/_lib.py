@@ -40,12 +40,14 @@ _SIGS = {
     "fmmgen_gpu_L2L": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, _vp]),
     "fmmgen_gpu_L2P": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_gpu_P2P": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_M2P": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_configure": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "P2M": (None, [C.c_double, C.c_double, C.c_double, C.c_double, _dp, C.c_int]),
     "M2M": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "M2L": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "L2L": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "L2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
+    "M2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "P2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "fmmgen_tree_build": (C.c_int, [_dp, C.c_long, C.c_long, C.c_int, C.c_double, C.c_int, _vp,
                                     C.POINTER(C.c_void_p)]),

@@ -89,6 +89,10 @@ int fmmgen_gpu_L2P(int n, const double *d, const double *L, double *F, int order
 int fmmgen_gpu_P2P(int n, const double *d, const double *Sv, double *F, int so, int potential, int field, void *st) {
   OPB(5, n, d, Sv, F, 0, so, potential, field, st);
 }
+int fmmgen_gpu_M2P(int n, const double *d, const double *M, double *F, int order, int so, int potential, int field,
+                   void *st) {
+  OPB(6, n, d, M, F, order, so, potential, field, st);
+}
 
 }  // extern "C"
 
@@ -158,6 +162,11 @@ void L2L(double x, double y, double z, double *L, double *Ls, int order) {
 void L2P(double x, double y, double z, double *L, double *F, int order) {
   if (!order_ok(order)) return;
   scalar_op(4, x, y, z, L, (int)fmmgen_lsize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
+            order);
+}
+void M2P(double x, double y, double z, double *M, double *F, int order) {
+  if (!order_ok(order)) return;
+  scalar_op(6, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
             order);
 }
 void P2P(double x, double y, double z, double *Sv, double *F) {

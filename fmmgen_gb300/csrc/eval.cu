@@ -17,6 +17,7 @@
 #include "internal.h"
 #include "mi_table.cuh"
 #include "m2l_gen.cuh"
+#include "deriv.cuh"
 
 #define TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
 
@@ -642,35 +643,6 @@ int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st
 // ---------------------------------------------------------------------------
 // Barnes-Hut (Tree::compute_field_bh, example/tree.cpp:273-293)
 // ---------------------------------------------------------------------------
-// D[idx(n)] = d^n (1/|y|) at y, |n| <= q, in one thread, degree by degree:
-//   |n| |y|^2 D_n = -(2|n| - 1) sum_a n_a y_a D_(n - e_a) - (|n| - 1) sum_a n_a (n_a - 1) D_(n - 2 e_a)
-__device__ __forceinline__ void thread_derivs(double yx, double yy, double yz, int q, double *D) {
-  const double ir2 = 1.0 / (yx * yx + yy * yy + yz * yz);
-  D[0] = sqrt(ir2);
-  int i = 1;
-  for (int d = 1; d <= q; d++) {
-    const double rd = 1.0 / d, a1 = -(2 * d - 1) * ir2 * rd, a2 = -(d - 1) * ir2 * rd;
-    for (int nx = d; nx >= 0; nx--)
-      for (int ny = d - nx; ny >= 0; ny--, i++) {
-        const int nz = d - nx - ny;
-        double s1 = 0, s2 = 0;
-        if (nx) {
-          s1 += nx * yx * D[fmm_idx3(nx - 1, ny, nz)];
-          if (nx > 1) s2 += nx * (nx - 1) * D[fmm_idx3(nx - 2, ny, nz)];
-        }
-        if (ny) {
-          s1 += ny * yy * D[fmm_idx3(nx, ny - 1, nz)];
-          if (ny > 1) s2 += ny * (ny - 1) * D[fmm_idx3(nx, ny - 2, nz)];
-        }
-        if (nz) {
-          s1 += nz * yz * D[fmm_idx3(nx, ny, nz - 1)];
-          if (nz > 1) s2 += nz * (nz - 1) * D[fmm_idx3(nx, ny, nz - 2)];
-        }
-        D[i] = a1 * s1 + a2 * s2;
-      }
-  }
-}
-
 // One thread per particle (sorted order), FP64: evaluate_M2P_and_P2P
 // (example/calculate.cpp:266-314) from the particle's root with an explicit
 // stack.  A child c of an open cell is opened when r_c > theta |x_i - c_c|,

@@ -151,11 +151,47 @@ __global__ void k_op_p2p(int n, const double *d, const double *S, double *F, int
 }
 
 // op: 0 P2M, 1 M2M, 2 M2L, 3 L2L, 4 L2P, 5 P2P
+// M2P_p (fmmgen/generator.py:174-206), one thread per application: the
+// potential V = sum_m D_m(d) M_m of fmmgen's M2P and its exact gradient
+// E = -sum_m D_(m+e)(d) M_m (the generated field is not that gradient);
+// d = particle - cell.  NTQ holds the derivatives to order + 1.
+template <int NTQ>
+__global__ void k_op_m2p(int n, const double *d, const double *M, double *F, int order, int so, int potential,
+                         int field) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double D[NTQ];
+  thread_derivs(d[3 * i], d[3 * i + 1], d[3 * i + 2], order + 1, D);
+  const int moff = fmm_nterms(so - 1), ms = fmm_nterms(order) - moff;
+  const double *Mi = M + (size_t)i * ms;
+  double v = 0, gx = 0, gy = 0, gz = 0;
+  int j = moff;
+  for (int dg = so; dg <= order; dg++)
+    for (int mx = dg; mx >= 0; mx--)
+      for (int my = dg - mx; my >= 0; my--, j++) {
+        const int mz = dg - mx - my;
+        const double w = Mi[j - moff];
+        v += D[j] * w;
+        gx += D[fmm_idx3(mx + 1, my, mz)] * w;
+        gy += D[fmm_idx3(mx, my + 1, mz)] * w;
+        gz += D[fmm_idx3(mx, my, mz + 1)] * w;
+      }
+  const int os = (potential ? 1 : 0) + (field ? 3 : 0);
+  double *Fi = F + (size_t)i * os;
+  int k = 0;
+  if (potential) Fi[k++] += v;
+  if (field) {
+    Fi[k] -= gx;
+    Fi[k + 1] -= gy;
+    Fi[k + 2] -= gz;
+  }
+}
+
 int fmm_op_batch(int op, int n, const double *d, const double *in, double *out, int order, int so, int potential,
                  int field, cudaStream_t st) {
   if (n < 0 || so < 0 || so > 1 || !d || !in || !out) return FMM_ERR_ARG;
   if (op != 5 && (order < 0 || order > FMM_PMAX || order < so)) return FMM_ERR_ARG;
-  if ((op == 4 || op == 5) && !potential && !field) return FMM_ERR_ARG;
+  if ((op == 4 || op == 5 || op == 6) && !potential && !field) return FMM_ERR_ARG;
   if (n == 0) return FMM_OK;
   unsigned nb = fmm_blocks(n, OPW);
   int ms = fmm_nterms(order) - fmm_nterms(so - 1), ls = fmm_nterms(order - so);
@@ -171,6 +207,11 @@ int fmm_op_batch(int op, int n, const double *d, const double *in, double *out, 
     case 3: fmm_note_launch(), k_op_shift<<<nb, 32 * OPW, 0, st>>>(ps->l2l, n, d, in, out, order, so, ls, ls, order - so); break;
     case 4: fmm_note_launch(), k_op_l2p<<<nb, 32 * OPW, 0, st>>>(n, d, in, out, order, so, potential, field); break;
     case 5: fmm_note_launch(), k_op_p2p<<<fmm_blocks(n, 128), 128, 0, st>>>(n, d, in, out, so, potential, field); break;
+    case 6:
+      if (order + 1 <= 6) fmm_note_launch(), k_op_m2p<84><<<fmm_blocks(n, 128), 128, 0, st>>>(n, d, in, out, order, so, potential, field);
+      else if (order + 1 <= 9) fmm_note_launch(), k_op_m2p<220><<<fmm_blocks(n, 128), 128, 0, st>>>(n, d, in, out, order, so, potential, field);
+      else fmm_note_launch(), k_op_m2p<560><<<fmm_blocks(n, 128), 128, 0, st>>>(n, d, in, out, order, so, potential, field);
+      break;
     default: return FMM_ERR_ARG;
   }
   FMM_CUDA_TRY(cudaGetLastError());

@@ -4,9 +4,9 @@ fmmgen emits `<name>_wrap` with `cpdef` functions over `double[:]` buffers
 (fmmgen/writer.py:349-432): the order dispatchers P2M, M2M, M2L, L2L, L2P, M2P
 taking a trailing `order`, per-order functions with the underscore dropped
 (`P2M_3` -> `P2M3`), P2P, and the FMMGEN_* constants.  `module(...)` returns
-an object with the same names for the operators this library covers (M2P, the
-Barnes-Hut operator, is not part of the FMM path); every call runs on the GPU
-through libfmmgen_gb300.so and adds into the caller's numpy array in place.
+an object with the same names; every call runs on the GPU through
+libfmmgen_gb300.so and adds into the caller's numpy array in place.  M2P's
+field is the exact gradient of its potential (the generated one is not).
 
 Batched device versions (torch tensors, many applications per launch) are the
 `*_batch` functions at module level.
@@ -18,7 +18,7 @@ import torch
 
 from ._lib import check, lib
 
-_OPS = ("P2M", "M2M", "M2L", "L2L", "L2P")
+_OPS = ("P2M", "M2M", "M2L", "L2L", "L2P", "M2P")
 
 
 def nterms(p):
@@ -74,6 +74,10 @@ class OperatorModule:
     def L2P(self, x, y, z, L, F, order):
         self._configure()
         lib().L2P(x, y, z, _buf(L), _buf(F), order)
+
+    def M2P(self, x, y, z, M, F, order):
+        self._configure()
+        lib().M2P(x, y, z, _buf(M), _buf(F), order)
 
     def P2P(self, x, y, z, S, F):
         self._configure()
@@ -136,6 +140,13 @@ def L2P_batch(d, L, F, order, source_order=0, potential=True, field=True, stream
     n = d.shape[0]
     os_ = int(lib().fmmgen_outputsize(int(potential), int(field)))
     check(lib().fmmgen_gpu_L2P(n, _dev(d, n, 3), _dev(L, n, lsize(order, source_order)), _dev(F, n, os_), order,
+                               source_order, int(potential), int(field), _st(stream)))
+
+
+def M2P_batch(d, M, F, order, source_order=0, potential=True, field=True, stream=None):
+    n = d.shape[0]
+    os_ = int(lib().fmmgen_outputsize(int(potential), int(field)))
+    check(lib().fmmgen_gpu_M2P(n, _dev(d, n, 3), _dev(M, n, msize(order, source_order)), _dev(F, n, os_), order,
                                source_order, int(potential), int(field), _st(stream)))
 
 

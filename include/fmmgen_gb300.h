@@ -66,7 +66,9 @@ int fmmgen_outputsize(int potential, int field);    /* FMMGEN_OUTPUTSIZE */
  *   M2L: in = M[n][Msize],   out = L[n][Lsize]     (fmmgen/expansions.py:108-172)
  *   L2L: in = L[n][Lsize],   out = Ls[n][Lsize]    (fmmgen/expansions.py:175-194)
  *   L2P: in = L[n][Lsize],   out = F[n][OUTPUTSIZE](fmmgen/expansions.py:197-207)
- *   P2P: in = S[n][SOURCESIZE], out = F[n][OUTPUTSIZE] (example/operators.cpp:54-66) */
+ *   P2P: in = S[n][SOURCESIZE], out = F[n][OUTPUTSIZE] (example/operators.cpp:54-66)
+ *   M2P: in = M[n][Msize],   out = F[n][OUTPUTSIZE] (fmmgen/generator.py:174-206: the
+ *        potential of fmmgen's M2P and its exact gradient as the field) */
 int fmmgen_gpu_P2M(int n, const double *d, const double *q, double *M, int order, int source_order, void *stream);
 int fmmgen_gpu_M2M(int n, const double *d, const double *M, double *Ms, int order, int source_order, void *stream);
 int fmmgen_gpu_M2L(int n, const double *d, const double *M, double *L, int order, int source_order, void *stream);
@@ -75,6 +77,8 @@ int fmmgen_gpu_L2P(int n, const double *d, const double *L, double *F, int order
                    int field, void *stream);
 int fmmgen_gpu_P2P(int n, const double *d, const double *S, double *F, int source_order, int potential, int field,
                    void *stream);
+int fmmgen_gpu_M2P(int n, const double *d, const double *M, double *F, int order, int source_order, int potential,
+                   int field, void *stream);
 
 /* ---- scalar twins of the generated dispatchers (host pointers, run on the
  *      GPU synchronously).  Signatures of example/operators.cpp:1376-1489;
@@ -88,6 +92,7 @@ void M2M(double x, double y, double z, double *M, double *Ms, int order);
 void M2L(double x, double y, double z, double *M, double *L, int order);
 void L2L(double x, double y, double z, double *L, double *Ls, int order);
 void L2P(double x, double y, double z, double *L, double *F, int order);
+void M2P(double x, double y, double z, double *M, double *F, int order);
 void P2P(double x, double y, double z, double *S, double *F);
 
 /* ---- tree-level API (example/tree.hpp:78-103) ---- */

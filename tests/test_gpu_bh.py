@@ -69,3 +69,29 @@ def test_bh_forest_matches_separate_trees(fg):
         sl = slice(off[s], off[s + 1])
         G = fg.build_tree(pos[sl], S[sl], k, 32, 5, 0.5).compute_field_bh().cpu().numpy()
         assert rel(F[sl], G) < 1e-13
+
+
+def test_m2p_operator(fg, oracle_lib):
+    """M2P on the operator surface: the batched device call, the scalar twin and
+    the module method against the reference's M2P potential and the oracle's
+    field."""
+    from fmmgen_gb300 import operators
+
+    g = np.load(os.path.join(GOLDEN, "m2p_potential.npz"))
+    for so, (pmin, pmax) in ((0, (1, 8)), (1, (2, 6))):
+        for p in range(pmin, pmax + 1):
+            d, M, phi = g[f"so{so}_p{p}_d"], g[f"so{so}_p{p}_M"], g[f"so{so}_p{p}_phi"]
+            K = len(d)
+            F = torch.zeros((K, 4), dtype=torch.float64, device="cuda")
+            operators.M2P_batch(torch.tensor(d, device="cuda"), torch.tensor(M, device="cuda"), F, p, so)
+            F = F.cpu().numpy()
+            Fo = np.zeros((K, 4))
+            for k in range(K):
+                oracle_lib.M2P(*d[k], np.ascontiguousarray(M[k]), Fo[k], p, so)
+            assert np.allclose(F[:, 0], phi, rtol=1e-12, atol=0)
+            assert np.allclose(F[:, 1:], Fo[:, 1:], rtol=1e-11, atol=1e-14 * np.abs(Fo).max())
+            mod = operators.module(pmax + 1, source_order=so)
+            Fs = np.zeros(4)
+            mod.M2P(*d[0], np.ascontiguousarray(M[0]), Fs, p)
+            getattr(mod, f"M2P{p}")(*d[0], np.ascontiguousarray(M[0]), Fs)  # += semantics: twice
+            assert np.allclose(Fs, 2 * F[0], rtol=1e-12, atol=0)
