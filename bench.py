@@ -78,6 +78,8 @@ def args_parse():
     ap.add_argument("--nsys", type=int, default=NSYS_BATCHED, help="systems of the batched configuration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default M2L rules (no autotuner run)")
+    ap.add_argument("--tune", default=None,
+                    help="impl,nslots,grouping,overlap: set the M2L choice instead of running the autotuner")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
     ap.add_argument("--profile-only", action="store_true",
@@ -337,7 +339,11 @@ def main():
     tree = fg.Tree(pos, q, a.ncrit, a.order, a.theta, source_order=a.so,
                    sys_off=sys_offsets(a) if a.sizes is not None else None)
     autotune = None
-    if not a.no_autotune and a.dist != "mixture":
+    if a.tune:
+        impl, nslots, grouping, overlap = (int(v) for v in a.tune.split(","))
+        tree.set_tune(impl, nslots, grouping, overlap)
+        autotune = {"chosen": tree.get_tune(), "candidates_ms": None, "legend": "set with --tune"}
+    elif not a.no_autotune and a.dist != "mixture":
         # the M2L autotuner, once before the warm-up (outside every timed region)
         r = tree.autotune(precision="mixed", reps=3)
         autotune = {"chosen": r["best"], "candidates_ms": [

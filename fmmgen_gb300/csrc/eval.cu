@@ -455,7 +455,7 @@ static int m2l_impl(const DevTree *t, int precision) {
   const bool tc_ok = fmm_m2l_tc_supported(t->order, t->so), gen_ok = fmm_m2l_gen_supported(t->order, t->so);
   int impl = t->tune.impl;
   if (impl < 0) impl = precision == 1 ? M2L_TC : M2L_GEN;
-  if (impl == M2L_TC && !tc_ok) impl = M2L_GEN;
+  if (impl == M2L_TC && (!tc_ok || t->nclasses > 262144)) impl = M2L_GEN;  // class bitmap of the tile schedule
   if (impl == M2L_GEN && !gen_ok) impl = M2L_ENGINE;
   return impl;
 }

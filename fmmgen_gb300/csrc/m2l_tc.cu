@@ -612,40 +612,70 @@ __global__ void k_tc_operators(const double *D64, const int *key4, int ncls, TcP
   }
 }
 
-// Class steps of every tile (one block of 128 threads per tile, thread = row):
-// the sorted union of the rows' class-sorted lists.  Counting pass (cls_out
-// null): count[tile] = steps; writing pass: the class of each step and, per
-// warp quarter of the tile, the rows with a source in it.
-__global__ void __launch_bounds__(TC_ROWS) k_tc_sched(const int *order, int ncells, const int *off, const int *cls,
-                                                      int *count, const int *sched_off, unsigned *cls_out,
-                                                      unsigned *mask_out) {
-  __shared__ unsigned wmin[TC_ROWS / 32];
-  const int tile = blockIdx.x, r = threadIdx.x, w = r >> 5, lane = r & 31;
+// Class steps of every tile: the sorted union of its rows' class-sorted
+// lists, as a bitmap over the classes in shared memory (one block of 128
+// threads per tile, thread = row).  Counting pass: count[tile] = classes in
+// the union.  Writing pass: step st of a class is its rank in the bitmap; every
+// list entry sets its row's bit in the step's mask (zeroed before) and the
+// step's class.
+#define TC_SCHED_MAXW 8192  // bitmap words: classes up to 262,144
+__device__ __forceinline__ void tc_sched_bitmap(const int *order, int ncells, const int *off, const int *cls,
+                                                int nwords, unsigned *bm, int &k0, int &k1) {
+  const int tile = blockIdx.x, r = threadIdx.x;
+  for (int i = r; i < nwords; i += TC_ROWS) bm[i] = 0u;
+  __syncthreads();
   const int rr = tile * TC_ROWS + r;
   const int A = rr < ncells ? order[rr] : -1;
-  int k = A >= 0 ? off[A] : 0;
-  const int kend = A >= 0 ? off[A + 1] : 0;
-  int st = cls_out ? sched_off[tile] : 0, n = 0;
-  while (true) {
-    const unsigned h = k < kend ? (unsigned)cls[k] : TC_NONE;
-    const unsigned m = __reduce_min_sync(0xffffffffu, h);
-    if (lane == 0) wmin[w] = m;
-    __syncthreads();
-    unsigned c = wmin[0];
-#pragma unroll
-    for (int i = 1; i < TC_ROWS / 32; i++) c = min(c, wmin[i]);
-    __syncthreads();  // wmin is rewritten next round
-    if (c == TC_NONE) break;
-    const unsigned bal = __ballot_sync(0xffffffffu, h == c);
-    if (cls_out) {
-      if (r == 0) cls_out[st] = c;
-      if (lane == 0) mask_out[4 * st + w] = bal;
-    }
-    st++;
-    n++;
-    if (h == c) k++;
+  k0 = A >= 0 ? off[A] : 0;
+  k1 = A >= 0 ? off[A + 1] : 0;
+  for (int k = k0; k < k1; k++) {
+    const unsigned c = (unsigned)cls[k];
+    atomicOr(bm + (c >> 5), 1u << (c & 31));
   }
-  if (!cls_out && r == 0) count[tile] = n;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(TC_ROWS) k_tc_sched_count(const int *order, int ncells, const int *off,
+                                                            const int *cls, int nwords, int *count) {
+  extern __shared__ unsigned bm[];
+  __shared__ int part[TC_ROWS / 32];
+  int k0, k1;
+  tc_sched_bitmap(order, ncells, off, cls, nwords, bm, k0, k1);
+  int n = 0;
+  for (int i = threadIdx.x; i < nwords; i += TC_ROWS) n += __popc(bm[i]);
+  n = __reduce_add_sync(0xffffffffu, n);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int i = 0; i < TC_ROWS / 32; i++) tot += part[i];
+    count[blockIdx.x] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(TC_ROWS) k_tc_sched_write(const int *order, int ncells, const int *off,
+                                                            const int *cls, int nwords, const int *sched_off,
+                                                            unsigned *cls_out, unsigned *mask_out) {
+  extern __shared__ unsigned bm[];  // [nwords] bitmap, then [nwords] rank of each word's first class
+  unsigned *rank = bm + nwords;
+  int k0, k1;
+  tc_sched_bitmap(order, ncells, off, cls, nwords, bm, k0, k1);
+  if (threadIdx.x == 0) {  // exclusive prefix of the word popcounts
+    unsigned tot = 0;
+    for (int i = 0; i < nwords; i++) {
+      rank[i] = tot;
+      tot += __popc(bm[i]);
+    }
+  }
+  __syncthreads();
+  const int base = sched_off[blockIdx.x], w = threadIdx.x >> 5;
+  const unsigned bit = 1u << (threadIdx.x & 31);
+  for (int k = k0; k < k1; k++) {
+    const unsigned c = (unsigned)cls[k];
+    const int st = base + (int)(rank[c >> 5] + __popc(bm[c >> 5] & ((1u << (c & 31)) - 1u)));
+    cls_out[st] = c;  // every row of the class writes the same value
+    atomicOr(mask_out + 4 * st + w, bit);
+  }
 }
 
 // Source multipoles as 2^e (hi + lo), hi and lo FP16 rows of kpad terms, e per
@@ -726,8 +756,14 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   if (t->sched_serial != t->build_serial || t->sched_version != t->order_version) {
     if (fmm_reserve(t->tc_sched_off, ntiles + 1)) return FMM_ERR_CUDA;
     int *cnt = t->tc_sched_off.p + 1;
-    fmm_note_launch(), k_tc_sched<<<ntiles, TC_ROWS, 0, st>>>(t->m2l_order.p, nc, t->m2l_off.p, t->m2l_cls.p, cnt,
-                                                             nullptr, nullptr, nullptr);
+    const int nwords = (t->nclasses + 31) / 32;
+    if (nwords > TC_SCHED_MAXW) return FMM_ERR_RANGE;
+    if (nwords * 8 > 48 * 1024) {
+      FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_sched_count, cudaFuncAttributeMaxDynamicSharedMemorySize, nwords * 4));
+      FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_sched_write, cudaFuncAttributeMaxDynamicSharedMemorySize, nwords * 8));
+    }
+    fmm_note_launch(), k_tc_sched_count<<<ntiles, TC_ROWS, nwords * 4, st>>>(t->m2l_order.p, nc, t->m2l_off.p,
+                                                                             t->m2l_cls.p, nwords, cnt);
     FMM_CUDA_TRY(cudaGetLastError());
     std::vector<int> h(ntiles + 1);
     FMM_CUDA_TRY(cudaMemcpyAsync(h.data() + 1, cnt, sizeof(int) * ntiles, cudaMemcpyDeviceToHost, st));
@@ -739,9 +775,10 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
     if (fmm_reserve(t->tc_sched_cls, nsteps > 0 ? nsteps : 1) ||
         fmm_reserve(t->tc_sched_mask, 4 * (size_t)(nsteps > 0 ? nsteps : 1)))
       return FMM_ERR_CUDA;
-    fmm_note_launch(), k_tc_sched<<<ntiles, TC_ROWS, 0, st>>>(t->m2l_order.p, nc, t->m2l_off.p, t->m2l_cls.p,
-                                                             nullptr, t->tc_sched_off.p, t->tc_sched_cls.p,
-                                                             t->tc_sched_mask.p);
+    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_sched_mask.p, 0, sizeof(unsigned) * 4 * (size_t)nsteps, st));
+    fmm_note_launch(), k_tc_sched_write<<<ntiles, TC_ROWS, nwords * 8, st>>>(
+        t->m2l_order.p, nc, t->m2l_off.p, t->m2l_cls.p, nwords, t->tc_sched_off.p, t->tc_sched_cls.p,
+        t->tc_sched_mask.p);
     FMM_CUDA_TRY(cudaGetLastError());
     FMM_CUDA_TRY(cudaStreamSynchronize(st));  // h is read by the copy above
     t->sched_serial = t->build_serial;
