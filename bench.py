@@ -105,6 +105,23 @@ def metric_name(a):
     return f"particles/s full FMM, {a.config} (N={a.n})"
 
 
+def max_over_ranks(x, pg=None, device=None):
+    """The job's time: the largest of the ranks' times (replicas run side by side)."""
+    if pg is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return t.item()
+
+
+def job_throughput(n_per_rank, steps, world, t_max_ms):
+    """Particles per second of the whole job: every rank's particles over the
+    slowest rank's time."""
+    return n_per_rank * steps * world / (t_max_ms / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -396,12 +413,8 @@ def main():
     launches = L.fmmgen_launch_count() - n0
     m2l_steps, m2l_mmas, m2l_exec_flops = tree.m2l_work()  # of the last timed (mixed) step
     m2l_orders = tree.m2l_orders() if model is not None else None
-    t_max = dev_ms
-    if pg:
-        t = torch.tensor([dev_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_max = t.item()
-    value = a.n * a.steps * world / (t_max / 1e3)
+    t_max = max_over_ranks(dev_ms, pg, dev)
+    value = job_throughput(a.n, a.steps, world, t_max)
     ms_per_step = t_max / a.steps
     # ---- eval-only (the reference's timed region, example/main.cpp:154-162): the tree is
     # built once, then the evaluation pass is replayed from its recorded CUDA graph ----
@@ -411,12 +424,8 @@ def main():
     eval_ms, _ = timed(a.steps, lambda: tree.compute_field_fmm(F, potential=a.potential, field=a.field,
                                                                   precision="mixed"))
     tree.set_graph(False)
-    eval_max = eval_ms
-    if pg:
-        t = torch.tensor([eval_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        eval_max = t.item()
-    eval_only = {"value": a.n * a.steps * world / (eval_max / 1e3), "unit": UNIT, "ms_per_step": eval_max / a.steps,
+    eval_max = max_over_ranks(eval_ms, pg, dev)
+    eval_only = {"value": job_throughput(a.n, a.steps, world, eval_max), "unit": UNIT, "ms_per_step": eval_max / a.steps,
                  "note": "P2M..L2P only, tree built once; the pass is replayed from its recorded CUDA graph"}
     if a.profile_only:
         if rank == 0:
@@ -441,12 +450,8 @@ def main():
     e2e_step()
     k_e2e = max(3, a.steps // 2)
     e2e_ms, _ = timed(k_e2e, e2e_step)
-    e2e_max = e2e_ms
-    if pg:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_max = t.item()
-    e2e_value = a.n * k_e2e * world / (e2e_max / 1e3)
+    e2e_max = max_over_ranks(e2e_ms, pg, dev)
+    e2e_value = job_throughput(a.n, k_e2e, world, e2e_max)
     h2d = pos_h.numel() * 8 + q_h.numel() * 8
     d2h = F_h.numel() * 8
     tree.rebuild(pos)
