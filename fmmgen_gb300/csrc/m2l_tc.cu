@@ -30,18 +30,19 @@
 // computed once per build (k_tc_sched): the kernel's warps then follow that
 // schedule independently, coupled only through mbarriers.
 //
-// Per CTA (one per SM, persistent), 13 warps:
-//  * warps 0-3 gather the source rows of each (class, 64-term K-block) step
+// Per CTA (one per SM, persistent), 17 warps:
+//  * warps 0-7 gather the source rows of each (class, 64-term K-block) step
+//    (warps w and w+4: rows 32 (w % 4) .. + 31, one half of the chunks each)
 //    into a stage slot with cp.async, in the 128-byte swizzled K-major layout,
 //    and arrive on the slot's mbarrier when their copies land
 //    (cp.async.mbarrier.arrive); thread 0 also fetches the class's pre-split
 //    operator chunks (32-byte swizzled) and column scales with bulk copies.  A
 //    row without a source in the class is not copied: its accumulator row
 //    holds garbage that the fold leaves out;
-//  * warps 4-11 fold each finished class step out of tensor memory (warps w
+//  * warps 8-15 fold each finished class step out of tensor memory (warps w
 //    and w+4 take the two column halves of lane quarter w % 4) and store the
 //    tile's rows;
-//  * warp 12 allocates 512 tensor-memory columns (two accumulators) and one of
+//  * warp 16 allocates 512 tensor-memory columns (two accumulators) and one of
 //    its lanes issues the MMAs.
 // Stage slots and accumulators circulate through mbarriers; every wait is
 // bounded and reports a timeout through an error flag instead of hanging.
@@ -59,9 +60,9 @@ constexpr int TC_KB = 64;         // terms per K-block: one 128-byte swizzle row
 constexpr int TC_A_BYTES = TC_ROWS * 128;  // one operand half (hi or lo) of a K-block
 constexpr int TC_MAXCH = 16;      // K chunks (p <= 9: at most 14)
 constexpr int TC_MAXKB = 4;
-constexpr int TC_GWARPS = 4;      // gather warps 0-3
-constexpr int TC_FWARPS = 8;      // fold warps 4-11
-constexpr int TC_MWARP = TC_GWARPS + TC_FWARPS;  // warp 12: tensor memory + MMA issue
+constexpr int TC_GWARPS = 8;      // gather warps 0-7
+constexpr int TC_FWARPS = 8;      // fold warps 8-15
+constexpr int TC_MWARP = TC_GWARPS + TC_FWARPS;  // warp 16: tensor memory + MMA issue
 constexpr int TC_GATHER = 32 * TC_GWARPS;
 constexpr int TC_FOLD = 32 * TC_FWARPS;
 constexpr int TC_THREADS = 32 * (TC_MWARP + 1);
@@ -215,7 +216,7 @@ namespace {
 struct TcShared {
   alignas(16) float colf[2][TC_ACC_COLS];  // column scales 2^g of the class in each accumulator (bulk-copy
                                            // destination: 16-byte aligned)
-  uint64_t full[TC_MAXSLOTS];   // slot filled: 128 cp.async arrivals + thread 0's expect_tx arrival
+  uint64_t full[TC_MAXSLOTS];   // slot filled: 256 cp.async arrivals + thread 0's expect_tx arrival
   uint64_t empty[TC_MAXSLOTS];  // slot consumed: MMA commit
   uint64_t accfull[2];          // class step accumulated: MMA commit
   uint64_t accempty[2];         // accumulator folded out: 256 fold arrivals
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
 
   if (warp < TC_GWARPS) {
     // ---------------- gather ----------------
-    const int quarter = warp;
+    const int quarter = warp & 3, chalf = warp >> 2;  // rows 32 quarter .. + 31, chunks 4 chalf .. + 3
     const int row = 32 * quarter + lane;  // tile row whose list this thread walks
     uint32_t g = 0, u = 0;
     bool ok = true;
@@ -350,8 +351,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
           const uint32_t sa = base + (uint32_t)slot * P.slot_bytes;
           const int qn = min(8, (P.kpad - TC_KB * kb) >> 3);  // valid 16-byte chunks of the K-block
 #pragma unroll
-          for (int jj = 0; jj < 8; jj++) {
-            const int rl = 4 * jj + (lane >> 3), q = lane & 7;  // 4 rows x 8 chunks per instruction
+          for (int jj = 0; jj < 4; jj++) {
+            const int rl = 8 * jj + (lane >> 2), q = 4 * chalf + (lane & 3);  // 8 rows x 4 chunks per instruction
             const int r = 32 * quarter + rl;
             const int sr = __shfl_sync(0xffffffffu, mysrc, rl);
             if (sr >= 0 && q < qn) {
@@ -444,7 +445,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
     }
     if (!ok && lane == 0) atomicOr(P.err, 1u);
   } else if (lane == 0) {
-    // ---------------- MMA issue (one thread of warp 12) ----------------
+    // ---------------- MMA issue (one thread of warp 16) ----------------
     // Per-chunk instruction descriptors and operator offsets live in
     // registers (compile-time indices below), so nothing but descriptor
     // arithmetic sits between consecutive MMAs.
