@@ -211,6 +211,27 @@ __global__ void k_ss_maps(const double *__restrict__ pos, long N, long nchunks, 
   }
 }
 
+// S * 2^(e-52) for |S| in [2^52, 2^53), assembled from its bits (integer
+// operations only: the chain runs on one warp per axis, where every FP64
+// instruction costs the narrow FP64 pipe a full warp's worth of cycles)
+__device__ __forceinline__ double ss_to_double(long long S, int e) {
+  const unsigned long long m = (unsigned long long)(S < 0 ? -S : S);
+  unsigned long long bits = ((unsigned long long)(e + 1023) << 52) | (m & ((1ull << 52) - 1));
+  if (S < 0) bits |= 1ull << 63;
+  return __longlong_as_double((long long)bits);
+}
+// binade e and S = s / 2^(e-52) of a normal double; false for zero,
+// subnormals, infinities and NaN (which take plain FP64 adds)
+__device__ __forceinline__ bool ss_from_double(double s, int &e, long long &S) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(s);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  if (ex == 0 || ex == 0x7ff) return false;
+  e = ex - 1023;
+  const long long m = (long long)((bits & ((1ull << 52) - 1)) | (1ull << 52));
+  S = (bits >> 63) ? -m : m;
+  return true;
+}
+
 // Chains the chunk maps in order, exactly: one warp per axis.  The state
 // (s, or S in ulps of binade e) is kept identical in every lane.  A chunk whose
 // map is missing or invalid for the exact state is run 32 elements at a time:
@@ -228,6 +249,10 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
   bool imode = false;
   long long S = 0;
   int e = 0;
+  // elements of the chunk after the last chunk that ran element by element
+  // (such chunks come in runs: their loads overlap the previous one's work)
+  long pref_k = -1;
+  double pr[SS_PER_LANE];
   for (long k0 = 0; k0 < nchunks; k0 += 32) {
     __syncwarp();
     if (k0 + lane < nchunks) sm[a][lane] = maps[a * nchunks + k0 + lane];
@@ -239,9 +264,11 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
       bool done = false;
       if (m.ok) {
         if (!imode || e != m.e) {
-          double cur = imode ? ldexp((double)S, e - 52) : s;
-          if (cur != 0.0 && ilogb(fabs(cur)) == m.e) {
-            S = (long long)ldexp(cur, 52 - m.e);  // exact: cur is a multiple of its ulp
+          double cur = imode ? ss_to_double(S, e) : s;
+          int ce;
+          long long cS;
+          if (ss_from_double(cur, ce, cS) && ce == m.e) {
+            S = cS;  // exact: cur is a multiple of its ulp
             e = m.e;
             imode = true;
           } else {
@@ -262,7 +289,18 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
       long i0 = k * SS_C;
       int n = (int)(min(N, (k + 1) * SS_C) - i0);
       __syncwarp();
-      for (int i = lane; i < n; i += 32) sx[a][i] = pos[3 * (i0 + i) + a];
+      if (pref_k == k) {
+#pragma unroll
+        for (int t = 0; t < SS_PER_LANE; t++) sx[a][lane + 32 * t] = pr[t];
+      } else {
+        for (int i = lane; i < n; i += 32) sx[a][i] = pos[3 * (i0 + i) + a];
+      }
+      pref_k = k + 1;
+#pragma unroll
+      for (int t = 0; t < SS_PER_LANE; t++) {
+        const long i = pref_k * SS_C + lane + 32 * t;
+        pr[t] = i < N ? pos[3 * i + a] : 0.0;
+      }
       __syncwarp();
       for (int b = 0; b < n; b += 32) {
         int cnt = min(32, n - b);
@@ -270,13 +308,11 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
         int c = 0;
         while (c < cnt) {
           if (!imode) {
-            if (s == 0.0 || !isfinite(s)) {
+            if (!ss_from_double(s, e, S)) {
               s = __dadd_rn(s, sx[a][b + c]);
               c++;
               continue;
             }
-            e = ilogb(fabs(s));
-            S = (long long)ldexp(s, 52 - e);
             imode = true;
           }
           bool act = lane >= c && lane < cnt;
@@ -300,7 +336,7 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
             int x = __ffs(bal) - 1;
             long long Sb = __shfl_sync(FULL, Sj, x > 0 ? x - 1 : 0);
             if (x == c) Sb = S;
-            s = __dadd_rn(ldexp((double)Sb, e - 52), sx[a][b + x]);
+            s = __dadd_rn(ss_to_double(Sb, e), sx[a][b + x]);
             imode = false;
             c = x + 1;
           }
@@ -309,7 +345,7 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
     }
   }
   if (lane == 0) {
-    if (imode) s = ldexp((double)S, e - 52);
+    if (imode) s = ss_to_double(S, e);
     out[a] = s;
   }
 }
