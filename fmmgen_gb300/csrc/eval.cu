@@ -402,12 +402,16 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
       t->pz.p, t->perm.p, S, so, p, cr, M, mstr);
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 1, st));
-  // M2M, deepest parents first
+  // M2M, deepest parents first (mixed pass: the eight fixed child-shift
+  // operators, shift.cu; FP64: the contraction engine)
   for (int l = t->nlevels - 2; l >= 0; l--) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
-    fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, M,
-        mstr);
+    if (mixed)
+      TRY(fmm_m2m_tab(t, lo, hi, (float *)(void *)M, mstr, st));
+    else
+      fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+          ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, M,
+          mstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 2, st));
@@ -423,11 +427,14 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
   } else {
     TRY(m2l_p2p<T>(t, ps, S, M, L, mixed, impl, mstr, lstr, dstr, st));
   }
-  // L2L, top-down
+  // L2L, top-down (as M2M: fixed child-shift operators in the mixed pass)
   for (int l = 1; l < t->nlevels; l++) {
     int lo = t->level_off[l], hi = t->level_off[l + 1];
-    fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        ps->l2l, lo, hi, so, p, t->parent.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, L, lstr);
+    if (mixed)
+      TRY(fmm_l2l_tab(t, lo, hi, (float *)(void *)L, lstr, st));
+    else
+      fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+          ps->l2l, lo, hi, so, p, t->parent.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, L, lstr);
   }
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 5, st));

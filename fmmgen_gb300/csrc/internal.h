@@ -176,5 +176,8 @@ int fmm_mlp_adam(float *params, const float *grad, float *m, float *v, int step,
 int fmm_learned_orders(DevTree *t, cudaStream_t st);
 bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops);
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st);
+// M2M of the parents / L2L into the children of cells [lo, hi), FP32 scaled expansions (shift.cu)
+int fmm_m2m_tab(DevTree *t, int lo, int hi, float *M, int mstr, cudaStream_t st);
+int fmm_l2l_tab(DevTree *t, int lo, int hi, float *L, int lstr, cudaStream_t st);
 int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
                int potential, int field, double *F, cudaStream_t st);
