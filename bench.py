@@ -377,8 +377,8 @@ def main():
         model.attach(tree)
 
     def step(precision="mixed"):
-        tree.rebuild(pos)
-        tree.compute_field_fmm(F, potential=a.potential, field=a.field, precision=precision)
+        # the build and the evaluation in one call (fmmgen_tree_build_compute)
+        tree.rebuild_compute(pos, F, potential=a.potential, field=a.field, precision=precision)
 
     phase_sum = {}
 
@@ -443,8 +443,7 @@ def main():
     def e2e_step():
         pos_d.copy_(pos_h, non_blocking=True)
         q_d.copy_(q_h, non_blocking=True)
-        tree.rebuild(pos_d)
-        tree.compute_field_fmm(F, S=q_d, potential=a.potential, field=a.field, precision="mixed")
+        tree.rebuild_compute(pos_d, F, S=q_d, potential=a.potential, field=a.field, precision="mixed")
         F_h.copy_(F, non_blocking=True)
 
     e2e_step()

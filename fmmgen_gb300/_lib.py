@@ -54,6 +54,8 @@ _SIGS = {
     "fmmgen_forest_build": (C.c_int, [_dp, _lp, C.c_int, C.c_long, C.c_int, C.c_double, C.c_int, _vp,
                                       C.POINTER(C.c_void_p)]),
     "fmmgen_tree_compute_field_fmm": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_int, C.c_int, _vp]),
+    "fmmgen_tree_build_compute": (C.c_int, [_dp, _lp, C.c_int, C.c_long, C.c_long, C.c_int, C.c_double, C.c_int, _dp,
+                                            _dp, C.c_int, C.c_int, C.c_int, _vp, C.POINTER(C.c_void_p)]),
     "fmmgen_gpu_direct": (C.c_int, [_dp, _dp, C.c_long, _lp, C.c_long, C.c_int, C.c_int, C.c_int, _dp, _vp]),
     "fmmgen_tree_compute_field_bh": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_int, _vp]),
     "fmmgen_tree_free": (C.c_int, [_vp]),

@@ -202,6 +202,26 @@ int fmmgen_forest_build(const double *pos, const long *sys_off, int nsys, long n
   return ret(rc);
 }
 
+int fmmgen_tree_build_compute(const double *pos, const long *sys_off, int nsys, long N, long ncrit, int order,
+                              double theta, int so, const double *Sv, double *F, int potential, int field,
+                              int precision, void *stream, fmmgen_tree **tree) {
+  g_err.clear();
+  if (!tree || nsys < 1 || (nsys > 1 && !sys_off)) return ret(FMM_ERR_ARG);
+  if (sys_off && sys_off[nsys] != N) return ret(FMM_ERR_ARG);
+  fmmgen_tree *h = *tree;
+  if (!h) h = new fmmgen_tree();
+  h->built = false;
+  h->last_precision = -1;
+  int rc = fmm_tree_build_evaluate(&h->t, pos, N, ncrit, order, theta, so, nsys > 1 ? sys_off : nullptr, nsys, Sv, F,
+                                   potential, field, precision, S(stream));
+  *tree = h;
+  if (rc == FMM_OK) {
+    h->built = true;
+    h->last_precision = precision;
+  }
+  return ret(rc);
+}
+
 int fmmgen_tree_compute_field_fmm(fmmgen_tree *tree, const double *Sv, double *F, int potential, int field,
                                   int precision, void *stream) {
   g_err.clear();

@@ -631,6 +631,136 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
   return FMM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// build + evaluate in one call
+// ---------------------------------------------------------------------------
+// The multipoles need nothing of the M2L classes, so while the build groups
+// the M2L lists by class (highest-priority stream) a second stream stages the
+// particles and runs P2M and M2M.  The M2L follows the classes on the
+// highest-priority stream -- its persistent CTAs take the SMs first -- and the
+// P2P starts beside it on the caller's stream (in the blocks the tuning
+// chose), as in the overlapped pass; L2L, L2P and the final sum follow.  Phase
+// records follow the streams: "M2L" spans the end of M2M to the end of M2L
+// (the class build included), "P2P" the near field's tail after it.
+template <typename T>
+static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, int precision,
+                      int mstr, int lstr, int dstr, cudaStream_t st) {
+  const int p = t->order, so = t->so, nl = t->nleaves;
+  const double *cr = t->cr.p;
+  cudaStream_t sn = t->s_near;
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_fork, st));
+  FMM_CUDA_TRY(cudaStreamWaitEvent(sn, t->ev_fork, 0));
+  TRY(rec(t, 0, sn));
+  if (mixed) TRY(fmm_stage_particles(t, S, sn));
+  fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
+      t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
+      t->pz.p, t->perm.p, S, so, p, cr, M, mstr);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 1, sn));
+  for (int l = t->nlevels - 2; l >= 0; l--) {
+    int lo = t->level_off[l], hi = t->level_off[l + 1];
+    if (mixed)
+      TRY(fmm_m2m_tab(t, lo, hi, (float *)(void *)M, mstr, sn));
+    else
+      fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
+          ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, M,
+          mstr);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 2, sn));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_m, sn));
+  // the classes (the host waits on this stream only), then the M2L
+  FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_fork, 0));
+  TRY(fmm_tree_finish_build(t, t->s_hi));
+  const int impl = m2l_impl(t, precision);
+  t->p2p_first = false;
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_c, t->s_hi));
+  FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_m, 0));
+  const bool learned = t->ord_mode == 2;
+  if (learned) {  // the orders read the near field: P2P first
+    FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
+    TRY(fmm_p2p_launch(t, mixed, S, st));
+    FMM_CUDA_TRY(cudaEventRecord(t->ev_p, st));
+    FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_p, 0));
+  }
+  TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, t->s_hi));
+  TRY(rec(t, 3, t->s_hi));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_join, t->s_hi));
+  if (!learned) {  // beside the M2L, launched after it
+    FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
+    TRY(fmm_p2p_launch(t, mixed, S, st, mixed && impl == M2L_TC && t->tune.overlap == 2));
+  }
+  FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
+  TRY(rec(t, 4, st));
+  for (int l = 1; l < t->nlevels; l++) {
+    int lo = t->level_off[l], hi = t->level_off[l + 1];
+    if (mixed)
+      TRY(fmm_l2l_tab(t, lo, hi, (float *)(void *)L, lstr, st));
+    else
+      fmm_note_launch(), k_l2l<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+          ps->l2l, lo, hi, so, p, t->parent.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, L, lstr);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 5, st));
+  fmm_note_launch(), k_l2p<T><<<fmm_blocks(nl, L2P_WARPS), 32 * L2P_WARPS, 0, st>>>(
+      t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
+      t->pz.p, so, p, cr, L, t->Ffar.p, lstr);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 6, st));
+  return FMM_OK;
+}
+
+int fmm_tree_build_evaluate(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
+                            const long *sys_off, int nsys, const double *S, double *F, int potential, int field,
+                            int precision, cudaStream_t st) {
+  if (!S || !F || (!potential && !field) || precision < 0 || precision > 2) return FMM_ERR_ARG;
+  TRY(fmm_tree_build(t, pos, N, ncrit, order, theta, so, st, sys_off, nsys, true));
+  fmm_graph_release(t);  // a recorded pass belongs to the previous build
+  TRY(side_stream(t));
+  if (!t->s_near) {
+    FMM_CUDA_TRY(cudaStreamCreateWithFlags(&t->s_near, cudaStreamNonBlocking));
+    FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_m, cudaEventDisableTiming));
+    FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_c, cudaEventDisableTiming));
+    FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_p, cudaEventDisableTiming));
+  }
+  const PlanSet *ps = fmm_get_plans(t->order, t->so);
+  if (!ps) return FMM_ERR_CUDA;
+  const bool mixed = precision != 0;
+  t->last_prec = mixed ? 1 : 0;
+  t->pass_potential = potential != 0;
+  const int p = t->order;
+  const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
+  const size_t nc = t->ncells;
+  TRY(fmm_reserve(t->Fnear, 4 * (size_t)t->N));
+  TRY(fmm_reserve(t->Ffar, 4 * (size_t)t->N));
+  int rc;
+  if (mixed) {
+    const int mstr = fmm_stride4((int)msize), lstr = fmm_stride4((int)lsize), dstr = fmm_stride4(fmm_nterms(p));
+    TRY(fmm_reserve(t->Mf, nc * mstr));
+    TRY(fmm_reserve(t->Lf, nc * lstr));
+    TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
+    TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
+    rc = fused_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, precision, mstr, lstr, dstr, st);
+  } else {
+    TRY(fmm_reserve(t->M, nc * msize));
+    TRY(fmm_reserve(t->L, nc * lsize));
+    rc = fused_pass<double>(t, ps, S, t->M.p, t->L.p, false, precision, (int)msize, (int)lsize, fmm_nterms(p), st);
+  }
+  if (rc == FMM_OK && t->eflags) {  // the build's own error, after the near-field stream is done
+    FMM_CUDA_TRY(cudaStreamSynchronize(t->s_near));
+    return (t->eflags & FMM_EFLAG_DEPTH) ? FMM_ERR_DEPTH : FMM_ERR_RANGE;
+  }
+  if (rc) {
+    cudaStreamSynchronize(t->s_near);
+    return rc;
+  }
+  fmm_note_launch(), k_finalize<<<fmm_blocks(t->N, 256), 256, 0, st>>>(t->Fnear.p, t->Ffar.p, t->perm.p, t->N,
+                                                                        potential, field, F);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 7, st));
+  return FMM_OK;
+}
+
 // The M2L and P2P phases alone on the multipoles and staged particles of the
 // last pass (same precision class): the autotuner's timed unit.
 int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st) {

@@ -614,7 +614,7 @@ static int build_lists(DevTree *t, cudaStream_t st);
 static int build_classes(DevTree *t, cudaStream_t st);
 
 int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
-                   cudaStream_t st, const long *sys_off, int nsys) {
+                   cudaStream_t st, const long *sys_off, int nsys, bool defer_classes) {
   if (N < 1 || N >= (1L << 31) - 1 || ncrit < 1 || order < so + 1 || order > FMM_PMAX || so < 0 || so > 1 ||
       !(theta > 0) || !pos || nsys < 1 || (nsys > 1 && !sys_off))
     return FMM_ERR_ARG;
@@ -708,6 +708,12 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
   TRY(rec(t, 3, st));
   TRY(build_lists(t, st));
   TRY(rec(t, 4, st));
+  return defer_classes ? FMM_OK : fmm_tree_finish_build(t, st);
+}
+
+// The M2L translation classes and the end of the build (fmm_tree_build with
+// defer_classes leaves them to this call).
+int fmm_tree_finish_build(DevTree *t, cudaStream_t st) {
   TRY(build_classes(t, st));
   TRY(rec(t, 5, st));
   FMM_CUDA_TRY(cudaMemcpyAsync(&t->eflags, t->d_eflags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -1052,11 +1058,13 @@ int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st) {
 void fmm_tree_destroy(DevTree *t) {
   if (!t) return;
   fmm_graph_release(t);
-  if (t->ev_fork) cudaEventDestroy(t->ev_fork);
-  if (t->ev_join) cudaEventDestroy(t->ev_join);
+  for (cudaEvent_t *e : {&t->ev_fork, &t->ev_join, &t->ev_m, &t->ev_c, &t->ev_p}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
   if (t->s_hi) cudaStreamDestroy(t->s_hi);
-  t->ev_fork = t->ev_join = nullptr;
-  t->s_hi = nullptr;
+  if (t->s_near) cudaStreamDestroy(t->s_near);
+  t->s_hi = t->s_near = nullptr;
   if (t->gstream) cudaStreamDestroy(t->gstream);
   t->gstream = nullptr;
   fmm_release(t->keys); fmm_release(t->keys2); fmm_release(t->perm); fmm_release(t->perm2);

@@ -81,6 +81,41 @@ class Tree:
          self.p2p_interactions) = (int(v) for v in info)
         return self
 
+    def rebuild_compute(self, pos=None, F=None, S=None, potential=True, field=True, precision="mixed",
+                        stream=None):
+        """rebuild(pos) followed by compute_field_fmm(F, S, ...) in one call: the
+        near field and the multipoles run while the build groups the M2L
+        lists by class.  Returns F like compute_field_fmm."""
+        if pos is not None:
+            self.pos = _as_device(pos, (3,))
+            self.N = self.pos.shape[0]
+        if S is not None:
+            self.S = _as_device(S, (sourcesize(self.source_order),))
+        if self.S is None or self.S.shape[0] != self.N:
+            raise ValueError("S must hold one source per particle")
+        os_ = outputsize(potential, field)
+        host_out = F is not None and not (isinstance(F, torch.Tensor) and F.is_cuda)
+        Fd = F if (F is not None and not host_out) else torch.empty((self.N, os_), dtype=torch.float64,
+                                                                     device=self.pos.device)
+        if Fd.dtype != torch.float64 or not Fd.is_contiguous() or Fd.numel() != self.N * os_:
+            raise ValueError("F must be a contiguous float64 [N][OUTPUTSIZE] array")
+        off = self.sys_off
+        if off is not None and off[-1] != self.N:
+            raise ValueError("the system offsets must end at N")
+        check(lib().fmmgen_tree_build_compute(
+            C.c_void_p(self.pos.data_ptr()), off.ctypes.data if off is not None else None,
+            len(off) - 1 if off is not None else 1, self.N, self.ncrit, self.order, self.theta, self.source_order,
+            C.c_void_p(self.S.data_ptr()), C.c_void_p(Fd.data_ptr()), int(potential), int(field),
+            PRECISIONS[precision], _stream_ptr(stream), C.byref(self._h)))
+        info = np.zeros(9, dtype=np.int64)
+        check(lib().fmmgen_tree_info(self._h, info.ctypes.data))
+        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _,
+         self.p2p_interactions) = (int(v) for v in info)
+        if host_out:
+            F[...] = Fd.reshape(np.shape(F)).cpu().numpy() if isinstance(F, np.ndarray) else Fd.cpu()
+            return F
+        return Fd
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

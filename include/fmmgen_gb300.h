@@ -158,6 +158,15 @@ int fmmgen_root_box_noalloc(const double *pos, long N, double *root4, void *stre
 /* Introspection (host outputs; synchronises).
  * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions]. */
 int fmmgen_tree_info(fmmgen_tree *tree, long *info);
+/* build_tree + Tree::compute_field_fmm in one call (fmmgen_tree_build /
+ * fmmgen_forest_build, then fmmgen_tree_compute_field_fmm, on the same
+ * handle): the near field and the multipoles are computed on a second stream
+ * while the build groups the M2L lists by class, and the M2L runs beside the
+ * near field's tail.  sys_off / nsys as in fmmgen_forest_build (NULL, 1: one
+ * system).  The handle is then built, as after fmmgen_tree_build. */
+int fmmgen_tree_build_compute(const double *pos, const long *sys_off, int nsys, long N, long ncrit, int order,
+                              double theta, int source_order, const double *S, double *F, int potential, int field,
+                              int precision, void *stream, fmmgen_tree **tree);
 /* Tree::compute_field_bh (example/tree.cpp:273-293): FP64 P2M and M2M, then
  * for every particle the walk of evaluate_M2P_and_P2P
  * (example/calculate.cpp:266-314) from its system's root: a child c of an
