@@ -652,6 +652,7 @@ static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L
   FMM_CUDA_TRY(cudaStreamWaitEvent(sn, t->ev_fork, 0));
   TRY(rec(t, 0, sn));
   if (mixed) TRY(fmm_stage_particles(t, S, sn));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_s, sn));
   fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
       t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
       t->pz.p, t->perm.p, S, so, p, cr, M, mstr);
@@ -679,6 +680,7 @@ static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L
   const bool learned = t->ord_mode == 2;
   if (learned) {  // the orders read the near field: P2P first
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
+    FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_s, 0));  // the staged particles
     TRY(fmm_p2p_launch(t, mixed, S, st));
     FMM_CUDA_TRY(cudaEventRecord(t->ev_p, st));
     FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_p, 0));
@@ -688,6 +690,7 @@ static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L
   FMM_CUDA_TRY(cudaEventRecord(t->ev_join, t->s_hi));
   if (!learned) {  // beside the M2L, launched after it
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
+    FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_s, 0));
     TRY(fmm_p2p_launch(t, mixed, S, st, mixed && impl == M2L_TC && t->tune.overlap == 2));
   }
   FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
@@ -718,10 +721,14 @@ int fmm_tree_build_evaluate(DevTree *t, const double *pos, long N, long ncrit, i
   fmm_graph_release(t);  // a recorded pass belongs to the previous build
   TRY(side_stream(t));
   if (!t->s_near) {
-    FMM_CUDA_TRY(cudaStreamCreateWithFlags(&t->s_near, cudaStreamNonBlocking));
+    // the multipoles are on the M2L's critical path: highest priority too
+    int lo = 0, hi = 0;
+    FMM_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    FMM_CUDA_TRY(cudaStreamCreateWithPriority(&t->s_near, cudaStreamNonBlocking, hi));
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_m, cudaEventDisableTiming));
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_c, cudaEventDisableTiming));
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_p, cudaEventDisableTiming));
+    FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_s, cudaEventDisableTiming));
   }
   const PlanSet *ps = fmm_get_plans(t->order, t->so);
   if (!ps) return FMM_ERR_CUDA;

@@ -50,7 +50,7 @@ struct DevTree {
   DevBuf<uint64_t> keys, keys2;
   DevBuf<uint32_t> perm, perm2;           // sorted position -> caller's particle index
   DevBuf<double> px, py, pz;              // sorted positions (FP64)
-  DevBuf<float4> phi4, plo4, sdip;        // FP32 P2P staging: (hi offset from leaf centre, q), lo offset, dipole
+  DevBuf<float4> phi4, plo4, sdip;        // FP32 P2P staging: (hi offset from root centre, q), (lo, index), dipole
   DevBuf<float2> levf;                    // per-level half-width as an FP32 (hi, lo) pair
   // cells, level-major, Morton order within a level
   DevBuf<double> cx, cy, cz;
@@ -78,7 +78,7 @@ struct DevTree {
   cudaStream_t s_hi = nullptr;            // the side stream (highest priority)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t s_near = nullptr;          // build_evaluate: P2M, M2M and P2P beside the class build
-  cudaEvent_t ev_m = nullptr, ev_c = nullptr, ev_p = nullptr;
+  cudaEvent_t ev_m = nullptr, ev_c = nullptr, ev_p = nullptr, ev_s = nullptr;
   int grouping_built = 0;                 // grouping m2l_order holds
   DevBuf<int> p2p_off, p2p_src;
   // M2L translation classes: operator vectors D^(k)(d/s_target), |k| <= order

@@ -34,13 +34,14 @@ def test_fused_equals_two_calls(fg, precision, so, p):
     b.times()  # phase records of the fused pass are readable
 
 
-def test_fused_with_tuning_and_learned_orders(fg):
+@pytest.mark.parametrize("overlap", [0, 2])
+def test_fused_with_tuning_and_learned_orders(fg, overlap):
     from fmmgen_gb300 import learned
 
     n = 40000
     pos, S = system(5, n)
-    a = fg.build_tree(pos, S, n, 64, 8, 0.5).set_tune(0, 3, 0, 2)
-    b = fg.build_tree(pos, S, n, 64, 8, 0.5).set_tune(0, 3, 0, 2)
+    a = fg.build_tree(pos, S, n, 64, 8, 0.5).set_tune(0, 3, 0, overlap)
+    b = fg.build_tree(pos, S, n, 64, 8, 0.5).set_tune(0, 3, 0, overlap)
     assert np.array_equal(a.compute_field_fmm(precision="mixed").cpu().numpy(),
                           b.rebuild_compute(pos, precision="mixed").cpu().numpy())
     m = learned.OrderModel.load()
@@ -51,16 +52,19 @@ def test_fused_with_tuning_and_learned_orders(fg):
     assert np.array_equal(Fa, Fb) and np.array_equal(a.m2l_orders(), b.m2l_orders())
 
 
-def test_fused_forest(fg):
+@pytest.mark.parametrize("so,overlap", [(0, 0), (0, 2), (1, 2)])
+def test_fused_forest(fg, so, overlap):
     sizes = [3000, 40, 12000, 700]
     rng = np.random.default_rng(9)
     pos = torch.tensor(np.concatenate([rng.uniform(0, 1, (k, 3)) + 2 * i for i, k in enumerate(sizes)]),
                        device="cuda")
-    S = torch.tensor(rng.uniform(-1, 1, (sum(sizes), 1)), device="cuda")
-    a = fg.build_forest(pos, S, sizes, 32, 6, 0.5)
-    b = fg.build_forest(pos, S, sizes, 32, 6, 0.5)
-    assert np.array_equal(a.compute_field_fmm(precision="mixed").cpu().numpy(),
-                          b.rebuild_compute(pos, precision="mixed").cpu().numpy())
+    S = torch.tensor(rng.uniform(-1, 1, (sum(sizes), 1 if so == 0 else 3)), device="cuda")
+    a = fg.build_forest(pos, S, sizes, 32, 6, 0.5, source_order=so).set_tune(0, 0, 0, overlap)
+    b = fg.build_forest(pos, S, sizes, 32, 6, 0.5, source_order=so).set_tune(0, 0, 0, overlap)
+    c = fg.build_forest(pos, S, sizes, 32, 6, 0.5, source_order=so)  # default choices, separate calls
+    Fa = a.compute_field_fmm(precision="mixed").cpu().numpy()
+    assert np.array_equal(Fa, b.rebuild_compute(pos, precision="mixed").cpu().numpy())
+    assert np.array_equal(Fa, c.compute_field_fmm(precision="mixed").cpu().numpy())
 
 
 def test_fused_reports_build_errors(fg):
