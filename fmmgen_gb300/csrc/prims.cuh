@@ -112,11 +112,14 @@ template <typename T> int fmm_scan(const T *in, T *out, size_t n, T *total, T *t
 
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort, 8-bit digits.  Each block owns a tile of RS_TILE
-// consecutive elements; ranks inside a tile follow element order, so equal
-// digits keep their input order (stability across passes).
+// consecutive elements.  The scatter ranks the tile's elements by digit in
+// element order (so equal digits keep their input order: stability across
+// passes), reorders the tile in shared memory, and then writes it out in that
+// order: consecutive threads write consecutive positions of one digit's run, so
+// the stores coalesce instead of landing one per bucket.
 // ---------------------------------------------------------------------------
 #define RS_BS 256
-#define RS_ROUNDS 16
+#define RS_ROUNDS 12
 #define RS_TILE (RS_BS * RS_ROUNDS)
 
 template <typename K> __global__ void k_rs_hist(const K *keys, size_t n, int shift, uint32_t *hist, int nb) {
@@ -133,43 +136,70 @@ template <typename K> __global__ void k_rs_hist(const K *keys, size_t n, int shi
 }
 
 template <typename K>
-__global__ void k_rs_scatter(const K *kin, const uint32_t *vin, K *kout, uint32_t *vout,
-                             size_t n, int shift, const uint32_t *offs, int nb) {
-  __shared__ uint32_t s_run[256];
-  __shared__ uint32_t s_wh[RS_BS / 32][256];
+__global__ void __launch_bounds__(RS_BS) k_rs_scatter(const K *kin, const uint32_t *vin, K *kout, uint32_t *vout,
+                                                      size_t n, int shift, const uint32_t *offs, int nb) {
+  __shared__ uint32_t s_run[256];             // per digit: elements of the tile ranked so far
+  __shared__ uint32_t s_wh[RS_BS / 32][256];  // per round: each warp's first rank of a digit
+  __shared__ uint32_t s_goff[256];            // per digit: global position of the tile's run - its start in the tile
+  __shared__ K s_k[RS_TILE];
+  __shared__ uint32_t s_v[RS_TILE];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  s_run[t] = offs[(size_t)t * nb + blockIdx.x];
   const unsigned lt = (1u << lane) - 1u;
-  size_t base = (size_t)blockIdx.x * RS_TILE;
+  const size_t base = (size_t)blockIdx.x * RS_TILE;
+  s_run[t] = 0;
+  K kr[RS_ROUNDS];
+  uint32_t vr[RS_ROUNDS], rk[RS_ROUNDS];
+#pragma unroll
   for (int r = 0; r < RS_ROUNDS; r++) {
 #pragma unroll
     for (int w = 0; w < RS_BS / 32; w++) s_wh[w][t] = 0;
     __syncthreads();
-    size_t i = base + (size_t)r * RS_BS + t;
-    bool valid = i < n;
+    const size_t i = base + (size_t)r * RS_BS + t;
+    const bool valid = i < n;
     K k = 0;
     uint32_t v = 0, d = 256;
     if (valid) { k = kin[i]; v = vin[i]; d = (uint32_t)((k >> shift) & 255u); }
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    int rank = __popc(peers & lt);
-    int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) s_wh[warp][d] = __popc(peers);
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int rank = __popc(peers & lt);
+    if (valid && lane == __ffs(peers) - 1) s_wh[warp][d] = __popc(peers);
     __syncthreads();
-    uint32_t run = s_run[t], acc = 0;
+    const uint32_t run = s_run[t];
+    uint32_t acc = 0;
 #pragma unroll
     for (int w = 0; w < RS_BS / 32; w++) {
-      uint32_t c = s_wh[w][t];
+      const uint32_t c = s_wh[w][t];
       s_wh[w][t] = run + acc;
       acc += c;
     }
     s_run[t] = run + acc;
     __syncthreads();
-    if (valid) {
-      uint32_t pos = s_wh[warp][d] + rank;
-      kout[pos] = k;
-      vout[pos] = v;
+    kr[r] = k;
+    vr[r] = v;
+    rk[r] = valid ? s_wh[warp][d] + rank : 0u;  // rank among the tile's elements of digit d
+    __syncthreads();                             // before the next round clears s_wh
+  }
+  // start of each digit's run in the reordered tile, and its global offset
+  uint32_t tot;
+  const uint32_t start = block_exclusive<uint32_t>(s_run[t], &tot);
+  s_goff[t] = offs[(size_t)t * nb + blockIdx.x] - start;
+  s_wh[0][t] = start;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RS_ROUNDS; r++) {
+    if (base + (size_t)r * RS_BS + t < n) {
+      const uint32_t d = (uint32_t)((kr[r] >> shift) & 255u);
+      const uint32_t lp = s_wh[0][d] + rk[r];
+      s_k[lp] = kr[r];
+      s_v[lp] = vr[r];
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  const int tile_n = (int)min((size_t)RS_TILE, n - base);
+  for (int j = t; j < tile_n; j += RS_BS) {
+    const K k = s_k[j];
+    const uint32_t pos = s_goff[(k >> shift) & 255u] + (uint32_t)j;
+    kout[pos] = k;
+    vout[pos] = s_v[j];
   }
 }
 

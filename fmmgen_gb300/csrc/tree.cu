@@ -300,6 +300,7 @@ __global__ void k_leaf_compact(int ncells, long ncrit, const int *pcount, const 
 // ---------------------------------------------------------------------------
 // dual-tree walk (example/calculate.cpp:81-133), breadth-first
 // ---------------------------------------------------------------------------
+#define WALK_BS 256
 struct WalkCells {
   const double *cx, *cy, *cz, *crmax;
   const unsigned char *mask, *clevel;
@@ -364,29 +365,51 @@ __global__ void k_root_pairs(int nsys, int *fa, int *fb) {
   if (s < nsys) fa[s] = fb[s] = s;
 }
 
-__global__ void k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t nf, double theta, U3 *cnt,
-                             unsigned char *dec) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nf) return;
-  int A = fa[i], B = fb[i];
-  int d = walk_decide(W, A, B, theta);
-  dec[i] = (unsigned char)d;
+// Output slots of a decided pair: one M2L pair, one P2P pair, or the split
+// cell's children as new frontier pairs.
+__device__ __forceinline__ U3 walk_slots(const WalkCells &W, int A, int B, int d) {
   U3 c{0u, 0u, 0u};
   if (d == 0) c.x = 1;
   else if (d == 1) c.y = 1;
-  else if (d == 2) c.z = __popc((unsigned)W.mask[A]);
-  else c.z = __popc((unsigned)W.mask[B]);
-  cnt[i] = c;
+  else c.z = __popc((unsigned)W.mask[d == 2 ? A : B]);
+  return c;
 }
 
-__global__ void k_walk_write(WalkCells W, const int *fa, const int *fb, uint32_t nf, const unsigned char *dec,
-                             const U3 *off, U3 base, int *m2l_src, int *m2l_tgt, int *p2p_tgt, int *p2p_src,
-                             int *na, int *nb) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// Decisions of the frontier pairs, and each block's slot totals (the per-pair
+// slots are recomputed by k_walk_write, so only the block totals are scanned).
+__global__ void __launch_bounds__(WALK_BS) k_walk_count(WalkCells W, const int *fa, const int *fb, uint32_t nf,
+                                                        double theta, U3 *bsum, unsigned char *dec) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  U3 c{0u, 0u, 0u};
+  if (i < nf) {
+    const int A = fa[i], B = fb[i];
+    const int d = walk_decide(W, A, B, theta);
+    dec[i] = (unsigned char)d;
+    c = walk_slots(W, A, B, d);
+  }
+  U3 tot;
+  block_exclusive<U3>(c, &tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+// Writes each pair's outputs at its block's offset (boff, the scanned block
+// totals) plus its rank in the block: the walk order of the sequential scan.
+__global__ void __launch_bounds__(WALK_BS) k_walk_write(WalkCells W, const int *fa, const int *fb, uint32_t nf,
+                                                        const unsigned char *dec, const U3 *boff, U3 base,
+                                                        int *m2l_src, int *m2l_tgt, int *p2p_tgt, int *p2p_src,
+                                                        int *na, int *nb) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  int A = 0, B = 0, d = 0;
+  U3 c{0u, 0u, 0u};
+  if (i < nf) {
+    A = fa[i];
+    B = fb[i];
+    d = dec[i];
+    c = walk_slots(W, A, B, d);
+  }
+  U3 tot;
+  const U3 o = boff[blockIdx.x] + block_exclusive<U3>(c, &tot);
   if (i >= nf) return;
-  int A = fa[i], B = fb[i];
-  int d = dec[i];
-  U3 o = off[i];
   if (d == 0) {
     m2l_src[base.x + o.x] = B;
     m2l_tgt[base.x + o.x] = A;
@@ -886,15 +909,15 @@ static int build_lists(DevTree *t, cudaStream_t st) {
   fmm_note_launch(), k_root_pairs<<<fmm_blocks(nf, 256), 256, 0, st>>>((int)nf, t->fa.p, t->fb.p);
   FMM_CUDA_TRY(cudaGetLastError());
   while (nf > 0) {
-    size_t need = (size_t)nf * sizeof(U3) + fmm_scan_tmp_elems<U3>(nf) * sizeof(U3) + 2 * sizeof(U3);
+    const unsigned nblk = fmm_blocks(nf, WALK_BS);
+    size_t need = (size_t)nblk * sizeof(U3) + fmm_scan_tmp_elems<U3>(nblk) * sizeof(U3) + 2 * sizeof(U3);
     if ((rc = tmp_reserve(t, need))) break;
-    U3 *cnt = (U3 *)t->tmp.p;
-    U3 *tot = cnt + nf;
+    U3 *cnt = (U3 *)t->tmp.p;  // per block: slot totals, then their exclusive scan
+    U3 *tot = cnt + nblk;
     U3 *stmp = tot + 1;
     if ((rc = fmm_reserve(t->wdec, nf))) break;
-    fmm_note_launch(), k_walk_count<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt,
-                                                                        t->wdec.p);
-    if ((rc = fmm_scan<U3>(cnt, cnt, nf, tot, stmp, st))) break;
+    fmm_note_launch(), k_walk_count<<<nblk, WALK_BS, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->theta, cnt, t->wdec.p);
+    if ((rc = fmm_scan<U3>(cnt, cnt, nblk, tot, stmp, st))) break;
     cudaMemcpyAsync(h_tot, tot, sizeof(U3), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
     U3 T = *h_tot;
@@ -903,7 +926,7 @@ static int build_lists(DevTree *t, cudaStream_t st) {
         (rc = fmm_reserve(t->fa2, T.z + 1)) || (rc = fmm_reserve(t->fb2, T.z + 1)))
       break;
     U3 base{(uint32_t)nm2l, (uint32_t)np2p, 0u};
-    fmm_note_launch(), k_walk_write<<<fmm_blocks(nf, 256), 256, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->wdec.p, cnt, base,
+    fmm_note_launch(), k_walk_write<<<nblk, WALK_BS, 0, st>>>(W, t->fa.p, t->fb.p, nf, t->wdec.p, cnt, base,
                                                      m2l_src_raw.p, m2l_tgt_raw.p, p2p_tgt_raw.p, p2p_src_raw.p,
                                                      t->fa2.p, t->fb2.p);
     if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
