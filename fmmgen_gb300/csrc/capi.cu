@@ -327,6 +327,7 @@ int fmmgen_tree_export_lists(fmmgen_tree *tree, unsigned long long *m2l, unsigne
   g_err.clear();
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   DevTree &t = tree->t;
+  if (int rc = fmm_m2l_csr(&t, 0)) return ret(rc);
   FMM_CUDA_TRY(cudaDeviceSynchronize());
   size_t nc = t.ncells;
   std::vector<uint64_t> cid;

@@ -507,6 +507,8 @@ template <typename T>
 static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed, int impl, int mstr, int lstr,
                      int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so, nc = t->ncells;
+  // every M2L but the tensor cores' reads the target lists
+  if (t->ord_mode != 0 || !(mixed && impl == M2L_TC)) TRY(fmm_m2l_csr(t, st));
   if (t->ord_mode != 0) {
     // per-pair orders: predicted now from this pass's multipoles, or given
     if (t->ord_mode == 2) TRY(fmm_learned_orders(t, st));

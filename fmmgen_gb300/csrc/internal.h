@@ -65,7 +65,9 @@ struct DevTree {
   DevBuf<int> leaf_cells;                 // leaf cell indices
   DevBuf<int> cell_leaf;                  // cell -> leaf ordinal or -1
   // interaction lists, grouped by target cell (CSR over cells)
-  DevBuf<int> m2l_off, m2l_src, m2l_cls;  // per target: sorted by class
+  DevBuf<int> m2l_off, m2l_src, m2l_cls;  // per target: sorted by class (built on demand: fmm_m2l_csr)
+  DevBuf<int> m2l_cls_raw;                // class of each walk-order M2L pair
+  uint64_t csr_serial = ~0ull;            // build whose target lists m2l_off/src/cls hold
   DevBuf<int> m2l_order;                  // cells in M2L processing order (level, then the grouping below)
   // M2L choices (set by fmmgen_tree_set_tune / the autotuner; -1 / 0: the default rules)
   struct M2LTune {
@@ -99,6 +101,7 @@ struct DevTree {
   DevBuf<int> m2l_tgt_raw, m2l_src_raw;   // walk output in frontier order (kept between builds)
   DevBuf<int> p2p_tgt_raw, p2p_src_raw;
   uint32_t *h_pinned = nullptr;           // 64 pinned host bytes for count readbacks
+#define FMM_PINNED_SCRATCH 8              // h_pinned word 8: the tensor-core schedule's step count
 #define FMM_PINNED_TCERR 12               // h_pinned words 12..15: last tensor-core M2L error flags, class steps
   // tensor-core M2L operands (m2l_tc.cu)
   DevBuf<unsigned char> tc_T;             // split, swizzled operator records per class
@@ -107,7 +110,8 @@ struct DevTree {
   DevBuf<uint32_t> d_tcerr;               // kernel timeout flags
   uint64_t build_serial = 0, tc_serial = ~0ull;  // tc_T belongs to the build with this serial
   DevBuf<int> tc_sched_off;               // class-step schedule of the tensor-core M2L tiles
-  DevBuf<unsigned> tc_sched_cls, tc_sched_mask;
+  DevBuf<unsigned> tc_sched_cls, tc_bitmap, tc_rank;
+  DevBuf<int> tc_stab, tc_pos;            // per class step: each tile row's source (-1: none); row of each cell
   uint64_t sched_serial = ~0ull, sched_version = ~0ull;  // ... of this build and cell order
   uint64_t order_version = 0;             // incremented whenever m2l_order is rewritten
   int tc_order = -1, tc_so = -1;          // ... and to this expansion order and source order
@@ -168,6 +172,9 @@ bool fmm_m2l_tc_supported(int p, int so);
 int fmm_m2l_tc_max_slots(int p, int so);       // 0 when the tensor-core M2L does not support (p, so)
 bool fmm_m2l_gen_supported(int p, int so);     // generated CUDA-core M2L kernels exist
 int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st);
+// the M2L pairs grouped by target and sorted by class within a target (CSR
+// m2l_off / m2l_src / m2l_cls), once per build, for the kernels that read them
+int fmm_m2l_csr(DevTree *t, cudaStream_t st);
 int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st);  // M2L + P2P alone (after a pass)
 int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand4, float *cand_ms,
                  int *ncand, cudaStream_t st);

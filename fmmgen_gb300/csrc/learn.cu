@@ -468,6 +468,7 @@ static int tol_scale(DevTree *t, cudaStream_t st) {
 }
 
 int fmm_order_features(DevTree *t, double eps, float *feat, cudaStream_t st) {
+  if (int rc = fmm_m2l_csr(t, st)) return rc;
   if (t->last_prec < 0) return FMM_ERR_STATE;  // the features read the multipoles and near field of a pass
   if (t->nm2l == 0) return FMM_OK;
   TRY_(mnorms(t, st));
@@ -480,6 +481,7 @@ int fmm_order_features(DevTree *t, double eps, float *feat, cudaStream_t st) {
 }
 
 int fmm_order_labels(DevTree *t, double eps, unsigned char *label, float *errq, cudaStream_t st) {
+  if (int rc = fmm_m2l_csr(t, st)) return rc;
   if (t->last_prec != 0) return FMM_ERR_STATE;  // needs the FP64 multipoles
   if (t->nm2l == 0) return FMM_OK;
   TRY_(label_tables());
@@ -532,6 +534,7 @@ int fmm_mlp_adam(float *params, const float *grad, float *m, float *v, int step,
 // the features of every M2L pair from this pass's multipoles and near field,
 // then the orders (into t->m2l_ord).
 int fmm_learned_orders(DevTree *t, cudaStream_t st) {
+  if (int rc = fmm_m2l_csr(t, st)) return rc;
   TRY_(fmm_reserve(t->feat, (size_t)(t->nm2l > 0 ? t->nm2l : 1) * MLP_IN));
   TRY_(fmm_reserve(t->m2l_ord, t->nm2l > 0 ? t->nm2l : 1));
   TRY_(fmm_order_features(t, t->model_eps, t->feat.p, st));

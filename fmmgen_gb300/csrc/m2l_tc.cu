@@ -26,9 +26,11 @@
 // Tiles take 128 cells of one level and one octant-within-parent, parents in
 // Morton order: those cells have near-identical interaction lists, so a tile
 // visits ~1.4x the classes of one list.  The class steps of every tile (the
-// sorted union of its rows' classes, and which rows have a source in each) are
-// computed once per build (k_tc_sched): the kernel's warps then follow that
-// schedule independently, coupled only through mbarriers.
+// sorted union of its rows' classes) and each step's source per row (-1 for a
+// row without a source in the class) are scattered once per build straight
+// from the walk-order pairs, with no sort (k_tc_bitmap .. k_tc_scatter): the
+// kernel's warps then follow that schedule independently, coupled only
+// through mbarriers.
 //
 // Per CTA (one per SM, persistent), 17 warps:
 //  * warps 0-7 gather the source rows of each (class, 64-term K-block) step
@@ -51,6 +53,7 @@
 #include <cuda_fp16.h>
 #include <vector>
 #include "internal.h"
+#include "prims.cuh"
 
 namespace {
 
@@ -75,10 +78,9 @@ constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
 struct TcParams {
   const int *order;               // cells in M2L processing order
   int ncells, ntiles;
-  const int *off, *src, *cls;     // class-sorted M2L lists (CSR over targets)
   const int *sched_off;           // [ntiles + 1] class steps of each tile
   const unsigned *sched_cls;      // [steps] class of the step
-  const unsigned *sched_mask;     // [steps][4] rows (bit lane of word quarter) with a source in it
+  const int *stab;                // [steps][128] source cell of each tile row in the step, -1: none
   const __half *Mh, *Ml;          // scaled, split source multipoles, row stride kpad
   const int *mexp;                // per cell: row scale exponent (M~ = 2^mexp (Mh + Ml))
   const unsigned char *T;         // per class: split, swizzled operator chunks, then column scales
@@ -326,24 +328,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
     uint32_t g = 0, u = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < P.ntiles && ok; tile += gridDim.x) {
-      const int rr = tile * TC_ROWS + row;
-      const int A = rr < P.ncells ? P.order[rr] : -1;
-      int k = 0, kend = 0;
-      if (A >= 0) {
-        k = P.off[A];
-        kend = P.off[A + 1];
-      }
-      // the row's next source, loaded a step before it is needed
-      int hsrc = k < kend ? P.src[k] : 0;
-      const int s1 = P.sched_off[tile + 1];
-      for (int st = P.sched_off[tile]; st < s1; st++, u++) {
+      const int s0 = P.sched_off[tile], s1 = P.sched_off[tile + 1];
+      // the row's source in the next step, loaded a step before it is needed
+      int hsrc = s0 < s1 ? P.stab[(size_t)s0 * TC_ROWS + row] : -1;
+      for (int st = s0; st < s1; st++, u++) {
         const unsigned c = P.sched_cls[st];
-        const bool mine = (P.sched_mask[4 * st + quarter] >> lane) & 1u;
-        const int mysrc = mine ? hsrc : -1;
-        if (mine) {
-          k++;
-          hsrc = k < kend ? P.src[k] : 0;
-        }
+        const int mysrc = hsrc;
+        if (st + 1 < s1) hsrc = P.stab[(size_t)(st + 1) * TC_ROWS + row];
         for (int kb = 0; kb < P.nkb; kb++) {
           const int slot = (int)(g % (uint32_t)P.nslots);
           const uint32_t use = g / (uint32_t)P.nslots;
@@ -416,22 +407,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
       const int A = rr < P.ncells ? P.order[rr] : -1;
       float *Lrow = A >= 0 ? P.L + (size_t)A * P.lstride + half * HALF : nullptr;
       const int ncol = min(HALF, P.lsize - half * HALF);  // stored columns of this half
-      int k = 0, kend = 0;
-      if (A >= 0) {
-        k = P.off[A];
-        kend = P.off[A + 1];
-      }
-      int hsrc = k < kend ? P.src[k] : 0;
 #pragma unroll
       for (int i = 0; i < HALF; i++) acc[i] = 0.f;
-      const int s1 = P.sched_off[tile + 1];
-      for (int st = P.sched_off[tile]; st < s1; st++, u++) {
-        const bool mine = (P.sched_mask[4 * st + quarter] >> lane) & 1u;
+      const int s0 = P.sched_off[tile], s1 = P.sched_off[tile + 1];
+      int hsrc = s0 < s1 ? P.stab[(size_t)s0 * TC_ROWS + row] : -1;
+      for (int st = s0; st < s1; st++, u++) {
+        const bool mine = hsrc >= 0;
         const int e = mine ? P.mexp[hsrc] : 0;
-        if (mine) {
-          k++;
-          hsrc = k < kend ? P.src[k] : 0;
-        }
+        if (st + 1 < s1) hsrc = P.stab[(size_t)(st + 1) * TC_ROWS + row];
         if (!fold<HALF>(acc, tlane, half * HALF, u, e, mine, accfull0, accempty0, colfull0, cs)) {
           ok = false;
           break;
@@ -613,70 +596,71 @@ __global__ void k_tc_operators(const double *D64, const int *key4, int ncls, TcP
   }
 }
 
-// Class steps of every tile: the sorted union of its rows' class-sorted
-// lists, as a bitmap over the classes in shared memory (one block of 128
-// threads per tile, thread = row).  Counting pass: count[tile] = classes in
-// the union.  Writing pass: step st of a class is its rank in the bitmap; every
-// list entry sets its row's bit in the step's mask (zeroed before) and the
-// step's class.
+// Class steps of every tile, from the walk-order M2L pairs (tgt, src, cls):
+//  k_tc_pos     row of each cell in the processing order;
+//  k_tc_bitmap  per tile, a bitmap over the classes of its rows' pairs;
+//  k_tc_rank    per tile, the exclusive prefix of the words' popcounts (the
+//               step of a class is its rank in the tile's bitmap) and the
+//               tile's step count;
+//  k_tc_steps   the class of every step;
+//  k_tc_scatter the source of every pair into its (step, row) slot.
+// The steps of a tile are its classes in increasing order, as the union of
+// its rows' class-sorted lists would give.
 #define TC_SCHED_MAXW 8192  // bitmap words: classes up to 262,144
-__device__ __forceinline__ void tc_sched_bitmap(const int *order, int ncells, const int *off, const int *cls,
-                                                int nwords, unsigned *bm, int &k0, int &k1) {
-  const int tile = blockIdx.x, r = threadIdx.x;
-  for (int i = r; i < nwords; i += TC_ROWS) bm[i] = 0u;
-  __syncthreads();
-  const int rr = tile * TC_ROWS + r;
-  const int A = rr < ncells ? order[rr] : -1;
-  k0 = A >= 0 ? off[A] : 0;
-  k1 = A >= 0 ? off[A + 1] : 0;
-  for (int k = k0; k < k1; k++) {
-    const unsigned c = (unsigned)cls[k];
-    atomicOr(bm + (c >> 5), 1u << (c & 31));
-  }
-  __syncthreads();
+__global__ void k_tc_pos(const int *order, int ncells, int *pos) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < ncells) pos[order[r]] = r;
 }
 
-__global__ void __launch_bounds__(TC_ROWS) k_tc_sched_count(const int *order, int ncells, const int *off,
-                                                            const int *cls, int nwords, int *count) {
-  extern __shared__ unsigned bm[];
-  __shared__ int part[TC_ROWS / 32];
-  int k0, k1;
-  tc_sched_bitmap(order, ncells, off, cls, nwords, bm, k0, k1);
-  int n = 0;
-  for (int i = threadIdx.x; i < nwords; i += TC_ROWS) n += __popc(bm[i]);
-  n = __reduce_add_sync(0xffffffffu, n);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = n;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int tot = 0;
-    for (int i = 0; i < TC_ROWS / 32; i++) tot += part[i];
-    count[blockIdx.x] = tot;
-  }
+__global__ void k_tc_bitmap(const int *tgt, const int *cls, long n, const int *pos, int nwords, unsigned *bm) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const unsigned c = (unsigned)cls[k];
+  unsigned *w = bm + (size_t)(pos[tgt[k]] / TC_ROWS) * nwords + (c >> 5);
+  const unsigned bit = 1u << (c & 31);
+  if (!(*(volatile unsigned *)w & bit)) atomicOr(w, bit);  // most bits are set already: read first
 }
 
-__global__ void __launch_bounds__(TC_ROWS) k_tc_sched_write(const int *order, int ncells, const int *off,
-                                                            const int *cls, int nwords, const int *sched_off,
-                                                            unsigned *cls_out, unsigned *mask_out) {
-  extern __shared__ unsigned bm[];  // [nwords] bitmap, then [nwords] rank of each word's first class
-  unsigned *rank = bm + nwords;
-  int k0, k1;
-  tc_sched_bitmap(order, ncells, off, cls, nwords, bm, k0, k1);
-  if (threadIdx.x == 0) {  // exclusive prefix of the word popcounts
-    unsigned tot = 0;
-    for (int i = 0; i < nwords; i++) {
-      rank[i] = tot;
-      tot += __popc(bm[i]);
+// one block per tile
+__global__ void k_tc_rank(const unsigned *bm, int nwords, unsigned *rank, int *count) {
+  const unsigned *b = bm + (size_t)blockIdx.x * nwords;
+  unsigned *rk = rank + (size_t)blockIdx.x * nwords;
+  const int per = (nwords + blockDim.x - 1) / blockDim.x, w0 = threadIdx.x * per;
+  unsigned n = 0;
+  for (int i = 0; i < per && w0 + i < nwords; i++) n += __popc(b[w0 + i]);
+  unsigned tot;
+  unsigned run = block_exclusive<unsigned>(n, &tot);
+  for (int i = 0; i < per && w0 + i < nwords; i++) {
+    rk[w0 + i] = run;
+    run += __popc(b[w0 + i]);
+  }
+  if (threadIdx.x == 0) count[blockIdx.x] = (int)tot;
+}
+
+// one block per tile, a thread per bitmap word
+__global__ void k_tc_steps(const unsigned *bm, const unsigned *rank, int nwords, const int *sched_off,
+                           unsigned *cls_out) {
+  const size_t o = (size_t)blockIdx.x * nwords;
+  for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
+    unsigned m = bm[o + w];
+    unsigned st = (unsigned)sched_off[blockIdx.x] + rank[o + w];
+    while (m) {
+      const int b = __ffs(m) - 1;
+      cls_out[st++] = 32u * (unsigned)w + (unsigned)b;
+      m &= m - 1;
     }
   }
-  __syncthreads();
-  const int base = sched_off[blockIdx.x], w = threadIdx.x >> 5;
-  const unsigned bit = 1u << (threadIdx.x & 31);
-  for (int k = k0; k < k1; k++) {
-    const unsigned c = (unsigned)cls[k];
-    const int st = base + (int)(rank[c >> 5] + __popc(bm[c >> 5] & ((1u << (c & 31)) - 1u)));
-    cls_out[st] = c;  // every row of the class writes the same value
-    atomicOr(mask_out + 4 * st + w, bit);
-  }
+}
+
+__global__ void k_tc_scatter(const int *tgt, const int *src, const int *cls, long n, const int *pos,
+                             const unsigned *bm, const unsigned *rank, int nwords, const int *sched_off, int *stab) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int row = pos[tgt[k]], tile = row / TC_ROWS;
+  const unsigned c = (unsigned)cls[k];
+  const size_t w = (size_t)tile * nwords + (c >> 5);
+  const unsigned st = (unsigned)sched_off[tile] + rank[w] + __popc(bm[w] & ((1u << (c & 31)) - 1u));
+  stab[(size_t)st * TC_ROWS + (row % TC_ROWS)] = src[k];
 }
 
 // Source multipoles as 2^e (hi + lo), hi and lo FP16 rows of kpad terms, e per
@@ -755,33 +739,33 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   // class-step schedule of the tiles: once per build and cell order
   const int ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
   if (t->sched_serial != t->build_serial || t->sched_version != t->order_version) {
-    if (fmm_reserve(t->tc_sched_off, ntiles + 1)) return FMM_ERR_CUDA;
-    int *cnt = t->tc_sched_off.p + 1;
     const int nwords = (t->nclasses + 31) / 32;
     if (nwords > TC_SCHED_MAXW) return FMM_ERR_RANGE;
-    if (nwords * 8 > 48 * 1024) {
-      FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_sched_count, cudaFuncAttributeMaxDynamicSharedMemorySize, nwords * 4));
-      FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_sched_write, cudaFuncAttributeMaxDynamicSharedMemorySize, nwords * 8));
-    }
-    fmm_note_launch(), k_tc_sched_count<<<ntiles, TC_ROWS, nwords * 4, st>>>(t->m2l_order.p, nc, t->m2l_off.p,
-                                                                             t->m2l_cls.p, nwords, cnt);
-    FMM_CUDA_TRY(cudaGetLastError());
-    std::vector<int> h(ntiles + 1);
-    FMM_CUDA_TRY(cudaMemcpyAsync(h.data() + 1, cnt, sizeof(int) * ntiles, cudaMemcpyDeviceToHost, st));
-    FMM_CUDA_TRY(cudaStreamSynchronize(st));
-    h[0] = 0;
-    for (int i = 0; i < ntiles; i++) h[i + 1] += h[i];
-    const int nsteps = h[ntiles];
-    FMM_CUDA_TRY(cudaMemcpyAsync(t->tc_sched_off.p, h.data(), sizeof(int) * (ntiles + 1), cudaMemcpyHostToDevice, st));
-    if (fmm_reserve(t->tc_sched_cls, nsteps > 0 ? nsteps : 1) ||
-        fmm_reserve(t->tc_sched_mask, 4 * (size_t)(nsteps > 0 ? nsteps : 1)))
+    const size_t nbm = (size_t)ntiles * nwords;
+    if (fmm_reserve(t->tc_sched_off, ntiles + 1) || fmm_reserve(t->tc_pos, nc) || fmm_reserve(t->tc_bitmap, nbm) ||
+        fmm_reserve(t->tc_rank, nbm) || fmm_reserve(t->tmp, sizeof(int) * (ntiles + 1 + fmm_scan_tmp_elems<int>(ntiles))))
       return FMM_ERR_CUDA;
-    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_sched_mask.p, 0, sizeof(unsigned) * 4 * (size_t)nsteps, st));
-    fmm_note_launch(), k_tc_sched_write<<<ntiles, TC_ROWS, nwords * 8, st>>>(
-        t->m2l_order.p, nc, t->m2l_off.p, t->m2l_cls.p, nwords, t->tc_sched_off.p, t->tc_sched_cls.p,
-        t->tc_sched_mask.p);
+    int *cnt = (int *)t->tmp.p, *stmp = cnt + ntiles + 1;
+    const long n = t->nm2l;
+    fmm_note_launch(), k_tc_pos<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->m2l_order.p, nc, t->tc_pos.p);
+    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_bitmap.p, 0, sizeof(unsigned) * nbm, st));
+    fmm_note_launch(), k_tc_bitmap<<<fmm_blocks(n, 256), 256, 0, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
+                                                                        t->tc_pos.p, nwords, t->tc_bitmap.p);
+    fmm_note_launch(), k_tc_rank<<<ntiles, 256, 0, st>>>(t->tc_bitmap.p, nwords, t->tc_rank.p, cnt);
+    if (int rc = fmm_scan<int>(cnt, t->tc_sched_off.p, ntiles, t->tc_sched_off.p + ntiles, stmp, st)) return rc;
+    FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_SCRATCH, t->tc_sched_off.p + ntiles, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    const int nsteps = (int)t->h_pinned[FMM_PINNED_SCRATCH];
+    const size_t ntab = (size_t)(nsteps > 0 ? nsteps : 1) * TC_ROWS;
+    if (fmm_reserve(t->tc_sched_cls, nsteps > 0 ? nsteps : 1) || fmm_reserve(t->tc_stab, ntab)) return FMM_ERR_CUDA;
+    fmm_note_launch(), k_tc_steps<<<ntiles, 128, 0, st>>>(t->tc_bitmap.p, t->tc_rank.p, nwords, t->tc_sched_off.p,
+                                                          t->tc_sched_cls.p);
+    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_stab.p, 0xff, sizeof(int) * ntab, st));
+    fmm_note_launch(), k_tc_scatter<<<fmm_blocks(n, 256), 256, 0, st>>>(
+        t->m2l_tgt_raw.p, t->m2l_src_raw.p, t->m2l_cls_raw.p, n, t->tc_pos.p, t->tc_bitmap.p, t->tc_rank.p, nwords,
+        t->tc_sched_off.p, t->tc_stab.p);
     FMM_CUDA_TRY(cudaGetLastError());
-    FMM_CUDA_TRY(cudaStreamSynchronize(st));  // h is read by the copy above
     t->sched_serial = t->build_serial;
     t->sched_version = t->order_version;
   }
@@ -812,12 +796,9 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   P.order = t->m2l_order.p;
   P.ncells = nc;
   P.ntiles = ntiles;
-  P.off = t->m2l_off.p;
-  P.src = t->m2l_src.p;
-  P.cls = t->m2l_cls.p;
   P.sched_off = t->tc_sched_off.p;
   P.sched_cls = t->tc_sched_cls.p;
-  P.sched_mask = t->tc_sched_mask.p;
+  P.stab = t->tc_stab.p;
   P.Mh = (const __half *)t->tc_Mh.p;
   P.Ml = (const __half *)t->tc_Ml.p;
   P.mexp = t->tc_mexp.p;

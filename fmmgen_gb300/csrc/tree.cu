@@ -970,10 +970,11 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   long n = t->nm2l;
   int nc = t->ncells;
   int p = t->order;
-  TRY(fmm_reserve(t->m2l_cls, n > 0 ? n : 1));
+  t->csr_serial = ~0ull;  // the target lists of this build are made on demand (fmm_m2l_csr)
+  TRY(fmm_reserve(t->m2l_cls_raw, n > 0 ? n : 1));
   if (n == 0) {
     t->nclasses = 0;
-    return group_by_target(t, t->m2l_tgt_raw, t->m2l_src_raw, nullptr, 0, 0, t->m2l_off, t->m2l_src, nullptr, st);
+    return fmm_m2l_cell_order(t, t->tune.grouping, st);
   }
   // classes of the raw (walk-order) pairs: the distinct keys through an
   // open-addressing table, ids by rank of the sorted distinct keys
@@ -1035,15 +1036,10 @@ static int build_classes(DevTree *t, cudaStream_t st) {
   t->order_prev = p;
   fmm_note_launch(), k_class_rank<<<fmm_blocks(ncls, 256), 256, 0, st>>>(U1, (int)ncls, t->cls_hkeys.p, hsize - 1,
                                                                           t->cls_table.p, t->cls_key4.p);
-  // raw classes go to the (finished) walk frontier buffer
-  TRY(fmm_reserve(t->fa, n));
+  // the class of each walk-order pair
   fmm_note_launch(), k_class_lookup<<<fmm_blocks(n, 256), 256, 0, st>>>(keys, n, t->cls_hkeys.p, hsize - 1,
-                                                                         t->cls_table.p, t->fa.p);
+                                                                         t->cls_table.p, t->m2l_cls_raw.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  // group by (target, class): a target has at most one source per class, so
-  // the order within a list is fully determined
-  TRY(group_by_target(t, t->m2l_tgt_raw, t->m2l_src_raw, t->fa.p, (int)ncls, n, t->m2l_off, t->m2l_src,
-                      t->m2l_cls.p, st));
   int nt = fmm_nterms(p);
   if (t->cls_D.cap < (size_t)ncls * nt || t->cls_Df.cap < (size_t)ncls * fmm_stride4(nt))  // contents lost
     FMM_CUDA_TRY(cudaMemsetAsync(t->d_cls_same.p, 0, sizeof(uint32_t), st));
@@ -1053,6 +1049,32 @@ static int build_classes(DevTree *t, cudaStream_t st) {
                                                                          t->cls_Df.p, t->d_cls_same.p);
   FMM_CUDA_TRY(cudaGetLastError());
   return fmm_m2l_cell_order(t, t->tune.grouping, st);
+}
+
+// The M2L pairs grouped by target, sorted by class within a target: a target
+// has at most one source per class, so the order within a list is fully
+// determined.  The walk-order pairs stay as they are (the sort runs on a copy).
+int fmm_m2l_csr(DevTree *t, cudaStream_t st) {
+  if (t->csr_serial == t->build_serial) return FMM_OK;
+  const long n = t->nm2l;
+  const int nc = t->ncells;
+  TRY(fmm_reserve(t->m2l_off, (size_t)nc + 1));
+  TRY(fmm_reserve(t->m2l_src, n > 0 ? n : 1));
+  TRY(fmm_reserve(t->m2l_cls, n > 0 ? n : 1));
+  if (n == 0) {
+    FMM_CUDA_TRY(cudaMemsetAsync(t->m2l_off.p, 0, sizeof(int) * ((size_t)nc + 1), st));
+  } else {
+    FMM_CUDA_TRY(cudaMemcpyAsync(t->m2l_src.p, t->m2l_src_raw.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    const int cbits = bits_for(t->nclasses), kbits = bits_for(nc) + cbits;
+    if (kbits <= 32)
+      TRY(sort_pairs<uint32_t>(t, t->m2l_tgt_raw.p, t->m2l_cls_raw.p, cbits, kbits, t->m2l_src, n, t->m2l_off,
+                               t->m2l_cls.p, st));
+    else
+      TRY(sort_pairs<uint64_t>(t, t->m2l_tgt_raw.p, t->m2l_cls_raw.p, cbits, kbits, t->m2l_src, n, t->m2l_off,
+                               t->m2l_cls.p, st));
+  }
+  t->csr_serial = t->build_serial;
+  return FMM_OK;
 }
 
 // The M2L processing order of the cells (t->m2l_order): level, then by octant
@@ -1098,6 +1120,8 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->pstart); fmm_release(t->pcount); fmm_release(t->parent); fmm_release(t->child_first);
   fmm_release(t->child_mask); fmm_release(t->clevel); fmm_release(t->leaf_cells); fmm_release(t->cell_leaf);
   fmm_release(t->m2l_off); fmm_release(t->m2l_src); fmm_release(t->m2l_cls); fmm_release(t->m2l_order);
+  fmm_release(t->m2l_cls_raw);
+  t->csr_serial = ~0ull;
   fmm_release(t->p2p_off); fmm_release(t->p2p_src);
   fmm_release(t->cls_key4); fmm_release(t->cls_D); fmm_release(t->cls_Df); fmm_release(t->cls_table);
   fmm_release(t->cls_hkeys); fmm_release(t->cls_prev); fmm_release(t->d_cls_same);
@@ -1109,7 +1133,8 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->p2p_tgt_raw); fmm_release(t->p2p_src_raw);
   fmm_release(t->tc_T); fmm_release(t->tc_Mh); fmm_release(t->tc_Ml); fmm_release(t->tc_mexp);
   fmm_release(t->d_tcerr);
-  fmm_release(t->tc_sched_off); fmm_release(t->tc_sched_cls); fmm_release(t->tc_sched_mask);
+  fmm_release(t->tc_sched_off); fmm_release(t->tc_sched_cls); fmm_release(t->tc_bitmap); fmm_release(t->tc_rank);
+  fmm_release(t->tc_stab); fmm_release(t->tc_pos);
   t->sched_serial = ~0ull;
   t->tc_serial = ~0ull;
   fmm_release(t->wdec);
