@@ -232,14 +232,54 @@ __device__ __forceinline__ bool ss_from_double(double s, int &e, long long &S) {
   return true;
 }
 
-// Chains the chunk maps in order, exactly: one warp per axis.  The state
-// (s, or S in ulps of binade e) is kept identical in every lane.  A chunk whose
-// map is missing or invalid for the exact state is run 32 elements at a time:
-// the lanes scan the element maps from the exact S, a ballot finds the first
-// element whose result leaves the binade, and only that element takes a plain
-// sequential FP64 add.
+// Chunk maps compose: chunk a then chunk b (same binade) is again
+//   S -> S + B[S mod 2],  B[p] = A_a[p] + A_b[(p + A_a[p]) mod 2]
+// (the parity after a is that of p + A_a[p]), valid while every intermediate
+// increment stays in [min(pmin_a, min A_a + pmin_b), max(pmax_a, max A_a + pmax_b)]
+// -- a conservative range, so a composite that checks valid is valid.  e ==
+// SS_ANY marks the identity.
+#define SS_ANY (-100000)
+__device__ __forceinline__ ChunkMap cm_identity() {
+  ChunkMap m;
+  m.A0 = m.A1 = m.pmin = m.pmax = 0;
+  m.e = SS_ANY;
+  m.ok = 1;
+  return m;
+}
+__device__ __forceinline__ ChunkMap cm_compose(const ChunkMap &a, const ChunkMap &b) {
+  if (a.e == SS_ANY) return b;
+  if (b.e == SS_ANY) return a;
+  ChunkMap c;
+  c.ok = a.ok && b.ok && a.e == b.e;
+  c.e = a.e;
+  c.A0 = a.A0 + ((a.A0 & 1) ? b.A1 : b.A0);
+  c.A1 = a.A1 + ((a.A1 & 1) ? b.A0 : b.A1);
+  c.pmin = min(a.pmin, min(a.A0, a.A1) + b.pmin);
+  c.pmax = max(a.pmax, max(a.A0, a.A1) + b.pmax);
+  return c;
+}
+__device__ __forceinline__ ChunkMap cm_shfl_up(const ChunkMap &m, int d) {
+  const unsigned FULL = 0xffffffffu;
+  ChunkMap o;
+  o.A0 = __shfl_up_sync(FULL, m.A0, d);
+  o.A1 = __shfl_up_sync(FULL, m.A1, d);
+  o.pmin = __shfl_up_sync(FULL, m.pmin, d);
+  o.pmax = __shfl_up_sync(FULL, m.pmax, d);
+  o.e = __shfl_up_sync(FULL, m.e, d);
+  o.ok = __shfl_up_sync(FULL, m.ok, d);
+  return o;
+}
+
+// Chains the chunk maps in order, exactly: one warp per axis, 32 chunks at a
+// time.  The state (s, or S in ulps of binade e) is kept identical in every
+// lane.  From the current chunk j of a block, the lanes compose the maps of
+// chunks j..lane (a warp scan); the longest run of composites that is valid
+// for the exact S is applied in one step.  A chunk that no composite covers
+// (its map is missing or invalid for the exact state) is run 32 elements at a
+// time: the lanes scan the element maps from the exact S, a ballot finds the
+// first element whose result leaves the binade, and only that element takes a
+// plain sequential FP64 add.
 __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks, const ChunkMap *maps, double *out) {
-  __shared__ ChunkMap sm[3][32];
   __shared__ double sx[3][SS_C];
   const unsigned FULL = 0xffffffffu;
   const int a = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -253,39 +293,48 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
   // (such chunks come in runs: their loads overlap the previous one's work)
   long pref_k = -1;
   double pr[SS_PER_LANE];
+  ChunkMap nxt = lane < nchunks ? maps[a * nchunks + lane] : cm_identity();
   for (long k0 = 0; k0 < nchunks; k0 += 32) {
-    __syncwarp();
-    if (k0 + lane < nchunks) sm[a][lane] = maps[a * nchunks + k0 + lane];
-    __syncwarp();
-    int nb = (int)min(32L, nchunks - k0);
-    for (int j = 0; j < nb; j++) {
-      long k = k0 + j;
-      ChunkMap m = sm[a][j];
-      bool done = false;
-      if (m.ok) {
-        if (!imode || e != m.e) {
-          double cur = imode ? ss_to_double(S, e) : s;
-          int ce;
-          long long cS;
-          if (ss_from_double(cur, ce, cS) && ce == m.e) {
-            S = cS;  // exact: cur is a multiple of its ulp
-            e = m.e;
-            imode = true;
-          } else {
-            s = cur;
-            imode = false;
-          }
-        }
-        if (imode) {
-          bool valid = S > 0 ? (S + m.pmin >= LO && S + m.pmax < HI) : (S + m.pmax <= -LO && S + m.pmin > -HI);
-          if (valid) {
-            S += (S & 1) ? m.A1 : m.A0;
-            done = true;
-          }
+    const ChunkMap mo = nxt;  // this lane's chunk k0 + lane
+    if (k0 + 32 + lane < nchunks) nxt = maps[a * nchunks + k0 + 32 + lane];  // the next block's, ahead
+    const int nb = (int)min(32L, nchunks - k0);
+    int j = 0;
+    while (j < nb) {
+      // the state in the binade of chunk j's map, when it has one
+      const int ej = __shfl_sync(FULL, mo.e, j), okj = __shfl_sync(FULL, mo.ok, j);
+      if (okj && (!imode || e != ej)) {
+        double cur = imode ? ss_to_double(S, e) : s;
+        int ce;
+        long long cS;
+        if (ss_from_double(cur, ce, cS) && ce == ej) {
+          S = cS;  // exact: cur is a multiple of its ulp
+          e = ej;
+          imode = true;
+        } else {
+          s = cur;
+          imode = false;
         }
       }
-      if (done) continue;
-      // ---- warp-parallel exact fallback over this chunk ----
+      if (okj && imode) {
+        ChunkMap c = lane >= j && lane < nb ? mo : cm_identity();
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const ChunkMap o = cm_shfl_up(c, d);
+          if (lane >= d) c = cm_compose(o, c);
+        }
+        const bool inr = S > 0 ? (S + c.pmin >= LO && S + c.pmax < HI) : (S + c.pmax <= -LO && S + c.pmin > -HI);
+        const bool v = lane >= j && lane < nb && c.ok && c.e == e && inr;
+        const unsigned inv = ~__ballot_sync(FULL, v) & (FULL << j);
+        const int f = inv ? __ffs(inv) - 1 : 32;  // first chunk not covered
+        if (f > j) {
+          const long long B0 = __shfl_sync(FULL, c.A0, f - 1), B1 = __shfl_sync(FULL, c.A1, f - 1);
+          S += (S & 1) ? B1 : B0;
+          j = f;
+          continue;
+        }
+      }
+      // ---- warp-parallel exact fallback over chunk k ----
+      const long k = k0 + j;
       long i0 = k * SS_C;
       int n = (int)(min(N, (k + 1) * SS_C) - i0);
       __syncwarp();
@@ -342,6 +391,7 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
           }
         }
       }
+      j++;
     }
   }
   if (lane == 0) {

@@ -93,13 +93,17 @@ def test_tree_strongly_clustered(fg, oracle_lib):
     oracle_check(fg, oracle_lib, pos, rng.uniform(-1, 1, (8000, 1)), 16, 4, 0.5)
 
 
-@pytest.mark.parametrize("dist", ["offset", "centred", "dyadic_ties", "tiny_scale", "single"])
+@pytest.mark.parametrize("dist", ["offset", "negative", "unit_1m", "centred", "dyadic_ties", "tiny_scale", "single"])
 def test_root_box_bits(fg, oracle_lib, dist):
     """Sequential-sum mean and 1.001 * max |x - mean| exactly as build_tree."""
     rng = np.random.default_rng(9)
-    n = 123457
+    n = 1_000_000 if dist == "unit_1m" else 123457
     if dist == "offset":
         pos = rng.uniform(-3, 7, (n, 3))
+    elif dist == "negative":  # negative running sums across binades
+        pos = rng.uniform(-7, 2, (n, 3))
+    elif dist == "unit_1m":  # long runs of chunks inside one binade
+        pos = rng.uniform(0, 1, (n, 3))
     elif dist == "centred":  # running sums wander across binades around zero
         pos = 0.1 * rng.standard_normal((n, 3))
     elif dist == "dyadic_ties":  # short mantissas: many additions round half-way
