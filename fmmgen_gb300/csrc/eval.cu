@@ -636,44 +636,77 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
 // ---------------------------------------------------------------------------
 // build + evaluate in one call
 // ---------------------------------------------------------------------------
-// The multipoles need nothing of the M2L classes, so while the build groups
-// the M2L lists by class (highest-priority stream) a second stream stages the
-// particles and runs P2M and M2M.  The M2L follows the classes on the
+// The multipoles need nothing of the interaction lists, so as soon as the
+// cells exist a second stream stages the particles and runs P2M and M2M
+// (near_start, beside the walk and the class build).  The M2L follows the classes on the
 // highest-priority stream -- its persistent CTAs take the SMs first -- and the
 // P2P starts beside it on the caller's stream (in the blocks the tuning
 // chose), as in the overlapped pass; L2L, L2P and the final sum follow.  Phase
 // records follow the streams: "M2L" spans the end of M2M to the end of M2L
 // (the class build included), "P2P" the near field's tail after it.
+// Stage the particles and run P2M and M2M on the near-field stream as soon as
+// the cells exist: the walk that builds the interaction lists runs beside them.
+struct NearStart {
+  const PlanSet *ps;
+  const double *S;
+  bool mixed;
+  cudaStream_t st;
+};
+template <typename T>
+static int near_start(DevTree *t, void *arg) {
+  const NearStart &a = *(const NearStart *)arg;
+  const int p = t->order, so = t->so, nl = t->nleaves;
+  const double *cr = t->cr.p;
+  const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so), nc = t->ncells;
+  const int mstr = a.mixed ? fmm_stride4((int)msize) : (int)msize;
+  TRY(fmm_reserve(t->Fnear, 4 * (size_t)t->N));
+  TRY(fmm_reserve(t->Ffar, 4 * (size_t)t->N));
+  T *M;
+  if (a.mixed) {
+    TRY(fmm_reserve(t->Mf, nc * mstr));
+    TRY(fmm_reserve(t->Lf, nc * fmm_stride4((int)lsize)));
+    TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
+    TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
+    M = (T *)(void *)t->Mf.p;
+  } else {
+    TRY(fmm_reserve(t->M, nc * msize));
+    TRY(fmm_reserve(t->L, nc * lsize));
+    M = (T *)(void *)t->M.p;
+  }
+  cudaStream_t sn = t->s_near;
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_fork, a.st));
+  FMM_CUDA_TRY(cudaStreamWaitEvent(sn, t->ev_fork, 0));
+  TRY(rec(t, 0, sn));
+  if (a.mixed) TRY(fmm_stage_particles(t, a.S, sn));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_s, sn));
+  fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
+      t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
+      t->pz.p, t->perm.p, a.S, so, p, cr, M, mstr);
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 1, sn));
+  for (int l = t->nlevels - 2; l >= 0; l--) {
+    int lo = t->level_off[l], hi = t->level_off[l + 1];
+    if (a.mixed)
+      TRY(fmm_m2m_tab(t, lo, hi, (float *)(void *)M, mstr, sn));
+    else
+      fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
+          a.ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr,
+          M, mstr);
+  }
+  FMM_CUDA_TRY(cudaGetLastError());
+  TRY(rec(t, 2, sn));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_m, sn));
+  return FMM_OK;
+}
+
 template <typename T>
 static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, bool mixed, int precision,
                       int mstr, int lstr, int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so, nl = t->nleaves;
   const double *cr = t->cr.p;
-  cudaStream_t sn = t->s_near;
-  FMM_CUDA_TRY(cudaEventRecord(t->ev_fork, st));
-  FMM_CUDA_TRY(cudaStreamWaitEvent(sn, t->ev_fork, 0));
-  TRY(rec(t, 0, sn));
-  if (mixed) TRY(fmm_stage_particles(t, S, sn));
-  FMM_CUDA_TRY(cudaEventRecord(t->ev_s, sn));
-  fmm_note_launch(), k_p2m<T><<<fmm_blocks(nl, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
-      t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, t->px.p, t->py.p,
-      t->pz.p, t->perm.p, S, so, p, cr, M, mstr);
-  FMM_CUDA_TRY(cudaGetLastError());
-  TRY(rec(t, 1, sn));
-  for (int l = t->nlevels - 2; l >= 0; l--) {
-    int lo = t->level_off[l], hi = t->level_off[l + 1];
-    if (mixed)
-      TRY(fmm_m2m_tab(t, lo, hi, (float *)(void *)M, mstr, sn));
-    else
-      fmm_note_launch(), k_m2m<T><<<fmm_blocks(hi - lo, FMM_WARPS), 32 * FMM_WARPS, 0, sn>>>(
-          ps->m2m, lo, hi, so, p, t->child_mask.p, t->child_first.p, t->clevel.p, t->cx.p, t->cy.p, t->cz.p, cr, M,
-          mstr);
-  }
-  FMM_CUDA_TRY(cudaGetLastError());
-  TRY(rec(t, 2, sn));
-  FMM_CUDA_TRY(cudaEventRecord(t->ev_m, sn));
+  FMM_CUDA_TRY(cudaEventRecord(t->ev_l, st));  // the interaction lists are built
   // the classes (the host waits on this stream only), then the M2L
-  FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_fork, 0));
+  FMM_CUDA_TRY(cudaStreamWaitEvent(t->s_hi, t->ev_l, 0));
   TRY(fmm_tree_finish_build(t, t->s_hi));
   const int impl = m2l_impl(t, precision);
   t->p2p_first = false;
@@ -719,7 +752,6 @@ int fmm_tree_build_evaluate(DevTree *t, const double *pos, long N, long ncrit, i
                             const long *sys_off, int nsys, const double *S, double *F, int potential, int field,
                             int precision, cudaStream_t st) {
   if (!S || !F || (!potential && !field) || precision < 0 || precision > 2) return FMM_ERR_ARG;
-  TRY(fmm_tree_build(t, pos, N, ncrit, order, theta, so, st, sys_off, nsys, true));
   fmm_graph_release(t);  // a recorded pass belongs to the previous build
   TRY(side_stream(t));
   if (!t->s_near) {
@@ -731,28 +763,28 @@ int fmm_tree_build_evaluate(DevTree *t, const double *pos, long N, long ncrit, i
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_c, cudaEventDisableTiming));
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_p, cudaEventDisableTiming));
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_s, cudaEventDisableTiming));
+    FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_l, cudaEventDisableTiming));
   }
-  const PlanSet *ps = fmm_get_plans(t->order, t->so);
+  if (so < 0 || so > 1 || order < so + 1 || order > FMM_PMAX) return FMM_ERR_ARG;
+  const PlanSet *ps = fmm_get_plans(order, so);
   if (!ps) return FMM_ERR_CUDA;
   const bool mixed = precision != 0;
+  // the tree, with the multipoles started beside its walk
+  NearStart ns{ps, S, mixed, st};
+  int rc = fmm_tree_build(t, pos, N, ncrit, order, theta, so, st, sys_off, nsys, true,
+                          mixed ? near_start<float> : near_start<double>, &ns);
+  if (rc) {
+    if (t->s_near) cudaStreamSynchronize(t->s_near);
+    return rc;
+  }
   t->last_prec = mixed ? 1 : 0;
   t->pass_potential = potential != 0;
   const int p = t->order;
   const size_t msize = fmm_nterms(p) - fmm_nterms(so - 1), lsize = fmm_nterms(p - so);
-  const size_t nc = t->ncells;
-  TRY(fmm_reserve(t->Fnear, 4 * (size_t)t->N));
-  TRY(fmm_reserve(t->Ffar, 4 * (size_t)t->N));
-  int rc;
   if (mixed) {
     const int mstr = fmm_stride4((int)msize), lstr = fmm_stride4((int)lsize), dstr = fmm_stride4(fmm_nterms(p));
-    TRY(fmm_reserve(t->Mf, nc * mstr));
-    TRY(fmm_reserve(t->Lf, nc * lstr));
-    TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
-    TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
     rc = fused_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, precision, mstr, lstr, dstr, st);
   } else {
-    TRY(fmm_reserve(t->M, nc * msize));
-    TRY(fmm_reserve(t->L, nc * lsize));
     rc = fused_pass<double>(t, ps, S, t->M.p, t->L.p, false, precision, (int)msize, (int)lsize, fmm_nterms(p), st);
   }
   if (rc == FMM_OK && t->eflags) {  // the build's own error, after the near-field stream is done

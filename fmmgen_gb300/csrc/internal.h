@@ -80,7 +80,7 @@ struct DevTree {
   cudaStream_t s_hi = nullptr;            // the side stream (highest priority)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t s_near = nullptr;          // build_evaluate: P2M, M2M and P2P beside the class build
-  cudaEvent_t ev_m = nullptr, ev_c = nullptr, ev_p = nullptr, ev_s = nullptr;
+  cudaEvent_t ev_m = nullptr, ev_c = nullptr, ev_p = nullptr, ev_s = nullptr, ev_l = nullptr;
   int grouping_built = 0;                 // grouping m2l_order holds
   DevBuf<int> p2p_off, p2p_src;
   // M2L translation classes: operator vectors D^(k)(d/s_target), |k| <= order
@@ -156,8 +156,11 @@ struct DevTree {
 
 // sys_off: nullptr for one system, else nsys + 1 host offsets of the systems'
 // particles in pos (a forest: one root cube and tree per system, one pass)
+// after_cells(t, arg), when given, runs once the cells exist and before the
+// interaction lists are built (its work can run beside the walk)
 int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
-                   cudaStream_t st, const long *sys_off = nullptr, int nsys = 1, bool defer_classes = false);
+                   cudaStream_t st, const long *sys_off = nullptr, int nsys = 1, bool defer_classes = false,
+                   int (*after_cells)(DevTree *, void *) = nullptr, void *arg = nullptr);
 int fmm_tree_finish_build(DevTree *t, cudaStream_t st);
 // build and evaluate in one call, the classes built while P2M, M2M and P2P run
 int fmm_tree_build_evaluate(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,

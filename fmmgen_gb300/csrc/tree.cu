@@ -637,7 +637,8 @@ static int build_lists(DevTree *t, cudaStream_t st);
 static int build_classes(DevTree *t, cudaStream_t st);
 
 int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
-                   cudaStream_t st, const long *sys_off, int nsys, bool defer_classes) {
+                   cudaStream_t st, const long *sys_off, int nsys, bool defer_classes,
+                   int (*after_cells)(DevTree *, void *), void *arg) {
   if (N < 1 || N >= (1L << 31) - 1 || ncrit < 1 || order < so + 1 || order > FMM_PMAX || so < 0 || so > 1 ||
       !(theta > 0) || !pos || nsys < 1 || (nsys > 1 && !sys_off))
     return FMM_ERR_ARG;
@@ -729,6 +730,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
 
   TRY(build_cells(t, st));
   TRY(rec(t, 3, st));
+  if (after_cells) TRY(after_cells(t, arg));  // work that needs the cells only, beside the walk
   TRY(build_lists(t, st));
   TRY(rec(t, 4, st));
   return defer_classes ? FMM_OK : fmm_tree_finish_build(t, st);
@@ -1103,7 +1105,7 @@ int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st) {
 void fmm_tree_destroy(DevTree *t) {
   if (!t) return;
   fmm_graph_release(t);
-  for (cudaEvent_t *e : {&t->ev_fork, &t->ev_join, &t->ev_m, &t->ev_c, &t->ev_p, &t->ev_s}) {
+  for (cudaEvent_t *e : {&t->ev_fork, &t->ev_join, &t->ev_m, &t->ev_c, &t->ev_p, &t->ev_s, &t->ev_l}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;
   }
