@@ -612,13 +612,37 @@ __global__ void k_tc_pos(const int *order, int ncells, int *pos) {
   if (r < ncells) pos[order[r]] = r;
 }
 
+// Bitmaps of all tiles, each block over a slice of the pairs into a private
+// copy in shared memory, written out whole (part[block][nbm]); k_tc_bitmap_or
+// then ORs the copies.  (Pairs of one word come from every part of the walk,
+// so atomics on one global copy serialise on a few hot words.)
+__global__ void k_tc_bitmap_part(const int *tgt, const int *cls, long n, const int *pos, int nwords, int nbm,
+                                 unsigned *part) {
+  extern __shared__ unsigned sbm[];
+  for (int i = threadIdx.x; i < nbm; i += blockDim.x) sbm[i] = 0u;
+  __syncthreads();
+  const long per = (n + gridDim.x - 1) / gridDim.x, k0 = blockIdx.x * per, k1 = min(n, k0 + per);
+  for (long k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    const unsigned c = (unsigned)cls[k];
+    atomicOr(sbm + (pos[tgt[k]] / TC_ROWS) * nwords + (c >> 5), 1u << (c & 31));
+  }
+  __syncthreads();
+  unsigned *out = part + (size_t)blockIdx.x * nbm;
+  for (int i = threadIdx.x; i < nbm; i += blockDim.x) out[i] = sbm[i];
+}
+__global__ void k_tc_bitmap_or(const unsigned *part, int nparts, int nbm, unsigned *bm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbm) return;
+  unsigned v = 0u;
+  for (int b = 0; b < nparts; b++) v |= part[(size_t)b * nbm + i];
+  bm[i] = v;
+}
+// the same on one global copy, for bitmaps too large for shared memory
 __global__ void k_tc_bitmap(const int *tgt, const int *cls, long n, const int *pos, int nwords, unsigned *bm) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const unsigned c = (unsigned)cls[k];
-  unsigned *w = bm + (size_t)(pos[tgt[k]] / TC_ROWS) * nwords + (c >> 5);
-  const unsigned bit = 1u << (c & 31);
-  if (!(*(volatile unsigned *)w & bit)) atomicOr(w, bit);  // most bits are set already: read first
+  atomicOr(bm + (size_t)(pos[tgt[k]] / TC_ROWS) * nwords + (c >> 5), 1u << (c & 31));
 }
 
 // one block per tile
@@ -748,9 +772,22 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
     int *cnt = (int *)t->tmp.p, *stmp = cnt + ntiles + 1;
     const long n = t->nm2l;
     fmm_note_launch(), k_tc_pos<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->m2l_order.p, nc, t->tc_pos.p);
-    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_bitmap.p, 0, sizeof(unsigned) * nbm, st));
-    fmm_note_launch(), k_tc_bitmap<<<fmm_blocks(n, 256), 256, 0, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
-                                                                        t->tc_pos.p, nwords, t->tc_bitmap.p);
+    const int nparts = 2 * tc_sm_count();
+    if (nbm * sizeof(unsigned) <= 160 * 1024 && n >= 64L * nparts) {
+      const int sbytes = (int)(nbm * sizeof(unsigned));
+      if (fmm_reserve(t->tc_stab, (size_t)nparts * nbm)) return FMM_ERR_CUDA;  // scratch until the table
+      if (sbytes > 48 * 1024)
+        FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_bitmap_part, cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes));
+      unsigned *part = (unsigned *)t->tc_stab.p;
+      fmm_note_launch(), k_tc_bitmap_part<<<nparts, 512, sbytes, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
+                                                                        t->tc_pos.p, nwords, (int)nbm, part);
+      fmm_note_launch(), k_tc_bitmap_or<<<fmm_blocks(nbm, 256), 256, 0, st>>>(part, nparts, (int)nbm,
+                                                                              t->tc_bitmap.p);
+    } else {
+      FMM_CUDA_TRY(cudaMemsetAsync(t->tc_bitmap.p, 0, sizeof(unsigned) * nbm, st));
+      fmm_note_launch(), k_tc_bitmap<<<fmm_blocks(n, 256), 256, 0, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
+                                                                          t->tc_pos.p, nwords, t->tc_bitmap.p);
+    }
     fmm_note_launch(), k_tc_rank<<<ntiles, 256, 0, st>>>(t->tc_bitmap.p, nwords, t->tc_rank.p, cnt);
     if (int rc = fmm_scan<int>(cnt, t->tc_sched_off.p, ntiles, t->tc_sched_off.p + ntiles, stmp, st)) return rc;
     FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_SCRATCH, t->tc_sched_off.p + ntiles, sizeof(int),

@@ -219,70 +219,60 @@ __global__ void k_apply_order(const uint32_t *idx, long N, const uint64_t *kin, 
   pout[i] = pin[idx[i]];
 }
 
+// One warp per cell of the level: lane o (1..7) finds where digit o starts in
+// the cell's sorted keys, so the eight child ranges come from seven searches
+// side by side; bnd[9 (c - lo) + o] = first particle of child o (bnd[.. + 8] = end).
 __global__ void k_count_children(int lo, int hi, int level, long ncrit, const uint64_t *keys, const int *pstart,
-                                 const int *pcount, unsigned char *child_mask, uint32_t *cnt,
+                                 const int *pcount, unsigned char *child_mask, uint32_t *cnt, int *bnd,
                                  uint32_t *eflags) {
-  int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = lo + (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (c >= hi) return;
-  uint32_t n = 0;
-  unsigned mask = 0;
-  if (pcount[c] >= ncrit) {
-    if (level >= FMM_MAXLEVEL) {
-      atomicOr(eflags, FMM_EFLAG_DEPTH);
-    } else {
-      int s = pstart[c], e = s + pcount[c];
-      int b = s;
-      for (int o = 0; o < 8; o++) {
-        int nb = lower_digit(keys, b, e, level + 1, o + 1);
-        if (nb > b) mask |= 1u << o;
-        b = nb;
-      }
-      n = __popc(mask);
-    }
+  const int s = pstart[c], e = s + pcount[c];
+  const bool split = pcount[c] >= ncrit && level < FMM_MAXLEVEL;
+  int b = lane == 0 ? s : e;
+  if (split && lane >= 1 && lane <= 7) b = lower_digit(keys, s, e, level + 1, lane);
+  if (lane <= 8) bnd[9 * (c - lo) + lane] = b;
+  // child o holds [bnd[o], bnd[o + 1])
+  const int nb = __shfl_down_sync(0xffffffffu, b, 1);
+  const unsigned mask = __ballot_sync(0xffffffffu, split && lane < 8 && nb > b) & 0xffu;
+  if (lane == 0) {
+    if (pcount[c] >= ncrit && level >= FMM_MAXLEVEL) atomicOr(eflags, FMM_EFLAG_DEPTH);
+    child_mask[c] = (unsigned char)mask;
+    cnt[c - lo] = (uint32_t)__popc(mask);
   }
-  child_mask[c] = (unsigned char)mask;
-  cnt[c - lo] = n;
 }
 
-__global__ void k_write_children(int lo, int hi, int level, const uint64_t *keys, const uint32_t *off, double *cx,
+// One warp per cell: lane o writes child o, when it exists.
+__global__ void k_write_children(int lo, int hi, int level, const uint32_t *off, const int *bnd, double *cx,
                                  double *cy, double *cz, uint64_t *cid, int *ix, int *iy, int *iz, int *pstart,
                                  int *pcount, int *parent, int *child_first, const unsigned char *child_mask_in,
                                  unsigned char *child_mask, unsigned char *clevel, double *cr, double *crmax,
                                  float2 *crf, int *csys) {
-  int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = lo + (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), o = threadIdx.x & 31;
   if (c >= hi) return;
-  unsigned mask = child_mask_in[c];
-  if (!mask) { child_first[c] = -1; return; }
-  int first = hi + (int)off[c - lo];
-  child_first[c] = first;
+  const unsigned mask = child_mask_in[c];
+  const int first = hi + (int)off[c - lo];
+  if (o == 0) child_first[c] = mask ? first : -1;
+  if (o >= 8 || !((mask >> o) & 1u)) return;
+  const int j = first + __popc(mask & ((1u << o) - 1u));
   const double r = __ddiv_rn(cr[c], 2.0);  // child half-width = parent r / 2.0 (example/tree.cpp:95)
-  const int sys = csys[c];
-  double px = cx[c], py = cy[c], pz = cz[c];
-  int s = pstart[c], e = s + pcount[c];
-  int b = s, j = first;
-  for (int o = 0; o < 8; o++) {
-    int nb = lower_digit(keys, b, e, level + 1, o + 1);
-    if (nb > b) {
-      // add_child (example/tree.cpp:95-98)
-      cx[j] = __dadd_rn(px, (o & 1) ? r : -r);
-      cy[j] = __dadd_rn(py, (o & 2) ? r : -r);
-      cz[j] = __dadd_rn(pz, (o & 4) ? r : -r);
-      cid[j] = (cid[c] << 3) | (uint64_t)o;
-      ix[j] = 2 * ix[c] + (o & 1);
-      iy[j] = 2 * iy[c] + ((o >> 1) & 1);
-      iz[j] = 2 * iz[c] + (o >> 2);
-      pstart[j] = b;
-      pcount[j] = nb - b;
-      parent[j] = c;
-      child_first[j] = -1;
-      child_mask[j] = 0;
-      clevel[j] = (unsigned char)(level + 1);
-      set_radius(j, r, cr, crmax, crf);
-      csys[j] = sys;
-      j++;
-    }
-    b = nb;
-  }
+  const int b = bnd[9 * (c - lo) + o], nb = bnd[9 * (c - lo) + o + 1];
+  // add_child (example/tree.cpp:95-98)
+  cx[j] = __dadd_rn(cx[c], (o & 1) ? r : -r);
+  cy[j] = __dadd_rn(cy[c], (o & 2) ? r : -r);
+  cz[j] = __dadd_rn(cz[c], (o & 4) ? r : -r);
+  cid[j] = (cid[c] << 3) | (uint64_t)o;
+  ix[j] = 2 * ix[c] + (o & 1);
+  iy[j] = 2 * iy[c] + ((o >> 1) & 1);
+  iz[j] = 2 * iz[c] + (o >> 2);
+  pstart[j] = b;
+  pcount[j] = nb - b;
+  parent[j] = c;
+  child_first[j] = -1;
+  child_mask[j] = 0;
+  clevel[j] = (unsigned char)(level + 1);
+  set_radius(j, r, cr, crmax, crf);
+  csys[j] = csys[c];
 }
 
 __global__ void k_leaf_flags(int ncells, long ncrit, const int *pcount, uint32_t *flag) {
@@ -780,13 +770,15 @@ static int build_cells(DevTree *t, cudaStream_t st) {
   int rc = FMM_OK;
   while (true) {
     int n = hi - lo;
-    size_t need = (size_t)n * 4 + fmm_scan_tmp_elems<uint32_t>(n) * 4 + 64;
+    const size_t nscan = (size_t)n + 1 + fmm_scan_tmp_elems<uint32_t>(n) + 16;
+    size_t need = nscan * 4 + (size_t)n * 9 * 4;
     if ((rc = tmp_reserve(t, need))) break;
     uint32_t *cnt = (uint32_t *)t->tmp.p;
     uint32_t *total = cnt + n;
     uint32_t *stmp = total + 1;
-    fmm_note_launch(), k_count_children<<<fmm_blocks(n, 128), 128, 0, st>>>(lo, hi, level, t->ncrit, t->keys.p, t->pstart.p,
-                                                         t->pcount.p, t->child_mask.p, cnt, t->d_eflags.p);
+    int *bnd = (int *)(cnt + nscan);  // child boundaries of each cell of the level
+    fmm_note_launch(), k_count_children<<<fmm_blocks((size_t)n * 32, 128), 128, 0, st>>>(
+        lo, hi, level, t->ncrit, t->keys.p, t->pstart.p, t->pcount.p, t->child_mask.p, cnt, bnd, t->d_eflags.p);
     if ((rc = fmm_scan<uint32_t>(cnt, cnt, n, total, stmp, st))) break;
     cudaMemcpyAsync(h_total, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -804,8 +796,8 @@ static int build_cells(DevTree *t, cudaStream_t st) {
         (rc = grow_keep(t->cr, need_cells, used, st)) || (rc = grow_keep(t->crmax, need_cells, used, st)) ||
         (rc = grow_keep(t->crf, need_cells, used, st)) || (rc = grow_keep(t->csys, need_cells, used, st)))
       break;
-    fmm_note_launch(), k_write_children<<<fmm_blocks(n, 128), 128, 0, st>>>(
-        lo, hi, level, t->keys.p, cnt, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p, t->pstart.p,
+    fmm_note_launch(), k_write_children<<<fmm_blocks((size_t)n * 32, 128), 128, 0, st>>>(
+        lo, hi, level, cnt, bnd, t->cx.p, t->cy.p, t->cz.p, t->cid.p, t->ix.p, t->iy.p, t->iz.p, t->pstart.p,
         t->pcount.p, t->parent.p, t->child_first.p, t->child_mask.p, t->child_mask.p, t->clevel.p, t->cr.p,
         t->crmax.p, t->crf.p, t->csys.p);
     if (cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
