@@ -38,6 +38,8 @@ __host__ __device__ __forceinline__ MI fmm_decode(int i) {
 #define FMM_EFLAG_DEPTH 1u     // a cell at FMM_MAXLEVEL still holds >= ncrit particles
 #define FMM_EFLAG_RANGE 2u     // an M2L offset outside the class table's range
 #define FMM_EFLAG_BOUNDS 4u    // an index check failed (never expected)
+#define FMM_EFLAG_KEYS 8u      // the particle keys need more levels (the build recomputes them)
+#define FMM_KEYLEVELS 10       // levels of digits in the first keys of a build
 
 // Status codes of the C ABI (mirrored in include/fmmgen_gb300.h).
 #define FMM_OK 0

@@ -77,8 +77,11 @@ __global__ void k_root_final(const double *sums, const unsigned long long *mx, l
 // ---------------------------------------------------------------------------
 // per-particle octant keys (example/tree.cpp:94-98, 189-204)
 // ---------------------------------------------------------------------------
+// The digits of levels 1..nlev (the rest of the key is zero): the cells are cut
+// from them, and the build asks for all FMM_MAXLEVEL levels only when a cell at
+// level nlev still has to be split.
 __global__ void k_keys(const double *__restrict__ pos, long N, const double *roots, const int *psys,
-                       uint64_t *keys, uint32_t *idx) {
+                       int nlev, uint64_t *keys, uint32_t *idx) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= N) return;
   const double *root = roots + 4 * (psys ? psys[i] : 0);  // the particle's system's root cube
@@ -86,7 +89,7 @@ __global__ void k_keys(const double *__restrict__ pos, long N, const double *roo
   double cx = root[0], cy = root[1], cz = root[2], r = root[3];
   uint64_t key = 0;
 #pragma unroll 3
-  for (int l = 0; l < FMM_MAXLEVEL; l++) {
+  for (int l = 0; l < nlev; l++) {
     int oct = (x > cx) + ((y > cy) << 1) + ((z > cz) << 2);
     key = (key << 3) | (uint64_t)oct;
     // r / 2.0 and r * (+-1) are exact: halving and a sign select round identically
@@ -95,7 +98,7 @@ __global__ void k_keys(const double *__restrict__ pos, long N, const double *roo
     cy = __dadd_rn(cy, (oct & 2) ? r : -r);
     cz = __dadd_rn(cz, (oct & 4) ? r : -r);
   }
-  keys[i] = key;
+  keys[i] = key << (3 * (FMM_MAXLEVEL - nlev));
   idx[i] = (uint32_t)i;
 }
 
@@ -222,13 +225,13 @@ __global__ void k_apply_order(const uint32_t *idx, long N, const uint64_t *kin, 
 // One warp per cell of the level: lane o (1..7) finds where digit o starts in
 // the cell's sorted keys, so the eight child ranges come from seven searches
 // side by side; bnd[9 (c - lo) + o] = first particle of child o (bnd[.. + 8] = end).
-__global__ void k_count_children(int lo, int hi, int level, long ncrit, const uint64_t *keys, const int *pstart,
-                                 const int *pcount, unsigned char *child_mask, uint32_t *cnt, int *bnd,
-                                 uint32_t *eflags) {
+__global__ void k_count_children(int lo, int hi, int level, int nlev, long ncrit, const uint64_t *keys,
+                                 const int *pstart, const int *pcount, unsigned char *child_mask, uint32_t *cnt,
+                                 int *bnd, uint32_t *eflags) {
   const int c = lo + (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (c >= hi) return;
   const int s = pstart[c], e = s + pcount[c];
-  const bool split = pcount[c] >= ncrit && level < FMM_MAXLEVEL;
+  const bool split = pcount[c] >= ncrit && level < nlev;
   int b = lane == 0 ? s : e;
   if (split && lane >= 1 && lane <= 7) b = lower_digit(keys, s, e, level + 1, lane);
   if (lane <= 8) bnd[9 * (c - lo) + lane] = b;
@@ -236,7 +239,8 @@ __global__ void k_count_children(int lo, int hi, int level, long ncrit, const ui
   const int nb = __shfl_down_sync(0xffffffffu, b, 1);
   const unsigned mask = __ballot_sync(0xffffffffu, split && lane < 8 && nb > b) & 0xffu;
   if (lane == 0) {
-    if (pcount[c] >= ncrit && level >= FMM_MAXLEVEL) atomicOr(eflags, FMM_EFLAG_DEPTH);
+    if (pcount[c] >= ncrit && level >= nlev)  // no digits below: give up, or ask for all levels
+      atomicOr(eflags, nlev >= FMM_MAXLEVEL ? FMM_EFLAG_DEPTH : FMM_EFLAG_KEYS);
     child_mask[c] = (unsigned char)mask;
     cnt[c - lo] = (uint32_t)__popc(mask);
   }
@@ -622,7 +626,7 @@ static int rec(DevTree *t, int i, cudaStream_t st) {
 }
 
 __global__ void k_p2p_count(const int *off, const int *src, int nc, const int *pcount, unsigned long long *out);
-static int build_cells(DevTree *t, cudaStream_t st);
+static int build_cells(DevTree *t, cudaStream_t st, int nlev, bool *deeper);
 static int build_lists(DevTree *t, cudaStream_t st);
 static int build_classes(DevTree *t, cudaStream_t st);
 
@@ -687,38 +691,44 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
   FMM_CUDA_TRY(cudaGetLastError());
   TRY(rec(t, 1, st));
 
-  // keys + stable sort
+  // keys + stable sort, then the cells; the keys hold the digits of the first
+  // FMM_KEYLEVELS levels unless a tree that deep needs more (then all of them)
   TRY(fmm_reserve(t->keys, N)); TRY(fmm_reserve(t->keys2, N));
   TRY(fmm_reserve(t->perm, N)); TRY(fmm_reserve(t->perm2, N));
-  fmm_note_launch(), k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, t->roots.p, nsys > 1 ? t->psys.p : nullptr,
-                                                                 t->keys.p, t->perm.p);
-  FMM_CUDA_TRY(cudaGetLastError());
-  size_t nbh = fmm_rs_nblocks(N);
-  size_t hist_n = 256 * nbh;
-  const size_t sort_bytes = hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 1024;
-  TRY(tmp_reserve(t, sort_bytes + (nsys > 1 ? 16 * (size_t)N : 0)));
-  uint32_t *hist = (uint32_t *)t->tmp.p;
-  uint32_t *scantmp = hist + hist_n;
-  TRY(fmm_radix_sort(t->keys.p, t->perm.p, t->keys2.p, t->perm2.p, N, 0, 3 * FMM_MAXLEVEL, hist, scantmp, st));
-  if (nsys > 1) {
-    // stable sort by system: (system, key) order, each system's particles contiguous
-    uint32_t *ks = (uint32_t *)(t->tmp.p + sort_bytes);
-    uint32_t *idx = ks + N, *ks2 = idx + N, *idx2 = ks2 + N;
-    fmm_note_launch(), k_sorted_sys<<<fmm_blocks(N, 256), 256, 0, st>>>(t->perm.p, t->psys.p, N, ks, idx);
-    TRY(fmm_radix_sort<uint32_t>(ks, idx, ks2, idx2, N, 0, bits_for(nsys), hist, scantmp, st));
-    fmm_note_launch(), k_apply_order<<<fmm_blocks(N, 256), 256, 0, st>>>(idx, N, t->keys.p, t->perm.p, t->keys2.p,
-                                                                         t->perm2.p);
+  for (int nlev = FMM_KEYLEVELS;; nlev = FMM_MAXLEVEL) {
+    fmm_note_launch(), k_keys<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, N, t->roots.p, nsys > 1 ? t->psys.p : nullptr,
+                                                                   nlev, t->keys.p, t->perm.p);
     FMM_CUDA_TRY(cudaGetLastError());
-    std::swap(t->keys, t->keys2);
-    std::swap(t->perm, t->perm2);
+    size_t nbh = fmm_rs_nblocks(N);
+    size_t hist_n = 256 * nbh;
+    const size_t sort_bytes = hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 1024;
+    TRY(tmp_reserve(t, sort_bytes + (nsys > 1 ? 16 * (size_t)N : 0)));
+    uint32_t *hist = (uint32_t *)t->tmp.p;
+    uint32_t *scantmp = hist + hist_n;
+    TRY(fmm_radix_sort(t->keys.p, t->perm.p, t->keys2.p, t->perm2.p, N, 3 * (FMM_MAXLEVEL - nlev),
+                       3 * FMM_MAXLEVEL, hist, scantmp, st));
+    if (nsys > 1) {
+      // stable sort by system: (system, key) order, each system's particles contiguous
+      uint32_t *ks = (uint32_t *)(t->tmp.p + sort_bytes);
+      uint32_t *idx = ks + N, *ks2 = idx + N, *idx2 = ks2 + N;
+      fmm_note_launch(), k_sorted_sys<<<fmm_blocks(N, 256), 256, 0, st>>>(t->perm.p, t->psys.p, N, ks, idx);
+      TRY(fmm_radix_sort<uint32_t>(ks, idx, ks2, idx2, N, 0, bits_for(nsys), hist, scantmp, st));
+      fmm_note_launch(), k_apply_order<<<fmm_blocks(N, 256), 256, 0, st>>>(idx, N, t->keys.p, t->perm.p,
+                                                                           t->keys2.p, t->perm2.p);
+      FMM_CUDA_TRY(cudaGetLastError());
+      std::swap(t->keys, t->keys2);
+      std::swap(t->perm, t->perm2);
+    }
+    TRY(fmm_reserve(t->px, N)); TRY(fmm_reserve(t->py, N)); TRY(fmm_reserve(t->pz, N));
+    fmm_note_launch(), k_gather_pos<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, t->perm.p, N, t->px.p, t->py.p,
+                                                                         t->pz.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaMemcpyAsync(&t->root, t->roots.p, sizeof(RootBox), cudaMemcpyDeviceToHost, st));  // system 0
+    TRY(rec(t, 2, st));
+    bool deeper = false;
+    TRY(build_cells(t, st, nlev, &deeper));
+    if (!deeper) break;
   }
-  TRY(fmm_reserve(t->px, N)); TRY(fmm_reserve(t->py, N)); TRY(fmm_reserve(t->pz, N));
-  fmm_note_launch(), k_gather_pos<<<fmm_blocks(N, 256), 256, 0, st>>>(pos, t->perm.p, N, t->px.p, t->py.p, t->pz.p);
-  FMM_CUDA_TRY(cudaGetLastError());
-  FMM_CUDA_TRY(cudaMemcpyAsync(&t->root, t->roots.p, sizeof(RootBox), cudaMemcpyDeviceToHost, st));  // system 0
-  TRY(rec(t, 2, st));
-
-  TRY(build_cells(t, st));
   TRY(rec(t, 3, st));
   if (after_cells) TRY(after_cells(t, arg));  // work that needs the cells only, beside the walk
   TRY(build_lists(t, st));
@@ -747,7 +757,9 @@ int fmm_tree_finish_build(DevTree *t, cudaStream_t st) {
   return FMM_OK;
 }
 
-static int build_cells(DevTree *t, cudaStream_t st) {
+// Cells level by level from keys holding nlev levels of digits; *deeper is set
+// (and the error flag cleared) when a cell at level nlev would need the next.
+static int build_cells(DevTree *t, cudaStream_t st, int nlev, bool *deeper) {
   long N = t->N;
   const int nsys = t->nsys;
   size_t cap = (size_t)(4 * N / std::max<long>(t->ncrit, 1)) + 1024 + nsys;
@@ -778,7 +790,8 @@ static int build_cells(DevTree *t, cudaStream_t st) {
     uint32_t *stmp = total + 1;
     int *bnd = (int *)(cnt + nscan);  // child boundaries of each cell of the level
     fmm_note_launch(), k_count_children<<<fmm_blocks((size_t)n * 32, 128), 128, 0, st>>>(
-        lo, hi, level, t->ncrit, t->keys.p, t->pstart.p, t->pcount.p, t->child_mask.p, cnt, bnd, t->d_eflags.p);
+        lo, hi, level, nlev, t->ncrit, t->keys.p, t->pstart.p, t->pcount.p, t->child_mask.p, cnt, bnd,
+        t->d_eflags.p);
     if ((rc = fmm_scan<uint32_t>(cnt, cnt, n, total, stmp, st))) break;
     cudaMemcpyAsync(h_total, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -823,8 +836,14 @@ static int build_cells(DevTree *t, cudaStream_t st) {
                                                       t->cell_leaf.p);
   FMM_CUDA_TRY(cudaGetLastError());
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + 1, t->d_eflags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   FMM_CUDA_TRY(cudaStreamSynchronize(st));
   t->nleaves = (int)t->h_pinned[0];
+  if (t->h_pinned[1] & FMM_EFLAG_KEYS) {
+    *deeper = true;
+    FMM_CUDA_TRY(cudaMemsetAsync(t->d_eflags.p, 0, sizeof(uint32_t), st));
+    return FMM_OK;
+  }
   TRY(fmm_reserve(t->cmargin, nc));
   fmm_note_launch(), k_cell_margins<<<fmm_blocks(nc, 256), 256, 0, st>>>(nc, t->csys.p, t->roots.p, t->cr.p,
                                                                           t->theta, t->cmargin.p);
