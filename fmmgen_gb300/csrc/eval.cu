@@ -24,16 +24,32 @@
 // ---------------------------------------------------------------------------
 // warp contraction engine (plans.cu)
 // ---------------------------------------------------------------------------
+// Four tasks per round: their words and operands are loaded before the first
+// is applied, so the dependent task-word -> shared-memory loads of a round
+// overlap (a lane's tasks are one contiguous range; pad words end it).
 template <typename T>
 __device__ __forceinline__ void engine_run(const Plan &P, const T *A, const T *B, T *slots, int lane) {
+  constexpr uint32_t PAD = 0xffffffffu;
   T acc = T(0);
-  for (int it = 0; it < P.iters; ++it) {
-    uint32_t w = __ldg(&P.task[it * 32 + lane]);
-    if (w == 0xffffffffu) break;
-    acc += A[w & 1023u] * B[(w >> 10) & 1023u];
-    if (w >> 31) {
-      slots[(w >> 20) & 2047u] += acc;
-      acc = T(0);
+  for (int it = 0; it < P.iters; it += 4) {
+    uint32_t w[4];
+    T a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) w[u] = it + u < P.iters ? __ldg(&P.task[(it + u) * 32 + lane]) : PAD;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t x = w[u] == PAD ? 0u : w[u];
+      a[u] = A[x & 1023u];
+      b[u] = B[(x >> 10) & 1023u];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (w[u] == PAD) return;
+      acc += a[u] * b[u];
+      if (w[u] >> 31) {
+        slots[(w[u] >> 20) & 2047u] += acc;
+        acc = T(0);
+      }
     }
   }
 }
@@ -244,18 +260,38 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(PlanVar PV, int ncel
 #pragma unroll
   for (int r = 0; r < M2LV_R; r++) acc[r] = T(0);
   const int la = clevel[A];
-  for (int k = off_[A]; k < off_[A + 1]; k++) {
-    const int q = min(max((int)ord[k], so + 1), order);
+  const int k0 = off_[A], k1 = off_[A + 1];
+  // the operands of the next pair are loaded into registers while the engine
+  // runs on the current one
+  T dr[M2LV_R], mr[M2LV_R];
+  int qn = 0, dln = 0;
+  auto fetch = [&](int k) {
+    qn = min(max((int)ord[k], so + 1), order);
+    const int B = src[k], nt = fmm_nterms(qn), ms = nt - moff;
+    const T *D = clsD + (size_t)cls[k] * dstr;
+    dln = la - (int)clevel[B];
+#pragma unroll
+    for (int r = 0; r < M2LV_R; r++) {
+      const int i = lane + 32 * r;
+      dr[r] = i < nt ? D[i] : T(0);
+      mr[r] = i < ms ? M[(size_t)B * mstr + i] : T(0);
+    }
+  };
+  if (k0 < k1) fetch(k0);
+  for (int k = k0; k < k1; k++) {
+    const int q = qn, dl = dln;
     const Plan &P = PV.p[q];
     const int nt = fmm_nterms(q), ms = nt - moff, ls = fmm_nterms(q - so);
-    const int B = src[k];
-    const T *D = clsD + (size_t)cls[k] * dstr;
-    const int dl = la - (int)clevel[B];
     __syncwarp();
-    for (int i = lane; i < nt; i += 32) sA[w][i] = D[i];
-    for (int j = lane; j < ms; j += 32) sB[w][j] = M[(size_t)B * mstr + j] * exp2i<T>(dl * (int)c_mi[j + moff][3]);
+#pragma unroll
+    for (int r = 0; r < M2LV_R; r++) {
+      const int i = lane + 32 * r;
+      if (i < nt) sA[w][i] = dr[r];
+      if (i < ms) sB[w][i] = mr[r] * exp2i<T>(dl * (int)c_mi[i + moff][3]);
+    }
     for (int s = lane; s < P.nseg; s += 32) sS[w][s] = T(0);
     __syncwarp();
+    if (k + 1 < k1) fetch(k + 1);
     engine_run<T>(P, sA[w], sB[w], sS[w], lane);
     __syncwarp();
 #pragma unroll
