@@ -11,7 +11,9 @@
 //   L2L:  L^_child[n]  += 2^-(|n|+1) sum_{|n|+|k| <= p-so} mono_o(k) L^_parent[n+k],  d = child - parent
 // The operators are built once per (order, source order) in FP64 and kept as
 // FP32 tables of (coefficient per octant, input term) entries, grouped by output
-// term; one thread computes one output term of one cell.
+// term.  One thread computes one output term of one parent (L2L: of all its
+// children at once); in L2L the few parents of the upper levels take a warp per
+// term.
 #include <map>
 #include <mutex>
 #include <vector>
@@ -24,6 +26,7 @@ struct ShiftTab {
   const int *off = nullptr;     // [nout + 1] entries of each output term
   const int *in = nullptr;      // [nent] input term (row-relative)
   const float *coef = nullptr;  // [8][nent] coefficient per octant
+  const float4 *coef8 = nullptr;  // [nent][2]: the eight octants' coefficients of an entry side by side
   void *dmem = nullptr;
 };
 struct ShiftSet {
@@ -49,21 +52,29 @@ void sign_of(int o, double &sx, double &sy, double &sz) {
 }
 
 int upload(ShiftTab &t, const std::vector<int> &off, const std::vector<int> &in, const std::vector<float> &coef) {
-  const size_t b0 = off.size() * 4, b1 = (in.size() ? in.size() : 1) * 4, b2 = (coef.size() ? coef.size() : 8) * 4;
-  const size_t o1 = (b0 + 255) & ~(size_t)255, o2 = o1 + ((b1 + 255) & ~(size_t)255);
+  const size_t nent = in.size();
+  std::vector<float> c8(8 * (nent ? nent : 1), 0.f);  // [entry][octant]
+  for (size_t e = 0; e < nent; e++)
+    for (int o = 0; o < 8; o++) c8[8 * e + o] = coef[(size_t)o * nent + e];
+  const size_t b0 = off.size() * 4, b1 = (nent ? nent : 1) * 4, b2 = (coef.size() ? coef.size() : 8) * 4,
+               b3 = c8.size() * 4;
+  const size_t o1 = (b0 + 255) & ~(size_t)255, o2 = o1 + ((b1 + 255) & ~(size_t)255),
+               o3 = o2 + ((b2 + 255) & ~(size_t)255);
   char *d = nullptr;
-  if (cudaMalloc((void **)&d, o2 + b2) != cudaSuccess) return FMM_ERR_CUDA;
+  if (cudaMalloc((void **)&d, o3 + b3) != cudaSuccess) return FMM_ERR_CUDA;
   if (cudaMemcpy(d, off.data(), b0, cudaMemcpyHostToDevice) != cudaSuccess ||
-      (in.size() && cudaMemcpy(d + o1, in.data(), in.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
-      (coef.size() && cudaMemcpy(d + o2, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)) {
+      (nent && cudaMemcpy(d + o1, in.data(), nent * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (coef.size() && cudaMemcpy(d + o2, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+      cudaMemcpy(d + o3, c8.data(), b3, cudaMemcpyHostToDevice) != cudaSuccess) {
     cudaFree(d);
     return FMM_ERR_CUDA;
   }
   t.nout = (int)off.size() - 1;
-  t.nent = (int)in.size();
+  t.nent = (int)nent;
   t.off = (const int *)d;
   t.in = (const int *)(d + o1);
   t.coef = (const float *)(d + o2);
+  t.coef8 = (const float4 *)(d + o3);
   t.dmem = d;
   return FMM_OK;
 }
@@ -152,20 +163,66 @@ __global__ void k_m2m_tab(int lo, int hi, int msize, ShiftTab T, const unsigned 
   M[(size_t)c * mstr + n] = acc;
 }
 
-// one thread per (child of the level, output term), added into the child
-__global__ void k_l2l_tab(int lo, int hi, int lsize, ShiftTab T, const int *parent, const double *cx,
-                          const double *cy, const double *cz, float *L, int lstr) {
+// one thread per (parent of the level, output term): each entry's parent term
+// is loaded once for all eight octants, and every child's output is added into it
+__global__ void k_l2l_tab(int lo, int hi, int lsize, ShiftTab T, const unsigned char *child_mask,
+                          const int *child_first, float *L, int lstr) {
   const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const int c = lo + (int)(g / lsize), n = (int)(g % lsize);
-  if (c >= hi) return;
-  const int p = parent[c];
-  const int o = child_octant(cx[p], cy[p], cz[p], cx[c], cy[c], cz[c]);
-  const float *co = T.coef + (size_t)o * T.nent;
+  const int p = lo + (int)(g / lsize), n = (int)(g % lsize);
+  if (p >= hi) return;
+  const unsigned mask = child_mask[p];
+  if (!mask) return;
   const float *Lp = L + (size_t)p * lstr;
-  float acc = 0.f;
-  for (int e = T.off[n]; e < T.off[n + 1]; e++) acc = fmaf(co[e], Lp[T.in[e]], acc);
-  L[(size_t)c * lstr + n] += acc;
+  float a[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) a[o] = 0.f;
+  for (int e = T.off[n]; e < T.off[n + 1]; e++) {
+    const float x = Lp[T.in[e]];
+    const float4 c0 = T.coef8[2 * e], c1 = T.coef8[2 * e + 1];
+    a[0] = fmaf(c0.x, x, a[0]); a[1] = fmaf(c0.y, x, a[1]); a[2] = fmaf(c0.z, x, a[2]); a[3] = fmaf(c0.w, x, a[3]);
+    a[4] = fmaf(c1.x, x, a[4]); a[5] = fmaf(c1.y, x, a[5]); a[6] = fmaf(c1.z, x, a[6]); a[7] = fmaf(c1.w, x, a[7]);
+  }
+  // children are stored in octant order after child_first
+  int ch = child_first[p];
+#pragma unroll
+  for (int o = 0; o < 8; o++)
+    if (mask & (1u << o)) L[(size_t)(ch++) * lstr + n] += a[o];
 }
+
+// L2L for the few parents of the upper levels, one warp per (parent, output
+// term): the lanes split the term's entries and the warp sums them (a thread
+// per term would walk up to NT(p) dependent entries alone).
+__global__ void k_l2l_tab_warp(int lo, int hi, int lsize, ShiftTab T, const unsigned char *child_mask,
+                               const int *child_first, float *L, int lstr) {
+  const long g = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int p = lo + (int)(g / lsize), n = (int)(g % lsize);
+  if (p >= hi) return;
+  const unsigned mask = child_mask[p];
+  if (!mask) return;
+  const float *Lp = L + (size_t)p * lstr;
+  float a[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) a[o] = 0.f;
+  for (int e = T.off[n] + lane; e < T.off[n + 1]; e += 32) {
+    const float x = Lp[T.in[e]];
+    const float4 c0 = T.coef8[2 * e], c1 = T.coef8[2 * e + 1];
+    a[0] = fmaf(c0.x, x, a[0]); a[1] = fmaf(c0.y, x, a[1]); a[2] = fmaf(c0.z, x, a[2]); a[3] = fmaf(c0.w, x, a[3]);
+    a[4] = fmaf(c1.x, x, a[4]); a[5] = fmaf(c1.y, x, a[5]); a[6] = fmaf(c1.z, x, a[6]); a[7] = fmaf(c1.w, x, a[7]);
+  }
+#pragma unroll
+  for (int o = 0; o < 8; o++)
+    for (int d = 16; d; d >>= 1) a[o] += __shfl_xor_sync(0xffffffffu, a[o], d);
+  if (lane == 0) {
+    int ch = child_first[p];
+#pragma unroll
+    for (int o = 0; o < 8; o++)
+      if (mask & (1u << o)) L[(size_t)(ch++) * lstr + n] += a[o];
+  }
+}
+
+// levels with fewer parents than this use the warp-per-term L2L
+constexpr int SHIFT_WARP_BELOW = 2048;
 
 }  // namespace
 
@@ -183,14 +240,25 @@ int fmm_m2m_tab(DevTree *t, int lo, int hi, float *M, int mstr, cudaStream_t st)
   return FMM_OK;
 }
 
+// L2L into the children [lo, hi) of one level, from their parents (the level above)
 int fmm_l2l_tab(DevTree *t, int lo, int hi, float *L, int lstr, cudaStream_t st) {
   const ShiftSet *S = get_shift(t->order, t->so);
   if (!S) return FMM_ERR_CUDA;
+  if (hi <= lo) return FMM_OK;
+  // the parents of [lo, hi): the cells of the level above
+  int l = 1;
+  while (l < t->nlevels && t->level_off[l] != lo) l++;
+  if (l >= t->nlevels) return FMM_ERR_STATE;
+  const int plo = t->level_off[l - 1], phi = t->level_off[l];
   const int lsize = S->l2l.nout;
-  const long n = (long)(hi - lo) * lsize;
-  if (n <= 0) return FMM_OK;
-  fmm_note_launch(), k_l2l_tab<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lo, hi, lsize, S->l2l, t->parent.p,
-                                                                          t->cx.p, t->cy.p, t->cz.p, L, lstr);
+  const long n = (long)(phi - plo) * lsize;
+  if (phi - plo < SHIFT_WARP_BELOW)
+    fmm_note_launch(), k_l2l_tab_warp<<<(unsigned)((32 * n + 255) / 256), 256, 0, st>>>(
+        plo, phi, lsize, S->l2l, t->child_mask.p, t->child_first.p, L, lstr);
+  else
+    fmm_note_launch(), k_l2l_tab<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(plo, phi, lsize, S->l2l,
+                                                                            t->child_mask.p, t->child_first.p, L,
+                                                                            lstr);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
