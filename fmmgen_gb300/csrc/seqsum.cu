@@ -270,8 +270,8 @@ __device__ __forceinline__ ChunkMap cm_shfl_up(const ChunkMap &m, int d) {
   return o;
 }
 
-// Chains the chunk maps in order, exactly: one warp per axis, 32 chunks at a
-// time.  The state (s, or S in ulps of binade e) is kept identical in every
+// Chains the chunk maps in order, exactly: one warp per axis (each on its own
+// SM), 32 chunks at a time.  The state (s, or S in ulps of binade e) is kept identical in every
 // lane.  From the current chunk j of a block, the lanes compose the maps of
 // chunks j..lane (a warp scan); the longest run of composites that is valid
 // for the exact S is applied in one step.  A chunk that no composite covers
@@ -280,10 +280,9 @@ __device__ __forceinline__ ChunkMap cm_shfl_up(const ChunkMap &m, int d) {
 // first element whose result leaves the binade, and only that element takes a
 // plain sequential FP64 add.
 __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks, const ChunkMap *maps, double *out) {
-  __shared__ double sx[3][SS_C];
+  __shared__ double sx[1][SS_C];
   const unsigned FULL = 0xffffffffu;
-  const int a = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (a >= 3) return;
+  const int a = blockIdx.x, lane = threadIdx.x & 31;  // one axis per block, so per SM
   const long long LO = 1ll << 52, HI = 1ll << 53;
   double s = 0.0;
   bool imode = false;
@@ -340,9 +339,9 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
       __syncwarp();
       if (pref_k == k) {
 #pragma unroll
-        for (int t = 0; t < SS_PER_LANE; t++) sx[a][lane + 32 * t] = pr[t];
+        for (int t = 0; t < SS_PER_LANE; t++) sx[0][lane + 32 * t] = pr[t];
       } else {
-        for (int i = lane; i < n; i += 32) sx[a][i] = pos[3 * (i0 + i) + a];
+        for (int i = lane; i < n; i += 32) sx[0][i] = pos[3 * (i0 + i) + a];
       }
       pref_k = k + 1;
 #pragma unroll
@@ -353,12 +352,12 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
       __syncwarp();
       for (int b = 0; b < n; b += 32) {
         int cnt = min(32, n - b);
-        double xj = lane < cnt ? sx[a][b + lane] : 0.0;
+        double xj = lane < cnt ? sx[0][b + lane] : 0.0;
         int c = 0;
         while (c < cnt) {
           if (!imode) {
             if (!ss_from_double(s, e, S)) {
-              s = __dadd_rn(s, sx[a][b + c]);
+              s = __dadd_rn(s, sx[0][b + c]);
               c++;
               continue;
             }
@@ -385,7 +384,7 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
             int x = __ffs(bal) - 1;
             long long Sb = __shfl_sync(FULL, Sj, x > 0 ? x - 1 : 0);
             if (x == c) Sb = S;
-            s = __dadd_rn(ss_to_double(Sb, e), sx[a][b + x]);
+            s = __dadd_rn(ss_to_double(Sb, e), sx[0][b + x]);
             imode = false;
             c = x + 1;
           }
@@ -415,7 +414,7 @@ int fmm_seqsum3(const double *pos, long N, double *out, void *scratch, cudaStrea
   fmm_note_launch(), k_ss_chunksum<<<g, 128, 0, st>>>(pos, N, nch, csum);
   fmm_note_launch(), k_ss_prefix<<<3, 1024, 0, st>>>(csum, nch, start);
   fmm_note_launch(), k_ss_maps<<<g, 128, 0, st>>>(pos, N, nch, start, maps);
-  fmm_note_launch(), k_ss_chain<<<1, 96, 0, st>>>(pos, N, nch, maps, out);
+  fmm_note_launch(), k_ss_chain<<<3, 32, 0, st>>>(pos, N, nch, maps, out);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
