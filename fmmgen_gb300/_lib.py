@@ -61,6 +61,7 @@ _SIGS = {
     "fmmgen_tree_free": (C.c_int, [_vp]),
     "fmmgen_root_box_noalloc": (C.c_int, [_dp, C.c_long, _dp, _vp]),
     "fmmgen_tree_info": (C.c_int, [_vp, _lp]),
+    "fmmgen_tree_counts": (C.c_int, [_vp, _lp]),
     "fmmgen_tree_root": (C.c_int, [_vp, _dp]),
     "fmmgen_tree_nsys": (C.c_int, [_vp]),
     "fmmgen_tree_set_graph": (C.c_int, [_vp, C.c_int]),

@@ -252,13 +252,18 @@ int fmmgen_tree_free(fmmgen_tree *tree) {
   return FMM_OK;
 }
 
-int fmmgen_tree_info(fmmgen_tree *tree, long *info) {
+int fmmgen_tree_counts(fmmgen_tree *tree, long *info) {
   g_err.clear();
   if (!tree || !tree->built || !info) return ret(FMM_ERR_STATE);
   DevTree &t = tree->t;
   info[0] = t.ncells; info[1] = t.nleaves; info[2] = t.nm2l; info[3] = t.np2p;
   info[4] = t.nlevels; info[5] = t.nclasses; info[6] = t.N; info[7] = t.ncrit;
-  info[8] = (long)t.p2p_interactions;
+  return FMM_OK;
+}
+
+int fmmgen_tree_info(fmmgen_tree *tree, long *info) {
+  if (int rc = fmmgen_tree_counts(tree, info)) return rc;
+  info[8] = (long)fmm_p2p_interactions(&tree->t);
   return FMM_OK;
 }
 

@@ -42,7 +42,9 @@ struct DevTree {
   std::vector<int> level_off;
   int ncells = 0, nleaves = 0;
   long nm2l = 0, np2p = 0;
-  long long p2p_interactions = 0;  // sum over P2P pairs of n_A n_B, minus self terms
+  long long p2p_interactions = 0;  // sum over P2P pairs of n_A n_B, minus self terms (fmm_p2p_interactions)
+  DevBuf<unsigned long long> d_p2pcount;  // ... on the device, until read
+  uint64_t p2p_count_serial = ~0ull;      // build whose count d_p2pcount holds, not yet read
   int nclasses = 0;
   uint32_t eflags = 0;
 
@@ -178,6 +180,7 @@ int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st);
 // the M2L pairs grouped by target and sorted by class within a target (CSR
 // m2l_off / m2l_src / m2l_cls), once per build, for the kernels that read them
 int fmm_m2l_csr(DevTree *t, cudaStream_t st);
+long long fmm_p2p_interactions(DevTree *t);  // reads the build's count (synchronous)
 int fmm_m2l_p2p_only(DevTree *t, const double *S, int precision, cudaStream_t st);  // M2L + P2P alone (after a pass)
 int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_cand, int *cand4, float *cand_ms,
                  int *ncand, cudaStream_t st);

@@ -955,15 +955,27 @@ static int build_lists(DevTree *t, cudaStream_t st) {
   t->nm2l = nm2l;
   t->np2p = np2p;
   TRY(group_by_target(t, p2p_tgt_raw, p2p_src_raw, nullptr, 0, np2p, t->p2p_off, t->p2p_src, nullptr, st));
-  TRY(tmp_reserve(t, 64));
-  unsigned long long *d = (unsigned long long *)t->tmp.p;
-  FMM_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(*d), st));
-  fmm_note_launch(), k_p2p_count<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->p2p_off.p, t->p2p_src.p, nc, t->pcount.p, d);
+  // the interaction count is a statistic: read when asked for (fmm_p2p_interactions)
+  TRY(fmm_reserve(t->d_p2pcount, 1));
+  FMM_CUDA_TRY(cudaMemsetAsync(t->d_p2pcount.p, 0, sizeof(unsigned long long), st));
+  fmm_note_launch(), k_p2p_count<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->p2p_off.p, t->p2p_src.p, nc, t->pcount.p,
+                                                                       t->d_p2pcount.p);
   FMM_CUDA_TRY(cudaGetLastError());
-  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned, d, sizeof(*d), cudaMemcpyDeviceToHost, st));
-  FMM_CUDA_TRY(cudaStreamSynchronize(st));
-  t->p2p_interactions = (long long)*(unsigned long long *)t->h_pinned;
+  t->p2p_count_serial = t->build_serial;
   return FMM_OK;
+}
+
+long long fmm_p2p_interactions(DevTree *t) {
+  if (t->p2p_count_serial == t->build_serial) {
+    unsigned long long v = 0;
+    // the count kernel ran on the build's stream, which may not block with the default one
+    if (cudaDeviceSynchronize() == cudaSuccess &&
+        cudaMemcpy(&v, t->d_p2pcount.p, sizeof(v), cudaMemcpyDeviceToHost) == cudaSuccess) {
+      t->p2p_interactions = (long long)v;
+      t->p2p_count_serial = ~0ull;
+    }
+  }
+  return t->p2p_interactions;
 }
 
 // particle-particle interactions of the P2P list (self pairs skip i == j)
@@ -1151,6 +1163,7 @@ void fmm_tree_destroy(DevTree *t) {
   t->sched_serial = ~0ull;
   t->tc_serial = ~0ull;
   fmm_release(t->wdec);
+  fmm_release(t->d_p2pcount);
   fmm_release(t->m2l_ord); fmm_release(t->mnorm); fmm_release(t->feat); fmm_release(t->tscale); fmm_release(t->tpart);
   fmm_release(t->sys_pairs);
   fmm_release(t->ltgt);

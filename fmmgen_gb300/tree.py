@@ -75,11 +75,21 @@ class Tree:
             check(lib().fmmgen_forest_build(C.c_void_p(self.pos.data_ptr()), self.sys_off.ctypes.data,
                                             len(self.sys_off) - 1, self.ncrit, self.order, self.theta,
                                             self.source_order, _stream_ptr(stream), C.byref(self._h)))
+        self._counts()
+        return self
+
+    def _counts(self):
+        info = np.zeros(8, dtype=np.int64)
+        check(lib().fmmgen_tree_counts(self._h, info.ctypes.data))  # does not wait for the device
+        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _) = (int(v) for v in info)
+
+    @property
+    def p2p_interactions(self):
+        """Particle-particle interactions of the P2P list (self pairs excluded);
+        waits for the build's work on the device."""
         info = np.zeros(9, dtype=np.int64)
         check(lib().fmmgen_tree_info(self._h, info.ctypes.data))
-        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _,
-         self.p2p_interactions) = (int(v) for v in info)
-        return self
+        return int(info[8])
 
     def rebuild_compute(self, pos=None, F=None, S=None, potential=True, field=True, precision="mixed",
                         stream=None):
@@ -107,10 +117,7 @@ class Tree:
             len(off) - 1 if off is not None else 1, self.N, self.ncrit, self.order, self.theta, self.source_order,
             C.c_void_p(self.S.data_ptr()), C.c_void_p(Fd.data_ptr()), int(potential), int(field),
             PRECISIONS[precision], _stream_ptr(stream), C.byref(self._h)))
-        info = np.zeros(9, dtype=np.int64)
-        check(lib().fmmgen_tree_info(self._h, info.ctypes.data))
-        (self.ncells, self.nleaves, self.nm2l, self.np2p, self.nlevels, self.nclasses, _, _,
-         self.p2p_interactions) = (int(v) for v in info)
+        self._counts()
         if host_out:
             F[...] = Fd.reshape(np.shape(F)).cpu().numpy() if isinstance(F, np.ndarray) else Fd.cpu()
             return F

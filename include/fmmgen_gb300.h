@@ -156,8 +156,10 @@ int fmmgen_tree_free(fmmgen_tree *tree);
 int fmmgen_root_box_noalloc(const double *pos, long N, double *root4, void *stream);
 
 /* Introspection (host outputs; synchronises).
- * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions]. */
+ * info: [ncells, nleaves, nm2l, np2p, nlevels, nclasses, N, ncrit, P2P particle interactions].
+ * fmmgen_tree_counts fills the first eight without waiting for the device. */
 int fmmgen_tree_info(fmmgen_tree *tree, long *info);
+int fmmgen_tree_counts(fmmgen_tree *tree, long *info8);
 /* build_tree + Tree::compute_field_fmm in one call (fmmgen_tree_build /
  * fmmgen_forest_build, then fmmgen_tree_compute_field_fmm, on the same
  * handle): the near field and the multipoles are computed on a second stream
