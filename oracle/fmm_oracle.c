@@ -43,6 +43,8 @@ long or_nterms(int p) { return p < 0 ? 0 : (long)(p + 1) * (p + 2) * (p + 3) / 6
 /* Msize/Lsize (example/utils.cpp:18-27). */
 long or_msize(int order, int so) { return or_nterms(order) - or_nterms(so - 1); }
 long or_lsize(int order, int so) { return or_nterms(order - so); }
+/* source components: the degree-so M coefficients (1 charge, 3 dipole, 6 quadrupole) */
+long or_sourcesize(int so) { return or_nterms(so) - or_nterms(so - 1); }
 
 /* Flat index of (nx,ny,nz) in the full layout: ordered by total degree, then
  * nx descending, then ny descending (grevlex on [z,y,x], fmmgen/utils.py:103-109). */
@@ -246,9 +248,18 @@ void or_M2P(double x, double y, double z, const double *M, double *F, int order,
 
 /* P2P: Coulomb  phi += q/R, E += q r/R^3 (example/operators.cpp:54-66);
  * dipole (source_order=1, S = degree-1 M coefficients):
- *   phi += -S.r/R^3, E += S/R^3 - 3 (S.r) r / R^5  (fmmgen/generator.py:257-288 potential). */
+ *   phi += -S.r/R^3, E += S/R^3 - 3 (S.r) r / R^5  (fmmgen/generator.py:257-288 potential);
+ * higher source orders (S = the degree-so M coefficients): the generator's
+ * P2P potential V = L_0 of a multipole whose only terms are S
+ * (fmmgen/generator.py:257-288), i.e. M2P at order so, with the exact field. */
+void or_M2P(double x, double y, double z, const double *M, double *F, int order, int so, int potential,
+            int field);
 void or_P2P(double x, double y, double z, const double *S, double *F, int so, int potential,
             int field) {
+    if (so >= 2) {
+        or_M2P(x, y, z, S, F, so, so, potential, field);
+        return;
+    }
     double R = sqrt(x * x + y * y + z * z);
     double phi, ex, ey, ez;
     if (so == 0) {
@@ -384,7 +395,7 @@ static void interact(otree_t *t, long A, long B) {
 void *or_tree_build(const double *pos, const double *S, long N, long ncrit, int order,
                     double theta, int so, int *err) {
     *err = 0;
-    if (N <= 0 || ncrit < 1 || order < 0 || order > OR_PMAX || so < 0 || so > 1) { *err = 1; return NULL; }
+    if (N <= 0 || ncrit < 1 || order < 0 || order > OR_PMAX || so < 0 || so > 2) { *err = 1; return NULL; }
     otree_t *t = (otree_t *)calloc(1, sizeof(otree_t));
     t->N = N; t->ncrit = ncrit; t->order = order; t->so = so; t->theta = theta;
     t->pos = pos; t->S = S;
@@ -515,7 +526,7 @@ static void csr_by_target(long npairs, const long *pairs, int tgt_slot, long nce
  * order); returns the P2M seconds through *tp2m. */
 static void or_tree_multipoles_t(otree_t *t, double *M, double *tp2m) {
     int order = t->order, so = t->so;
-    int ssize = so == 0 ? 1 : 3;
+    int ssize = (int)or_sourcesize(so);
     long msize = or_msize(order, so);
     long nc = t->ncells, ncrit = t->ncrit;
     double t0 = now_s();
@@ -557,7 +568,7 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     mi_init();
     int order = t->order, so = t->so;
     int outsize = (potential ? 1 : 0) + (field ? 3 : 0);
-    int ssize = so == 0 ? 1 : 3;
+    int ssize = (int)or_sourcesize(so);
     long msize = or_msize(order, so), lsize = or_lsize(order, so);
     long nc = t->ncells, N = t->N, ncrit = t->ncrit;
     if (sample_stride < 1) sample_stride = 1;
@@ -640,7 +651,7 @@ static void bh_walk(const otree_t *t, const double *M, long p, long i, double *F
                     int field) {
     const ocell_t *cp = &t->cells[p];
     long msize = or_msize(t->order, t->so);
-    int ssize = t->so == 0 ? 1 : 3;
+    int ssize = (int)or_sourcesize(t->so);
     if (cp->nleaf >= t->ncrit) {
         for (int o = 0; o < 8; o++) {
             if (!(cp->nchild & (1u << o))) continue;
@@ -683,7 +694,7 @@ void or_tree_evaluate_bh(void *h, double *F, int potential, int field) {
 void or_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
                int potential, int field, double *F) {
     int outsize = (potential ? 1 : 0) + (field ? 3 : 0);
-    int ssize = so == 0 ? 1 : 3;
+    int ssize = (int)or_sourcesize(so);
     memset(F, 0, sizeof(double) * ntargets * outsize);
 #pragma omp parallel for schedule(dynamic, 4)
     for (long t = 0; t < ntargets; t++) {

@@ -64,6 +64,11 @@ def nterms(p):
     return int(lib().or_nterms(p))
 
 
+def sourcesize(so):
+    """Components of a source: the degree-so multipole coefficients (1, 3, 6)."""
+    return nterms(so) - nterms(so - 1)
+
+
 def msize(order, so):
     return nterms(order) - nterms(so - 1)
 
@@ -116,7 +121,7 @@ class OracleTree:
 
     def __init__(self, pos, S, ncrit, order, theta, source_order=0):
         self.pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
-        ss = 1 if source_order == 0 else 3
+        ss = sourcesize(source_order)
         self.S = np.ascontiguousarray(S, dtype=np.float64).reshape(-1, ss)
         self.N = self.pos.shape[0]
         self.ncrit, self.order, self.theta, self.so = ncrit, order, theta, source_order
@@ -191,7 +196,7 @@ class OracleTree:
 def direct(pos, S, targets=None, source_order=0, potential=True, field=True):
     """evaluate_direct (example/calculate.cpp:252-264) on a target subset."""
     pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
-    ss = 1 if source_order == 0 else 3
+    ss = sourcesize(source_order)
     S = np.ascontiguousarray(S, dtype=np.float64).reshape(-1, ss)
     N = pos.shape[0]
     if targets is None:
@@ -254,7 +259,7 @@ class RefTree:
     def __init__(self, pos, S, ncrit, order, theta, source_order=0):
         self.L = ref(source_order)
         self.pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
-        ss = 1 if source_order == 0 else 3
+        ss = sourcesize(source_order)
         self.S = np.ascontiguousarray(S, dtype=np.float64).reshape(-1, ss)
         self.N = self.pos.shape[0]
         self.ncrit, self.order, self.so = ncrit, order, source_order

@@ -5,17 +5,18 @@ Recipe, run in the development container where the reference checkout exists:
      checkout) emits operators.{cpp,h} for Coulomb (source_order=0, orders
      1..PMAX0) and dipole (source_order=1, orders 2..PMAX1) sources, with the
      settings of the reference's example/example.py (CSE, harmonic derivatives,
-     minpow=11, atomic, C++).
+     minpow=11, atomic, C++), and for quadrupole sources (source_order=2,
+     orders 3..PMAX2).
   2. g++ compiles the reference's example/tree.cpp, calculate.cpp, utils.cpp
      where they lie in the checkout, plus the generated operators and
-     oracle/ref/ref_harness.cpp, into oracle/_ref/libref_so{0,1}.so.
+     oracle/ref/ref_harness.cpp, into oracle/_ref/libref_so{0,1,2}.so.
      -ffp-contract=off keeps every FP64 expression as written (no FMA
      contraction), which the bit-exact tree/list comparisons rely on.
 
 Outputs are cached: a step is skipped when its output is newer than its inputs.
 Nothing here is shipped; the GPU machine never runs it.
 
-Usage: python oracle/ref/build_ref.py [--reference DIR] [--pmax0 8] [--pmax1 6]
+Usage: python oracle/ref/build_ref.py [--reference DIR] [--pmax0 8] [--pmax1 6] [--pmax2 5]
 """
 import argparse
 import contextlib
@@ -68,13 +69,13 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(ref=DEFAULT_REF, pmax0=8, pmax1=6, jobs=4, verbose=True):
+def build(ref=DEFAULT_REF, pmax0=8, pmax1=6, pmax2=5, jobs=4, verbose=True):
     """Generate + compile; returns {source_order: path to .so}.  Raises if the
     reference checkout is absent."""
     ex = os.path.join(ref, "example")
     if not os.path.isdir(ex):
         raise FileNotFoundError(f"reference checkout not found at {ref}")
-    specs = [(0, pmax0), (1, pmax1)]
+    specs = [(0, pmax0), (1, pmax1), (2, pmax2)]
     gen_jobs = []
     for so, pmax in specs:
         outdir = os.path.join(OUT, f"so{so}_p{pmax}")
@@ -126,8 +127,9 @@ def main():
     ap.add_argument("--reference", default=DEFAULT_REF)
     ap.add_argument("--pmax0", type=int, default=8)
     ap.add_argument("--pmax1", type=int, default=6)
+    ap.add_argument("--pmax2", type=int, default=5)
     a = ap.parse_args()
-    print(build(a.reference, a.pmax0, a.pmax1))
+    print(build(a.reference, a.pmax0, a.pmax1, a.pmax2))
 
 
 if __name__ == "__main__":

@@ -29,13 +29,32 @@ void P2P(double x, double y, double z, double *S, double *F) {
 #if FMMGEN_SOURCEORDER == 0
   double r3 = 1.0 / (R * R * R);
   double phi = S[0] / R, ex = S[0] * x * r3, ey = S[0] * y * r3, ez = S[0] * z * r3;
-#else
+#elif FMMGEN_SOURCEORDER == 1
   double rinv = 1.0 / R, r3 = rinv * rinv * rinv, r5 = r3 * rinv * rinv;
   double sr = S[0] * x + S[1] * y + S[2] * z;
   double phi = -sr * r3;
   double ex = S[0] * r3 - 3.0 * sr * x * r5;
   double ey = S[1] * r3 - 3.0 * sr * y * r5;
   double ez = S[2] * r3 - 3.0 * sr * z * r5;
+#else
+  // quadrupole (source_order 2, S = the degree-2 M coefficients xx xy xz yy yz zz):
+  // phi = sum_m S_m d^m (1/R), E_a = -sum_m S_m d^(m+e_a) (1/R), with
+  // d_i d_j (1/R) = (3 r_i r_j - delta_ij R^2) / R^5 and
+  // d_i d_j d_k (1/R) = -15 r_i r_j r_k / R^7 + 3 (delta_ij r_k + delta_ik r_j + delta_jk r_i) / R^5
+  const double r[3] = {x, y, z};
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+  double rinv = 1.0 / R, r2 = R * R, r5 = rinv * rinv * rinv * rinv * rinv, r7 = r5 * rinv * rinv;
+  double phi = 0, e[3] = {0, 0, 0};
+  for (int m = 0; m < 6; m++) {
+    const int i = pi[m], j = pj[m];
+    phi += S[m] * (3.0 * r[i] * r[j] - (i == j ? r2 : 0.0)) * r5;
+    for (int a = 0; a < 3; a++) {
+      double d3 = -15.0 * r[i] * r[j] * r[a] * r7 +
+                  3.0 * ((i == j ? r[a] : 0.0) + (i == a ? r[j] : 0.0) + (j == a ? r[i] : 0.0)) * r5;
+      e[a] -= S[m] * d3;
+    }
+  }
+  double ex = e[0], ey = e[1], ez = e[2];
 #endif
 #pragma omp atomic
   F[0] += phi;

@@ -9,7 +9,8 @@ The one restated piece is P2P (the generated field is zero at HEAD); its
 potential is checked against the generated P2P here before anything is saved.
 Barnes-Hut fixtures (compute_field_bh, M2P) keep potentials only: the
 generated M2P's field is not the gradient of its potential.
-`--bh` writes only the Barnes-Hut fixtures.
+`--bh` writes only the Barnes-Hut fixtures; `--so2` only the quadrupole-source
+fixtures (ops_so2.npz, tree_quadrupole_plummer.npz, m2p_potential_so2.npz).
 """
 import hashlib
 import os
@@ -29,9 +30,9 @@ def list_digest(pairs):
     return hashlib.sha256(a[order].tobytes()).hexdigest()
 
 
-def make_ops():
-    rng = np.random.default_rng(2024)
-    for so, (pmin, pmax) in ((0, (1, 8)), (1, (2, 6))):
+def make_ops(specs=((0, (1, 8)), (1, (2, 6))), seed=2024):
+    rng = np.random.default_rng(seed)
+    for so, (pmin, pmax) in specs:
         R = O.ref(so)
         out = {}
         K = 6
@@ -56,7 +57,7 @@ def make_ops():
             for k, v in res.items():
                 out[f"p{p}_{k}"] = np.array(v)
         # P2P: restated physics; its potential must equal the generated P2P's
-        ss = 1 if so == 0 else 3
+        ss = O.sourcesize(so)
         d = rng.uniform(-1, 1, (16, 3))
         S = rng.standard_normal((16, ss))
         Fr = np.zeros((16, 4))
@@ -98,11 +99,14 @@ CASES = {
     "clustered": (5000, 16, 5, 0.4, 0, "clusters"),
     "tiny": (50, 64, 3, 0.5, 0, "uniform"),
     "example_scaled": (2000, 64, 4, 0.5, 0, "example"),
+    "quadrupole_plummer": (3000, 32, 4, 0.5, 2, "plummer"),
 }
 
 
-def make_trees():
+def make_trees(only=None):
     for seed, (name, (N, ncrit, p, theta, so, gen)) in enumerate(CASES.items()):
+        if only is not None and name not in only:
+            continue
         rng = np.random.default_rng(seed)
         if gen == "uniform":
             pos = rng.uniform(0, 1, (N, 3))
@@ -112,7 +116,7 @@ def make_trees():
             pos = clusters(rng, N)
         else:  # the example driver's data: U(-1,1) scaled by 1e-9 (example/main.cpp:86-110)
             pos = rng.uniform(-1, 1, (N, 3)) * 1e-9
-        S = rng.uniform(-1, 1, (N, 1)) if so == 0 else rng.standard_normal((N, 3))
+        S = rng.uniform(-1, 1, (N, 1)) if so == 0 else rng.standard_normal((N, O.sourcesize(so)))
         rt = O.RefTree(pos, S, ncrit, p, theta, so)
         cells = rt.cells()
         m2l, p2p = rt.lists()
@@ -175,8 +179,33 @@ def make_bh():
     print("m2p_potential.npz")
 
 
+def make_m2p(specs, name, seed):
+    """The generated M2P's potential at every order of the given source orders."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for so, (pmin, pmax) in specs:
+        R = O.ref(so)
+        for p in range(pmin, pmax + 1):
+            K = 5
+            d = rng.uniform(-1, 1, (K, 3))
+            d *= rng.uniform(1.5, 3.0, (K, 1)) / np.linalg.norm(d, axis=1, keepdims=True)
+            M = rng.standard_normal((K, O.msize(p, so)))
+            phi = np.zeros(K)
+            for k in range(K):
+                F = np.zeros(4)
+                R.ref_M2P(*d[k], np.ascontiguousarray(M[k]), F, p)
+                phi[k] = F[0]
+            out[f"so{so}_p{p}_d"], out[f"so{so}_p{p}_M"], out[f"so{so}_p{p}_phi"] = d, M, phi
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print(name)
+
+
 if __name__ == "__main__":
-    if "--bh" in sys.argv:
+    if "--so2" in sys.argv:
+        make_ops(specs=((2, (3, 5)),), seed=2025)
+        make_trees(only={"quadrupole_plummer"})
+        make_m2p(((2, (3, 5)),), "m2p_potential_so2.npz", 78)
+    elif "--bh" in sys.argv:
         make_bh()
     else:
         make_ops()

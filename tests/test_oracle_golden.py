@@ -25,7 +25,7 @@ def test_index_layout(oracle_lib):
     assert oracle_lib.msize(6, 1) == 83 and oracle_lib.lsize(6, 1) == 56
 
 
-@pytest.mark.parametrize("so", [0, 1])
+@pytest.mark.parametrize("so", [0, 1, 2])
 def test_operators_match_generated(oracle_lib, so):
     """Every operator at every generated order vs fmmgen's generated C (1e-12)."""
     g = np.load(os.path.join(GOLDEN, f"ops_so{so}.npz"))
@@ -46,7 +46,7 @@ def test_operators_match_generated(oracle_lib, so):
             assert relerr(a, g[f"p{p}_L2P"][i]) < 1e-12
 
 
-@pytest.mark.parametrize("so", [0, 1])
+@pytest.mark.parametrize("so", [0, 1, 2])
 def test_p2p_restated(oracle_lib, so):
     g = np.load(os.path.join(GOLDEN, f"ops_so{so}.npz"))
     for i in range(len(g["p2p_d"])):
@@ -85,7 +85,7 @@ def test_reference_known_answers(oracle_lib):
         assert M[0] == 0.0 and M[1] == 0.0 and M[2] == 0.0 and M[3] == 0.0 and M[4] == 2 * mux * d
 
 
-TREES = ["uniform10k", "deep", "dipole_plummer", "clustered", "tiny", "example_scaled"]
+TREES = ["uniform10k", "deep", "dipole_plummer", "clustered", "tiny", "example_scaled", "quadrupole_plummer"]
 
 
 def canonical(pairs):
@@ -128,6 +128,23 @@ def test_fmm_accuracy_vs_direct(oracle_lib):
     Fd = oracle_lib.direct(g["pos"], g["S"], idx)
     e = np.linalg.norm(F[idx, 1:] - Fd[:, 1:]) / np.linalg.norm(Fd[:, 1:])
     assert 1e-5 < e < 5e-4  # p=4, theta=0.5 truncation error
+
+
+def test_quadrupole_p2p_is_the_field_of_its_potential(oracle_lib):
+    """Quadrupole sources (source_order 2): the restated P2P field is minus the
+    gradient of the potential the generated P2P gives (central differences)."""
+    g = np.load(os.path.join(GOLDEN, "ops_so2.npz"))
+    h = 1e-6
+    for i in range(len(g["p2p_d"])):
+        d, S = g["p2p_d"][i], g["p2p_S"][i]
+        grad = []
+        for a in range(3):
+            e = np.zeros(3); e[a] = h
+            Fp, Fm = np.zeros(4), np.zeros(4)
+            oracle_lib.P2P(*(d + e), S.copy(), Fp, 2)
+            oracle_lib.P2P(*(d - e), S.copy(), Fm, 2)
+            grad.append(-(Fp[0] - Fm[0]) / (2 * h))
+        assert relerr(grad, g["p2p_F"][i][1:]) < 1e-7
 
 
 def test_oracle_rejects_coincident_points(oracle_lib):
