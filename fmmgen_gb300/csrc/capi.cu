@@ -136,7 +136,7 @@ bool order_ok(int order) {
 extern "C" {
 
 int fmmgen_configure(int so, int potential, int field, int maxorder) {
-  if (so < 0 || so > 1 || (!potential && !field) || maxorder < so || maxorder > FMM_PMAX) return ret(FMM_ERR_ARG);
+  if (so < 0 || so > 2 || (!potential && !field) || maxorder < so || maxorder > FMM_PMAX) return ret(FMM_ERR_ARG);
   std::lock_guard<std::mutex> lk(g_cfg.mu);
   g_cfg.so = so; g_cfg.potential = potential; g_cfg.field = field; g_cfg.maxorder = maxorder;
   return FMM_OK;

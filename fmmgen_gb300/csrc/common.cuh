@@ -41,6 +41,29 @@ __host__ __device__ __forceinline__ MI fmm_decode(int i) {
 #define FMM_EFLAG_KEYS 8u      // the particle keys need more levels (the build recomputes them)
 #define FMM_KEYLEVELS 10       // levels of digits in the first keys of a build
 
+// Quadrupole sources (source order 2): S holds the degree-2 multipole
+// coefficients (xx, xy, xz, yy, yz, zz) and a source at offset r = target -
+// source contributes phi = sum_m S_m d^m (1/r) and E = -grad phi (the P2P of
+// fmmgen/generator.py:257-288 for source_order 2, with the exact field).  With
+// A the symmetric matrix of S (A_ii = S_ii, A_ij = S_ij / 2) and t = trace:
+//   phi = (3 r.A.r - t r^2) / r^5,  E = 15 (r.A.r) r / r^7 - 3 (t r + 2 A r) / r^5.
+template <typename T>
+__host__ __device__ __forceinline__ void quadrupole_p2p(T x, T y, T z, const T *s, T &phi, T &ex, T &ey, T &ez) {
+  const T r2 = x * x + y * y + z * z;
+  const T rinv = T(1) / sqrt(r2), ri2 = rinv * rinv;
+  const T r5 = ri2 * ri2 * rinv, r7 = r5 * ri2;
+  const T h = T(0.5);
+  const T ax = s[0] * x + h * (s[1] * y + s[2] * z);
+  const T ay = h * (s[1] * x + s[4] * z) + s[3] * y;
+  const T az = h * (s[2] * x + s[4] * y) + s[5] * z;
+  const T rar = x * ax + y * ay + z * az, tr = s[0] + s[3] + s[5];
+  phi += (T(3) * rar - tr * r2) * r5;
+  const T c = T(15) * rar * r7, t3 = T(3) * r5;
+  ex += c * x - t3 * (tr * x + T(2) * ax);
+  ey += c * y - t3 * (tr * y + T(2) * ay);
+  ez += c * z - t3 * (tr * z + T(2) * az);
+}
+
 // Status codes of the C ABI (mirrored in include/fmmgen_gb300.h).
 #define FMM_OK 0
 #define FMM_ERR_ARG 1

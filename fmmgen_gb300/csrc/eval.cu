@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
                                                         const uint32_t *perm, const double *S, int so, int order,
                                                         const double *cr, T *M, int mstr) {
   __shared__ T tb[FMM_WARPS][3][32][FMM_PMAX + 1];
-  __shared__ T sq[FMM_WARPS][32][3];
+  __shared__ T sq[FMM_WARPS][32][6];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int leaf = blockIdx.x * FMM_WARPS + w;
   if (leaf >= nleaves) return;
@@ -116,10 +116,12 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
       uint32_t o = perm[i];
       if (so == 0) {
         sq[w][lane][0] = (T)S[o];
-      } else {
+      } else if (so == 1) {
         sq[w][lane][0] = (T)(S[3 * (size_t)o] * inv_s);
         sq[w][lane][1] = (T)(S[3 * (size_t)o + 1] * inv_s);
         sq[w][lane][2] = (T)(S[3 * (size_t)o + 2] * inv_s);
+      } else {  // quadrupole: the degree-2 coefficients, scaled by 1 / s^2
+        for (int k = 0; k < 6; k++) sq[w][lane][k] = (T)(S[6 * (size_t)o + k] * inv_s * inv_s);
       }
     }
     __syncwarp();
@@ -133,12 +135,22 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_p2m(const int *leaf_cells, i
         if (so == 0) {
           for (int jj = 0; jj < cnt; jj++)
             sum += sq[w][jj][0] * tb[w][0][jj][nx] * tb[w][1][jj][ny] * tb[w][2][jj][nz];
-        } else {
+        } else if (so == 1) {
           for (int jj = 0; jj < cnt; jj++) {
             if (nx) sum += sq[w][jj][0] * tb[w][0][jj][nx - 1] * tb[w][1][jj][ny] * tb[w][2][jj][nz];
             if (ny) sum += sq[w][jj][1] * tb[w][0][jj][nx] * tb[w][1][jj][ny - 1] * tb[w][2][jj][nz];
             if (nz) sum += sq[w][jj][2] * tb[w][0][jj][nx] * tb[w][1][jj][ny] * tb[w][2][jj][nz - 1];
           }
+        } else {
+          // M~_n += sum_{|k| = 2, k <= n} S~_k u^(n-k) / (n-k)!, k in the layout
+          // order xx xy xz yy yz zz
+          for (int jj = 0; jj < cnt; jj++)
+#pragma unroll
+            for (int kk = 0; kk < 6; kk++) {
+              const int kx = c_mi[4 + kk][0], ky = c_mi[4 + kk][1], kz = c_mi[4 + kk][2];
+              if (nx >= kx && ny >= ky && nz >= kz)
+                sum += sq[w][jj][kk] * tb[w][0][jj][nx - kx] * tb[w][1][jj][ny - ky] * tb[w][2][jj][nz - kz];
+            }
         }
         acc[k] = sum;
       }
@@ -655,7 +667,7 @@ static int evaluate_pass(DevTree *t, const double *S, double *F, int potential, 
     TRY(fmm_reserve(t->Mf, nc * mstr));
     TRY(fmm_reserve(t->Lf, nc * lstr));
     TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
-    TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
+    TRY(fmm_reserve(t->sdip, t->so == 1 ? t->N : 1));
     TRY(fmm_stage_particles(t, S, st));
     TRY(run_pass<float>(t, ps, S, t->Mf.p, t->Lf.p, true, impl, mstr, lstr, dstr, st));
   } else {
@@ -702,7 +714,7 @@ static int near_start(DevTree *t, void *arg) {
     TRY(fmm_reserve(t->Mf, nc * mstr));
     TRY(fmm_reserve(t->Lf, nc * fmm_stride4((int)lsize)));
     TRY(fmm_reserve(t->phi4, t->N)); TRY(fmm_reserve(t->plo4, t->N));
-    TRY(fmm_reserve(t->sdip, t->so ? t->N : 1));
+    TRY(fmm_reserve(t->sdip, t->so == 1 ? t->N : 1));
     M = (T *)(void *)t->Mf.p;
   } else {
     TRY(fmm_reserve(t->M, nc * msize));
@@ -801,7 +813,7 @@ int fmm_tree_build_evaluate(DevTree *t, const double *pos, long N, long ncrit, i
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_s, cudaEventDisableTiming));
     FMM_CUDA_TRY(cudaEventCreateWithFlags(&t->ev_l, cudaEventDisableTiming));
   }
-  if (so < 0 || so > 1 || order < so + 1 || order > FMM_PMAX) return FMM_ERR_ARG;
+  if (so < 0 || so > 2 || order < so + 1 || order > FMM_PMAX) return FMM_ERR_ARG;
   const PlanSet *ps = fmm_get_plans(order, so);
   if (!ps) return FMM_ERR_CUDA;
   const bool mixed = precision != 0;
@@ -936,9 +948,13 @@ __global__ void __launch_bounds__(BH_THREADS) k_bh64(long N, int nsys, const lon
       for (int j = j0; j < j1; j++) {
         if (j == i) continue;
         const double dx = xi - px[j], dy = yi - py[j], dz = zi - pz[j];
+        const uint32_t oj = perm[j];
+        if (so == 2) {
+          quadrupole_p2p<double>(dx, dy, dz, S + 6 * (size_t)oj, phi, ex, ey, ez);
+          continue;
+        }
         const double r2 = dx * dx + dy * dy + dz * dz;
         const double rinv = 1.0 / sqrt(r2), r3 = rinv * rinv * rinv;
-        const uint32_t oj = perm[j];
         if (so == 0) {
           const double q = S[oj];
           phi += q * rinv;
@@ -1034,7 +1050,7 @@ void fmm_eval_times(DevTree *t) {
 #define DIR_BS 128
 __global__ void __launch_bounds__(DIR_BS) k_direct(const double *pos, const double *S, long N, const long *targets,
                                                    long nt, int so, int potential, int field, double *F) {
-  __shared__ double sx[DIR_BS], sy[DIR_BS], sz[DIR_BS], sq[DIR_BS][3];
+  __shared__ double sx[DIR_BS], sy[DIR_BS], sz[DIR_BS], sq[DIR_BS][6];
   long t = blockIdx.x * (long)DIR_BS + threadIdx.x;
   long i = t < nt ? (targets ? targets[t] : t) : -1;
   double xi = 0, yi = 0, zi = 0;
@@ -1046,7 +1062,8 @@ __global__ void __launch_bounds__(DIR_BS) k_direct(const double *pos, const doub
     if (j < N) {
       sx[threadIdx.x] = pos[3 * j]; sy[threadIdx.x] = pos[3 * j + 1]; sz[threadIdx.x] = pos[3 * j + 2];
       if (so == 0) sq[threadIdx.x][0] = S[j];
-      else { sq[threadIdx.x][0] = S[3 * j]; sq[threadIdx.x][1] = S[3 * j + 1]; sq[threadIdx.x][2] = S[3 * j + 2]; }
+      else if (so == 1) { sq[threadIdx.x][0] = S[3 * j]; sq[threadIdx.x][1] = S[3 * j + 1]; sq[threadIdx.x][2] = S[3 * j + 2]; }
+      else for (int k = 0; k < 6; k++) sq[threadIdx.x][k] = S[6 * j + k];
     }
     __syncthreads();
     int cnt = (int)min((long)DIR_BS, N - b);
@@ -1054,6 +1071,10 @@ __global__ void __launch_bounds__(DIR_BS) k_direct(const double *pos, const doub
     for (int jj = 0; jj < cnt; jj++) {
       if (b + jj == i) continue;
       double dx = xi - sx[jj], dy = yi - sy[jj], dz = zi - sz[jj];
+      if (so == 2) {
+        quadrupole_p2p<double>(dx, dy, dz, sq[jj], phi, ex, ey, ez);
+        continue;
+      }
       double R = sqrt(dx * dx + dy * dy + dz * dz);
       double rinv = 1.0 / R;
       double r3 = rinv * rinv * rinv;
@@ -1081,7 +1102,7 @@ __global__ void __launch_bounds__(DIR_BS) k_direct(const double *pos, const doub
 
 int fmm_direct(const double *pos, const double *S, long N, const long *targets, long ntargets, int so,
                int potential, int field, double *F, cudaStream_t st) {
-  if (!pos || !S || !F || N < 1 || (!potential && !field) || so < 0 || so > 1) return FMM_ERR_ARG;
+  if (!pos || !S || !F || N < 1 || (!potential && !field) || so < 0 || so > 2) return FMM_ERR_ARG;
   long nt = targets ? ntargets : N;
   if (nt < 1) return FMM_OK;
   fmm_note_launch(), k_direct<<<fmm_blocks(nt, DIR_BS), DIR_BS, 0, st>>>(pos, S, N, targets, nt, so, potential, field, F);

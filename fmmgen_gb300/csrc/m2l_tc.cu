@@ -517,7 +517,7 @@ struct TcPlan {
 };
 
 bool tc_plan(int p, int so, TcPlan &pl) {
-  if (p < 1 || p > 9 || so < 0 || so > 1 || p < so + 1) return false;
+  if (p < 1 || p > 9 || so < 0 || so > 2 || p < so + 1) return false;
   pl.p = p;
   pl.so = so;
   const int moff = fmm_nterms(so - 1);

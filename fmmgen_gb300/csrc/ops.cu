@@ -124,14 +124,17 @@ __global__ void k_op_l2p(int n, const double *d, const double *L, double *F, int
   }
 }
 
-// P2P (Coulomb form of example/operators.cpp:54-66; dipole field restated)
+// P2P (Coulomb form of example/operators.cpp:54-66; dipole and quadrupole
+// fields restated as the gradients of the generated potentials)
 __global__ void k_op_p2p(int n, const double *d, const double *S, double *F, int so, int potential, int field) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = d[3 * i], y = d[3 * i + 1], z = d[3 * i + 2];
   double R = sqrt(x * x + y * y + z * z);
-  double phi, ex, ey, ez;
-  if (so == 0) {
+  double phi = 0, ex = 0, ey = 0, ez = 0;
+  if (so == 2) {
+    quadrupole_p2p<double>(x, y, z, S + 6 * (size_t)i, phi, ex, ey, ez);
+  } else if (so == 0) {
     double q = S[i];
     double r3 = 1.0 / (R * R * R);
     phi = q / R;
@@ -189,7 +192,7 @@ __global__ void k_op_m2p(int n, const double *d, const double *M, double *F, int
 
 int fmm_op_batch(int op, int n, const double *d, const double *in, double *out, int order, int so, int potential,
                  int field, cudaStream_t st) {
-  if (n < 0 || so < 0 || so > 1 || !d || !in || !out) return FMM_ERR_ARG;
+  if (n < 0 || so < 0 || so > 2 || !d || !in || !out) return FMM_ERR_ARG;
   if (op != 5 && (order < 0 || order > FMM_PMAX || order < so)) return FMM_ERR_ARG;
   if ((op == 4 || op == 5 || op == 6) && !potential && !field) return FMM_ERR_ARG;
   if (n == 0) return FMM_OK;

@@ -12,7 +12,7 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p64(const int *leaf_cells,
                                                           const double *px, const double *py, const double *pz,
                                                           const uint32_t *perm, const double *S, int so,
                                                           double *Fnear) {
-  __shared__ double sx[P2P_WARPS][32], sy[P2P_WARPS][32], sz[P2P_WARPS][32], sq[P2P_WARPS][32][3];
+  __shared__ double sx[P2P_WARPS][32], sy[P2P_WARPS][32], sz[P2P_WARPS][32], sq[P2P_WARPS][32][6];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int leaf = blockIdx.x * P2P_WARPS + w;
   if (leaf >= nleaves) return;
@@ -35,7 +35,8 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p64(const int *leaf_cells,
           sx[w][lane] = px[j]; sy[w][lane] = py[j]; sz[w][lane] = pz[j];
           uint32_t o = perm[j];
           if (so == 0) sq[w][lane][0] = S[o];
-          else { sq[w][lane][0] = S[3 * (size_t)o]; sq[w][lane][1] = S[3 * (size_t)o + 1]; sq[w][lane][2] = S[3 * (size_t)o + 2]; }
+          else if (so == 1) { sq[w][lane][0] = S[3 * (size_t)o]; sq[w][lane][1] = S[3 * (size_t)o + 1]; sq[w][lane][2] = S[3 * (size_t)o + 2]; }
+          else for (int k = 0; k < 6; k++) sq[w][lane][k] = S[6 * (size_t)o + k];
         }
         __syncwarp();
         const int cnt = min(32, nb - sb);
@@ -43,6 +44,10 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p64(const int *leaf_cells,
           for (int jj = 0; jj < cnt; jj++) {
             if (b0 + sb + jj == i) continue;  // l2 != l1
             double dx = xi - sx[w][jj], dy = yi - sy[w][jj], dz = zi - sz[w][jj];
+            if (so == 2) {  // quadrupole sources
+              quadrupole_p2p<double>(dx, dy, dz, sq[w][jj], phi, ex, ey, ez);
+              continue;
+            }
             double r2 = dx * dx + dy * dy + dz * dz;
             double rinv = rsqrt(r2);
             double r3 = rinv * rinv * rinv;
@@ -300,7 +305,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_p2p32(const int *leaf_cells, int
 // ---------------------------------------------------------------------------
 int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st, bool narrow) {
   const int nl = t->nleaves, so = t->so;
-  if (mixed) {
+  if (mixed && so <= 1) {  // quadrupole sources take the FP64 kernel in every precision
     // narrow blocks (2 warps) when running beside the tensor-core M2L: they
     // fit in the registers its CTA leaves free
     const bool pot = t->pass_potential || so;
@@ -324,6 +329,7 @@ int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st, boo
 }
 
 int fmm_stage_particles(DevTree *t, const double *S, cudaStream_t st) {
+  if (t->so > 1) return FMM_OK;  // the FP64 P2P reads the sources directly
   fmm_note_launch(), k_stage_particles<<<t->nleaves, 128, 0, st>>>(
       t->leaf_cells.p, t->nleaves, t->pstart.p, t->pcount.p, t->csys.p, t->roots.p, t->px.p, t->py.p, t->pz.p,
       t->perm.p, S, t->so, t->phi4.p, t->plo4.p, t->sdip.p);

@@ -95,14 +95,14 @@ HostPlan plan_l2l(int p, int so) {
 }
 
 std::mutex g_mu;
-PlanSet *g_plans[16][FMM_PMAX + 1][2] = {};
+PlanSet *g_plans[16][FMM_PMAX + 1][3] = {};
 
 }  // namespace
 
 const PlanSet *fmm_get_plans(int order, int so) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return nullptr;
-  if (order < 0 || order > FMM_PMAX || so < 0 || so > 1) return nullptr;
+  if (order < 0 || order > FMM_PMAX || so < 0 || so > 2) return nullptr;
   std::lock_guard<std::mutex> lk(g_mu);
   if (g_plans[dev][order][so]) return g_plans[dev][order][so];
   HostPlan hp[3] = {plan_m2l(order, so), plan_m2m(order, so), plan_l2l(order, so)};

@@ -34,7 +34,7 @@ struct ShiftSet {
 };
 
 std::mutex g_mu;
-ShiftSet *g_sets[16][FMM_PMAX + 1][2] = {};
+ShiftSet *g_sets[16][FMM_PMAX + 1][3] = {};
 
 double mono(int kx, int ky, int kz, double vx, double vy, double vz) {
   double r = 1;
@@ -81,7 +81,7 @@ int upload(ShiftTab &t, const std::vector<int> &off, const std::vector<int> &in,
 
 const ShiftSet *get_shift(int p, int so) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16 || p < 0 || p > FMM_PMAX || so < 0 || so > 1)
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16 || p < 0 || p > FMM_PMAX || so < 0 || so > 2)
     return nullptr;
   std::lock_guard<std::mutex> lk(g_mu);
   if (g_sets[dev][p][so]) return g_sets[dev][p][so];

@@ -633,7 +633,7 @@ static int build_classes(DevTree *t, cudaStream_t st);
 int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order, double theta, int so,
                    cudaStream_t st, const long *sys_off, int nsys, bool defer_classes,
                    int (*after_cells)(DevTree *, void *), void *arg) {
-  if (N < 1 || N >= (1L << 31) - 1 || ncrit < 1 || order < so + 1 || order > FMM_PMAX || so < 0 || so > 1 ||
+  if (N < 1 || N >= (1L << 31) - 1 || ncrit < 1 || order < so + 1 || order > FMM_PMAX || so < 0 || so > 2 ||
       !(theta > 0) || !pos || nsys < 1 || (nsys > 1 && !sys_off))
     return FMM_ERR_ARG;
   if (sys_off) {

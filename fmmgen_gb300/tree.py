@@ -37,7 +37,8 @@ def _as_device(a, shape_tail):
 
 
 def sourcesize(source_order):
-    return 1 if source_order == 0 else 3
+    """Components of a source: 1 charge, 3 dipole, 6 quadrupole (xx xy xz yy yz zz)."""
+    return {0: 1, 1: 3, 2: 6}[source_order]
 
 
 def outputsize(potential=True, field=True):
@@ -48,8 +49,8 @@ class Tree:
     """Device octree + interaction lists for fixed particle positions."""
 
     def __init__(self, pos, S, ncrit, order, theta, source_order=0, stream=None, sys_off=None):
-        if source_order not in (0, 1):
-            raise ValueError("source_order must be 0 (charges) or 1 (dipoles)")
+        if source_order not in (0, 1, 2):
+            raise ValueError("source_order must be 0 (charges), 1 (dipoles) or 2 (quadrupoles)")
         # a forest of independent systems when sys_off (nsys + 1 particle offsets) is given
         self.sys_off = None if sys_off is None else np.ascontiguousarray(sys_off, dtype=np.int64)
         self.pos = _as_device(pos, (3,))

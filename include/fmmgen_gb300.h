@@ -12,7 +12,8 @@
  *      Tree::compute_field_fmm(F) / Tree::compute_field_exact(F).
  *
  * Layouts are fmmgen's: positions [N][3], sources [N][SOURCESIZE]
- * (SOURCESIZE = 1 for charges, 3 for dipoles), outputs [N][OUTPUTSIZE]
+ * (SOURCESIZE = 1 for charges, 3 for dipoles, 6 for quadrupoles: the degree-
+ * source_order multipole coefficients in fmmgen's order), outputs [N][OUTPUTSIZE]
  * (phi, Ex, Ey, Ez as selected by potential/field), multipole/local arrays in
  * the Nterms multi-index order of fmmgen/utils.py:65-118.  All arrays are
  * FP64.  Unless a function says "host", pointers are device pointers and work

@@ -51,7 +51,8 @@ def test_invalid_arguments_rejected_without_gpu(fg):
     from fmmgen_gb300 import _lib
 
     L = fg.lib()
-    assert L.fmmgen_configure(2, 1, 1, 8) == _lib.ERR_ARG
+    assert L.fmmgen_configure(3, 1, 1, 8) == _lib.ERR_ARG  # source orders 0, 1, 2
+    assert L.fmmgen_sourcesize(2) == 6 and L.fmmgen_msize(5, 2) == 56 - 4
     assert L.fmmgen_configure(0, 0, 0, 8) == _lib.ERR_ARG
     assert L.fmmgen_configure(0, 1, 1, 13) == _lib.ERR_ARG
     # order above the supported maximum is rejected before any device work
