@@ -41,6 +41,13 @@ _SIGS = {
     "fmmgen_gpu_L2P": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_gpu_P2P": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_gpu_M2P": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_P2M_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_M2M_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_M2L_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_L2L_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_L2P_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_P2P_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _vp]),
+    "fmmgen_gpu_M2P_f32": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     "fmmgen_configure": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "P2M": (None, [C.c_double, C.c_double, C.c_double, C.c_double, _dp, C.c_int]),
     "M2M": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
@@ -49,6 +56,13 @@ _SIGS = {
     "L2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "M2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "P2P": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp]),
+    "P2Mf": (None, [C.c_float, C.c_float, C.c_float, C.c_float, _dp, C.c_int]),
+    "M2Mf": (None, [C.c_float, C.c_float, C.c_float, _dp, _dp, C.c_int]),
+    "M2Lf": (None, [C.c_float, C.c_float, C.c_float, _dp, _dp, C.c_int]),
+    "L2Lf": (None, [C.c_float, C.c_float, C.c_float, _dp, _dp, C.c_int]),
+    "L2Pf": (None, [C.c_float, C.c_float, C.c_float, _dp, _dp, C.c_int]),
+    "M2Pf": (None, [C.c_float, C.c_float, C.c_float, _dp, _dp, C.c_int]),
+    "P2Pf": (None, [C.c_float, C.c_float, C.c_float, _dp, _dp]),
     "fmmgen_tree_build": (C.c_int, [_dp, C.c_long, C.c_long, C.c_int, C.c_double, C.c_int, _vp,
                                     C.POINTER(C.c_void_p)]),
     "fmmgen_forest_build": (C.c_int, [_dp, _lp, C.c_int, C.c_long, C.c_int, C.c_double, C.c_int, _vp,

@@ -18,6 +18,8 @@ struct fmmgen_tree {
 
 int fmm_op_batch(int op, int n, const double *d, const double *in, double *out, int order, int so, int potential,
                  int field, cudaStream_t st);
+int fmm_op_batch_f32(int op, int n, const float *d, const float *in, float *out, int order, int so, int potential,
+                     int field, cudaStream_t st);
 void fmm_eval_times(DevTree *t);
 
 namespace {
@@ -69,6 +71,11 @@ int fmmgen_outputsize(int potential, int field) { return (potential ? 1 : 0) + (
     g_err.clear();                                                                                  \
     return ret(fmm_op_batch(opid, n, d, in, out, order, so, pot, fld, S(st)));                     \
   } while (0)
+#define OPBF(opid, n, d, in, out, order, so, pot, fld, st)                                          \
+  do {                                                                                              \
+    g_err.clear();                                                                                  \
+    return ret(fmm_op_batch_f32(opid, n, d, in, out, order, so, pot, fld, S(st)));                 \
+  } while (0)
 
 int fmmgen_gpu_P2M(int n, const double *d, const double *q, double *M, int order, int so, void *st) {
   OPB(0, n, d, q, M, order, so, 1, 1, st);
@@ -94,6 +101,30 @@ int fmmgen_gpu_M2P(int n, const double *d, const double *M, double *F, int order
   OPB(6, n, d, M, F, order, so, potential, field, st);
 }
 
+int fmmgen_gpu_P2M_f32(int n, const float *d, const float *q, float *M, int order, int so, void *st) {
+  OPBF(0, n, d, q, M, order, so, 1, 1, st);
+}
+int fmmgen_gpu_M2M_f32(int n, const float *d, const float *M, float *Ms, int order, int so, void *st) {
+  OPBF(1, n, d, M, Ms, order, so, 1, 1, st);
+}
+int fmmgen_gpu_M2L_f32(int n, const float *d, const float *M, float *L, int order, int so, void *st) {
+  OPBF(2, n, d, M, L, order, so, 1, 1, st);
+}
+int fmmgen_gpu_L2L_f32(int n, const float *d, const float *L, float *Ls, int order, int so, void *st) {
+  OPBF(3, n, d, L, Ls, order, so, 1, 1, st);
+}
+int fmmgen_gpu_L2P_f32(int n, const float *d, const float *L, float *F, int order, int so, int potential, int field,
+                       void *st) {
+  OPBF(4, n, d, L, F, order, so, potential, field, st);
+}
+int fmmgen_gpu_P2P_f32(int n, const float *d, const float *Sv, float *F, int so, int potential, int field, void *st) {
+  OPBF(5, n, d, Sv, F, 0, so, potential, field, st);
+}
+int fmmgen_gpu_M2P_f32(int n, const float *d, const float *M, float *F, int order, int so, int potential, int field,
+                       void *st) {
+  OPBF(6, n, d, M, F, order, so, potential, field, st);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -113,19 +144,25 @@ struct ScalarCfg {
 };
 ScalarCfg g_cfg;
 
-// runs one operator on host arrays through the device path
-void scalar_op(int op, double x, double y, double z, const double *in, int insize, double *out, int outsize,
-               int order) {
+// runs one operator on host arrays through the device path (T = double, or
+// float for the precision="float" twins)
+template <typename T>
+void scalar_op(int op, T x, T y, T z, const T *in, int insize, T *out, int outsize, int order) {
   std::lock_guard<std::mutex> lk(g_cfg.mu);
   if (!g_cfg.st && cudaStreamCreateWithFlags(&g_cfg.st, cudaStreamNonBlocking) != cudaSuccess) return;
   if (!g_cfg.dbuf && cudaMalloc((void **)&g_cfg.dbuf, sizeof(double) * (4 + 2 * FMM_NTMAX)) != cudaSuccess) return;
-  double *d = g_cfg.dbuf, *din = d + 4, *dout = din + FMM_NTMAX;
-  double h[3] = {x, y, z};
+  T *d = (T *)g_cfg.dbuf, *din = d + 4, *dout = din + FMM_NTMAX;
+  T h[3] = {x, y, z};
   cudaMemcpyAsync(d, h, sizeof(h), cudaMemcpyHostToDevice, g_cfg.st);
-  cudaMemcpyAsync(din, in, sizeof(double) * insize, cudaMemcpyHostToDevice, g_cfg.st);
-  cudaMemcpyAsync(dout, out, sizeof(double) * outsize, cudaMemcpyHostToDevice, g_cfg.st);
-  if (fmm_op_batch(op, 1, d, din, dout, order, g_cfg.so, g_cfg.potential, g_cfg.field, g_cfg.st) != FMM_OK) return;
-  cudaMemcpyAsync(out, dout, sizeof(double) * outsize, cudaMemcpyDeviceToHost, g_cfg.st);
+  cudaMemcpyAsync(din, in, sizeof(T) * insize, cudaMemcpyHostToDevice, g_cfg.st);
+  cudaMemcpyAsync(dout, out, sizeof(T) * outsize, cudaMemcpyHostToDevice, g_cfg.st);
+  int rc;
+  if constexpr (sizeof(T) == 8)
+    rc = fmm_op_batch(op, 1, d, din, dout, order, g_cfg.so, g_cfg.potential, g_cfg.field, g_cfg.st);
+  else
+    rc = fmm_op_batch_f32(op, 1, d, din, dout, order, g_cfg.so, g_cfg.potential, g_cfg.field, g_cfg.st);
+  if (rc != FMM_OK) return;
+  cudaMemcpyAsync(out, dout, sizeof(T) * outsize, cudaMemcpyDeviceToHost, g_cfg.st);
   cudaStreamSynchronize(g_cfg.st);
 }
 bool order_ok(int order) {
@@ -143,34 +180,69 @@ int fmmgen_configure(int so, int potential, int field, int maxorder) {
 }
 void P2M(double x, double y, double z, double q, double *M, int order) {
   if (!order_ok(order)) return;
-  scalar_op(0, x, y, z, &q, 1, M, (int)fmmgen_msize(order, g_cfg.so), order);
+  scalar_op<double>(0, x, y, z, &q, 1, M, (int)fmmgen_msize(order, g_cfg.so), order);
 }
 void M2M(double x, double y, double z, double *M, double *Ms, int order) {
   if (!order_ok(order)) return;
   int ms = (int)fmmgen_msize(order, g_cfg.so);
-  scalar_op(1, x, y, z, M, ms, Ms, ms, order);
+  scalar_op<double>(1, x, y, z, M, ms, Ms, ms, order);
 }
 void M2L(double x, double y, double z, double *M, double *L, int order) {
   if (!order_ok(order)) return;
-  scalar_op(2, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), L, (int)fmmgen_lsize(order, g_cfg.so), order);
+  scalar_op<double>(2, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), L, (int)fmmgen_lsize(order, g_cfg.so), order);
 }
 void L2L(double x, double y, double z, double *L, double *Ls, int order) {
   if (!order_ok(order)) return;
   int ls = (int)fmmgen_lsize(order, g_cfg.so);
-  scalar_op(3, x, y, z, L, ls, Ls, ls, order);
+  scalar_op<double>(3, x, y, z, L, ls, Ls, ls, order);
 }
 void L2P(double x, double y, double z, double *L, double *F, int order) {
   if (!order_ok(order)) return;
-  scalar_op(4, x, y, z, L, (int)fmmgen_lsize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
+  scalar_op<double>(4, x, y, z, L, (int)fmmgen_lsize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
             order);
 }
 void M2P(double x, double y, double z, double *M, double *F, int order) {
   if (!order_ok(order)) return;
-  scalar_op(6, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
+  scalar_op<double>(6, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
             order);
 }
 void P2P(double x, double y, double z, double *Sv, double *F) {
-  scalar_op(5, x, y, z, Sv, fmmgen_sourcesize(g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field), 0);
+  scalar_op<double>(5, x, y, z, Sv, fmmgen_sourcesize(g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field), 0);
+}
+
+// precision="float" twins (fmmgen/writer.py:105, fmmgen/printers.py:301-303:
+// every double of the generated signatures becomes float)
+void P2Mf(float x, float y, float z, float q, float *M, int order) {
+  if (!order_ok(order)) return;
+  scalar_op<float>(0, x, y, z, &q, 1, M, (int)fmmgen_msize(order, g_cfg.so), order);
+}
+void M2Mf(float x, float y, float z, float *M, float *Ms, int order) {
+  if (!order_ok(order)) return;
+  int ms = (int)fmmgen_msize(order, g_cfg.so);
+  scalar_op<float>(1, x, y, z, M, ms, Ms, ms, order);
+}
+void M2Lf(float x, float y, float z, float *M, float *L, int order) {
+  if (!order_ok(order)) return;
+  scalar_op<float>(2, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), L, (int)fmmgen_lsize(order, g_cfg.so), order);
+}
+void L2Lf(float x, float y, float z, float *L, float *Ls, int order) {
+  if (!order_ok(order)) return;
+  int ls = (int)fmmgen_lsize(order, g_cfg.so);
+  scalar_op<float>(3, x, y, z, L, ls, Ls, ls, order);
+}
+void L2Pf(float x, float y, float z, float *L, float *F, int order) {
+  if (!order_ok(order)) return;
+  scalar_op<float>(4, x, y, z, L, (int)fmmgen_lsize(order, g_cfg.so), F,
+                   fmmgen_outputsize(g_cfg.potential, g_cfg.field), order);
+}
+void M2Pf(float x, float y, float z, float *M, float *F, int order) {
+  if (!order_ok(order)) return;
+  scalar_op<float>(6, x, y, z, M, (int)fmmgen_msize(order, g_cfg.so), F,
+                   fmmgen_outputsize(g_cfg.potential, g_cfg.field), order);
+}
+void P2Pf(float x, float y, float z, float *Sv, float *F) {
+  scalar_op<float>(5, x, y, z, Sv, fmmgen_sourcesize(g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
+                   0);
 }
 
 // ---------------------------------------------------------------------------

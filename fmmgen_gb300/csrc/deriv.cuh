@@ -59,27 +59,28 @@ __device__ void warp_derivs(T x, T y, T z, int p, T *D, T *tmp, T *sbase) {
 
 // D[idx(n)] = d^n (1/|y|) at y, |n| <= q, in one thread, degree by degree:
 //   |n| |y|^2 D_n = -(2|n| - 1) sum_a n_a y_a D_(n - e_a) - (|n| - 1) sum_a n_a (n_a - 1) D_(n - 2 e_a)
-__device__ __forceinline__ void thread_derivs(double yx, double yy, double yz, int q, double *D) {
-  const double ir2 = 1.0 / (yx * yx + yy * yy + yz * yz);
+template <typename T>
+__device__ __forceinline__ void thread_derivs(T yx, T yy, T yz, int q, T *D) {
+  const T ir2 = T(1) / (yx * yx + yy * yy + yz * yz);
   D[0] = sqrt(ir2);
   int i = 1;
   for (int d = 1; d <= q; d++) {
-    const double rd = 1.0 / d, a1 = -(2 * d - 1) * ir2 * rd, a2 = -(d - 1) * ir2 * rd;
+    const T rd = T(1) / T(d), a1 = -T(2 * d - 1) * ir2 * rd, a2 = -T(d - 1) * ir2 * rd;
     for (int nx = d; nx >= 0; nx--)
       for (int ny = d - nx; ny >= 0; ny--, i++) {
         const int nz = d - nx - ny;
-        double s1 = 0, s2 = 0;
+        T s1 = 0, s2 = 0;
         if (nx) {
-          s1 += nx * yx * D[fmm_idx3(nx - 1, ny, nz)];
-          if (nx > 1) s2 += nx * (nx - 1) * D[fmm_idx3(nx - 2, ny, nz)];
+          s1 += T(nx) * yx * D[fmm_idx3(nx - 1, ny, nz)];
+          if (nx > 1) s2 += T(nx * (nx - 1)) * D[fmm_idx3(nx - 2, ny, nz)];
         }
         if (ny) {
-          s1 += ny * yy * D[fmm_idx3(nx, ny - 1, nz)];
-          if (ny > 1) s2 += ny * (ny - 1) * D[fmm_idx3(nx, ny - 2, nz)];
+          s1 += T(ny) * yy * D[fmm_idx3(nx, ny - 1, nz)];
+          if (ny > 1) s2 += T(ny * (ny - 1)) * D[fmm_idx3(nx, ny - 2, nz)];
         }
         if (nz) {
-          s1 += nz * yz * D[fmm_idx3(nx, ny, nz - 1)];
-          if (nz > 1) s2 += nz * (nz - 1) * D[fmm_idx3(nx, ny, nz - 2)];
+          s1 += T(nz) * yz * D[fmm_idx3(nx, ny, nz - 1)];
+          if (nz > 1) s2 += T(nz * (nz - 1)) * D[fmm_idx3(nx, ny, nz - 2)];
         }
         D[i] = a1 * s1 + a2 * s2;
       }

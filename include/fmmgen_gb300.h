@@ -81,6 +81,20 @@ int fmmgen_gpu_P2P(int n, const double *d, const double *S, double *F, int sourc
 int fmmgen_gpu_M2P(int n, const double *d, const double *M, double *F, int order, int source_order, int potential,
                    int field, void *stream);
 
+/* The same seven operators in FP32: the generator's precision="float" variant
+ * (fmmgen/writer.py:105, fmmgen/printers.py:237-303 -- every double of the
+ * generated code becomes float).  float buffers, float arithmetic throughout. */
+int fmmgen_gpu_P2M_f32(int n, const float *d, const float *q, float *M, int order, int source_order, void *stream);
+int fmmgen_gpu_M2M_f32(int n, const float *d, const float *M, float *Ms, int order, int source_order, void *stream);
+int fmmgen_gpu_M2L_f32(int n, const float *d, const float *M, float *L, int order, int source_order, void *stream);
+int fmmgen_gpu_L2L_f32(int n, const float *d, const float *L, float *Ls, int order, int source_order, void *stream);
+int fmmgen_gpu_L2P_f32(int n, const float *d, const float *L, float *F, int order, int source_order, int potential,
+                       int field, void *stream);
+int fmmgen_gpu_P2P_f32(int n, const float *d, const float *S, float *F, int source_order, int potential, int field,
+                       void *stream);
+int fmmgen_gpu_M2P_f32(int n, const float *d, const float *M, float *F, int order, int source_order, int potential,
+                       int field, void *stream);
+
 /* ---- scalar twins of the generated dispatchers (host pointers, run on the
  *      GPU synchronously).  Signatures of example/operators.cpp:1376-1489;
  *      source_order / potential / field are those set by fmmgen_configure
@@ -95,6 +109,16 @@ void L2L(double x, double y, double z, double *L, double *Ls, int order);
 void L2P(double x, double y, double z, double *L, double *F, int order);
 void M2P(double x, double y, double z, double *M, double *F, int order);
 void P2P(double x, double y, double z, double *S, double *F);
+/* precision="float" scalar twins: the generated float signatures
+ * (fmmgen/printers.py:301-303), with an f suffix so that both live in one
+ * library; same configuration and order rules as the double twins. */
+void P2Mf(float x, float y, float z, float q, float *M, int order);
+void M2Mf(float x, float y, float z, float *M, float *Ms, int order);
+void M2Lf(float x, float y, float z, float *M, float *L, int order);
+void L2Lf(float x, float y, float z, float *L, float *Ls, int order);
+void L2Pf(float x, float y, float z, float *L, float *F, int order);
+void M2Pf(float x, float y, float z, float *M, float *F, int order);
+void P2Pf(float x, float y, float z, float *S, float *F);
 
 /* ---- tree-level API (example/tree.hpp:78-103) ---- */
 typedef struct fmmgen_tree fmmgen_tree;

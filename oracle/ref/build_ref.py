@@ -13,10 +13,15 @@ Recipe, run in the development container where the reference checkout exists:
      -ffp-contract=off keeps every FP64 expression as written (no FMA
      contraction), which the bit-exact tree/list comparisons rely on.
 
+  3. (--float) fmmgen.generate_code with precision="float" and language="c"
+     emits the FP32 operators (the same settings otherwise); gcc compiles
+     them alone into oracle/_ref/libref_f32_so{0,1,2}.so, whose plain C
+     symbols (P2M, M2M, ... with float arguments) ctypes calls directly.
+
 Outputs are cached: a step is skipped when its output is newer than its inputs.
 Nothing here is shipped; the GPU machine never runs it.
 
-Usage: python oracle/ref/build_ref.py [--reference DIR] [--pmax0 8] [--pmax1 6] [--pmax2 5]
+Usage: python oracle/ref/build_ref.py [--reference DIR] [--pmax0 8] [--pmax1 6] [--pmax2 5] [--float]
 """
 import argparse
 import contextlib
@@ -32,7 +37,8 @@ DEFAULT_REF = "/root/reference"
 
 
 def _generate(args):
-    ref, so, pmax, outdir = args
+    ref, so, pmax, outdir = args[:4]
+    precision, language = args[4:] if len(args) > 4 else ("double", "c++")
     sys.path.insert(0, ref)
     import fmmgen  # the reference generator
 
@@ -44,7 +50,7 @@ def _generate(args):
             fmmgen.generate_code(
                 pmax + 1,  # the generator's upper order bound is exclusive
                 "operators",
-                precision="double",
+                precision=precision,
                 CSE=True,
                 cython=False,
                 potential=True,
@@ -53,7 +59,7 @@ def _generate(args):
                 atomic=True,
                 minpow=11,
                 harmonic_derivs=True,
-                language="c++",
+                language=language,
                 include_dir=outdir,
                 src_dir=outdir,
             )
@@ -122,14 +128,49 @@ def build(ref=DEFAULT_REF, pmax0=8, pmax1=6, pmax2=5, jobs=4, verbose=True):
     return libs
 
 
+def build_float(ref=DEFAULT_REF, pmax0=8, pmax1=6, pmax2=5, verbose=True):
+    """The precision="float" operators alone; returns {source_order: path to .so}."""
+    if not os.path.isdir(os.path.join(ref, "fmmgen")):
+        raise FileNotFoundError(f"reference checkout not found at {ref}")
+    specs = [(0, pmax0), (1, pmax1), (2, pmax2)]
+    gen = [os.path.join(ref, "fmmgen", f) for f in ("generator.py", "printers.py", "writer.py")]
+    jobs = []
+    for so, pmax in specs:
+        outdir = os.path.join(OUT, f"f32_so{so}_p{pmax}")
+        if _stale(os.path.join(outdir, "operators.c"), gen):
+            jobs.append((ref, so, pmax, outdir, "float", "c"))
+    if jobs:
+        if verbose:
+            print(f"[build_ref] generating float operators: {[(j[1], j[2]) for j in jobs]}", flush=True)
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            pool.map(_generate, jobs)
+    libs, procs = {}, []
+    for so, pmax in specs:
+        gdir = os.path.join(OUT, f"f32_so{so}_p{pmax}")
+        lib = os.path.join(OUT, f"libref_f32_so{so}.so")
+        libs[so] = lib
+        src = os.path.join(gdir, "operators.c")
+        if _stale(lib, [src, __file__]):
+            cmd = ["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I", gdir, src, "-o", lib, "-lm"]
+            if verbose:
+                print(f"[build_ref] compiling {lib}", flush=True)
+            procs.append(subprocess.Popen(cmd))
+    if any(p.wait() for p in procs):
+        raise RuntimeError("float operator compile failed")
+    return libs
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=DEFAULT_REF)
     ap.add_argument("--pmax0", type=int, default=8)
     ap.add_argument("--pmax1", type=int, default=6)
     ap.add_argument("--pmax2", type=int, default=5)
+    ap.add_argument("--float", action="store_true", help="also build the precision=\"float\" operators")
     a = ap.parse_args()
     print(build(a.reference, a.pmax0, a.pmax1, a.pmax2))
+    if a.float:
+        print(build_float(a.reference, a.pmax0, a.pmax1, a.pmax2))
 
 
 if __name__ == "__main__":

@@ -11,6 +11,9 @@ Barnes-Hut fixtures (compute_field_bh, M2P) keep potentials only: the
 generated M2P's field is not the gradient of its potential.
 `--bh` writes only the Barnes-Hut fixtures; `--so2` only the quadrupole-source
 fixtures (ops_so2.npz, tree_quadrupole_plummer.npz, m2p_potential_so2.npz).
+`--f32` (after `build_ref.py --float`) writes ops_f32_so{0,1,2}.npz: the outputs
+of the reference's precision="float" operators on the inputs of ops_so*.npz
+rounded to float32 -- the accuracy the FP32 variant is held to.
 """
 import hashlib
 import os
@@ -70,6 +73,51 @@ def make_ops(specs=((0, (1, 8)), (1, (2, 6))), seed=2024):
         out["pmin"], out["pmax"] = np.int64(pmin), np.int64(pmax)
         np.savez_compressed(os.path.join(HERE, f"ops_so{so}.npz"), **out)
         print(f"ops_so{so}.npz: orders {pmin}..{pmax}")
+
+
+def make_ops_f32():
+    import ctypes as C
+
+    fp = C.POINTER(C.c_float)
+    for so in (0, 1, 2):
+        lib = C.CDLL(os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_ref", f"libref_f32_so{so}.so"))
+        for nm in ("M2M", "M2L", "L2L", "L2P"):
+            getattr(lib, nm).argtypes = [C.c_float] * 3 + [fp, fp, C.c_int]
+        lib.P2M.argtypes = [C.c_float] * 4 + [fp, C.c_int]
+        lib.P2P.argtypes = [C.c_float] * 3 + [fp, fp]
+
+        def ptr(a):
+            return a.ctypes.data_as(fp)
+
+        g = np.load(os.path.join(HERE, f"ops_so{so}.npz"))
+        pmin, pmax = int(g["pmin"]), int(g["pmax"])
+        out = {"pmin": g["pmin"], "pmax": g["pmax"]}
+        for p in range(pmin, pmax + 1):
+            d = g[f"p{p}_d"].astype(np.float32)
+            q = g[f"p{p}_q"].astype(np.float32)
+            Min = g[f"p{p}_M"].astype(np.float32)
+            Lin = g[f"p{p}_L"].astype(np.float32)
+            K = len(d)
+            ms, ls = Min.shape[1], Lin.shape[1]
+            res = {k: np.zeros((K, w), np.float32) for k, w in (("P2M", ms), ("M2M", ms), ("M2L", ls), ("L2L", ls),
+                                                                 ("L2P", 4))}
+            for i in range(K):
+                x, y, z = (float(v) for v in d[i])
+                lib.P2M(x, y, z, float(q[i]), ptr(res["P2M"][i]), p)
+                lib.M2M(x, y, z, ptr(Min[i].copy()), ptr(res["M2M"][i]), p)
+                lib.M2L(x, y, z, ptr(Min[i].copy()), ptr(res["M2L"][i]), p)
+                lib.L2L(x, y, z, ptr(Lin[i].copy()), ptr(res["L2L"][i]), p)
+                lib.L2P(x, y, z, ptr(Lin[i].copy()), ptr(res["L2P"][i]), p)
+            for k, v in res.items():
+                out[f"p{p}_{k}"] = v
+        d = g["p2p_d"].astype(np.float32)
+        S = g["p2p_S"].astype(np.float32)
+        F = np.zeros((len(d), 4), np.float32)
+        for i in range(len(d)):
+            lib.P2P(*(float(v) for v in d[i]), ptr(S[i].copy()), ptr(F[i]))
+        out["p2p_phi"] = F[:, 0].copy()  # the generated P2P's field is zero; its potential is kept
+        np.savez_compressed(os.path.join(HERE, f"ops_f32_so{so}.npz"), **out)
+        print(f"ops_f32_so{so}.npz: orders {pmin}..{pmax}")
 
 
 def plummer(rng, n, a=0.1, rmax=1.0):
@@ -201,7 +249,9 @@ def make_m2p(specs, name, seed):
 
 
 if __name__ == "__main__":
-    if "--so2" in sys.argv:
+    if "--f32" in sys.argv:
+        make_ops_f32()
+    elif "--so2" in sys.argv:
         make_ops(specs=((2, (3, 5)),), seed=2025)
         make_trees(only={"quadrupole_plummer"})
         make_m2p(((2, (3, 5)),), "m2p_potential_so2.npz", 78)

@@ -59,6 +59,21 @@ def test_p2p_restated(oracle_lib, so):
         assert np.all(g["p2p_F_generated"][:, 1:] == 0)
 
 
+@pytest.mark.parametrize("so", [0, 1, 2])
+def test_float_fixtures_are_float_rounding(so):
+    """ops_f32_so*.npz (the reference's precision="float" operators) sit within
+    float rounding of the FP64 generated operators on the same inputs, so they
+    measure the FP32 variant's accuracy and nothing else."""
+    g = np.load(os.path.join(GOLDEN, f"ops_so{so}.npz"))
+    f = np.load(os.path.join(GOLDEN, f"ops_f32_so{so}.npz"))
+    for p in range(int(g["pmin"]), int(g["pmax"]) + 1):
+        for k in ("P2M", "M2M", "M2L", "L2L", "L2P"):
+            a, b = f[f"p{p}_{k}"], g[f"p{p}_{k}"]
+            assert a.dtype == np.float32 and a.shape == b.shape
+            assert np.all(np.max(np.abs(a - b), axis=1) <= 2e-5 * np.max(np.abs(b), axis=1)), (p, k)
+    assert relerr(f["p2p_phi"], g["p2p_F"][:, 0]) < 1e-6
+
+
 def test_reference_known_answers(oracle_lib):
     """The numeric assertions of the reference's tests/test_multipoles.py."""
     O = oracle_lib
