@@ -7,5 +7,6 @@ the host-side binding.
 from ._lib import FMMError, lib  # noqa: F401
 from .tree import Tree, build_forest, build_tree, direct  # noqa: F401
 from . import operators  # noqa: F401
+from .demag import DemagFMM  # noqa: F401
 
-__all__ = ["Tree", "build_forest", "build_tree", "direct", "operators", "FMMError", "lib"]
+__all__ = ["Tree", "build_forest", "build_tree", "direct", "operators", "DemagFMM", "FMMError", "lib"]
