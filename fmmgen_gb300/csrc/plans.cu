@@ -9,6 +9,7 @@
 // one running sum per (lane, output) segment and writes it to a private slot,
 // and the outputs are then summed from their consecutive slots in a fixed
 // order (deterministic, no atomics).
+#include <algorithm>
 #include <array>
 #include <cstring>
 #include <mutex>
@@ -24,6 +25,15 @@ struct HostPlan {
 };
 
 // tasks: (out, a, b), sorted by out.
+//
+// Within a (lane, output) segment the order of the terms is free, so each
+// round's terms are chosen to spread the 32 lanes' shared-memory reads of A and
+// of B over distinct banks (4-byte banks; lanes that read the same word share
+// it): lanes are filled in turn, those with the fewest terms left first, each
+// taking the remaining term of its current segment that collides with the
+// fewest reads already placed in the round.
+// Shared-memory bank conflicts otherwise multiply the engine's load wavefronts
+// several times over.
 HostPlan make_plan(const std::vector<std::array<int, 3>> &tasks, int nout) {
   HostPlan P;
   int T = (int)tasks.size();
@@ -31,24 +41,60 @@ HostPlan make_plan(const std::vector<std::array<int, 3>> &tasks, int nout) {
   P.iters = (T + 31) / 32;
   P.task.assign((size_t)P.iters * 32, 0xffffffffu);
   P.out_seg.assign(nout + 1, -1);
+  struct Seg {
+    int id, t0, t1;  // tasks[t0, t1) of one output
+  };
+  std::vector<std::vector<Seg>> segs(32);
   int seg = 0;
   for (int l = 0; l < 32; l++) {
     int t0 = (int)((long)l * T / 32), t1 = (int)((long)(l + 1) * T / 32);
-    for (int t = t0; t < t1; t++) {
-      int out = tasks[t][0];
-      bool start = (t == t0) || tasks[t - 1][0] != out;
-      if (start && t != t0) seg++;
-      if (start && P.out_seg[out] < 0) P.out_seg[out] = seg;
-      bool end = (t == t1 - 1) || tasks[t + 1][0] != out;
-      uint32_t w = (uint32_t)tasks[t][1] | ((uint32_t)tasks[t][2] << 10) | ((uint32_t)seg << 20) |
-                   ((end ? 1u : 0u) << 31);
-      P.task[(size_t)(t - t0) * 32 + l] = w;
+    for (int t = t0; t < t1;) {
+      int out = tasks[t][0], e = t;
+      while (e < t1 && tasks[e][0] == out) e++;
+      if (P.out_seg[out] < 0) P.out_seg[out] = seg;
+      segs[l].push_back({seg++, t, e});
+      t = e;
     }
-    if (t1 > t0) seg++;
   }
   P.nseg = seg;
   P.out_seg[nout] = seg;
   // every output owns at least one task, so out_seg is fully set
+  std::vector<std::vector<char>> used(32);
+  std::vector<size_t> cur(32, 0);  // current segment per lane
+  std::vector<int> left(32, 0);    // terms of it not yet placed
+  for (int l = 0; l < 32; l++) {
+    used[l].assign((size_t)((long)(l + 1) * T / 32 - (long)l * T / 32), 0);
+    if (!segs[l].empty()) left[l] = segs[l][0].t1 - segs[l][0].t0;
+  }
+  for (int it = 0; it < P.iters; it++) {
+    int bankA[32], bankB[32];
+    for (int k = 0; k < 32; k++) bankA[k] = bankB[k] = -1;
+    // lanes with the fewest terms left to choose from go first
+    int ord[32];
+    for (int k = 0; k < 32; k++) ord[k] = k;
+    std::stable_sort(ord, ord + 32, [&](int x, int y) { return left[x] < left[y]; });
+    for (int li = 0; li < 32; li++) {
+      const int l = ord[li];
+      if (cur[l] >= segs[l].size()) continue;
+      const Seg &S = segs[l][cur[l]];
+      const int base = (int)((long)l * T / 32);
+      int best = -1, bcost = 3;
+      for (int t = S.t0; t < S.t1 && bcost > 0; t++) {
+        if (used[l][t - base]) continue;
+        const int a = tasks[t][1], b = tasks[t][2];
+        const int cost = (bankA[a & 31] >= 0 && bankA[a & 31] != a) + (bankB[b & 31] >= 0 && bankB[b & 31] != b);
+        if (cost < bcost) { bcost = cost; best = t; }
+      }
+      used[l][best - base] = 1;
+      const int a = tasks[best][1], b = tasks[best][2];
+      if (bankA[a & 31] < 0) bankA[a & 31] = a;
+      if (bankB[b & 31] < 0) bankB[b & 31] = b;
+      const bool end = --left[l] == 0;
+      P.task[(size_t)it * 32 + l] =
+          (uint32_t)a | ((uint32_t)b << 10) | ((uint32_t)S.id << 20) | ((end ? 1u : 0u) << 31);
+      if (end && ++cur[l] < segs[l].size()) left[l] = segs[l][cur[l]].t1 - segs[l][cur[l]].t0;
+    }
+  }
   return P;
 }
 
