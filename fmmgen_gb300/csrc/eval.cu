@@ -251,14 +251,14 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l(Plan P, int ncells, int 
 // target A is applied at order q_k <= order, i.e. only the terms with
 // |n| + |m| <= q_k of the order-`order` contraction -- the leading blocks of D,
 // M and L in the degree-major layout, so the order-q_k plan runs on the same
-// rows.  One warp per target; lane l keeps outputs l, l + 32, ... in registers.
+// rows.  One launch per order q: every warp of it runs the one order-q plan
+// (whose task words then stay in L1), takes its target's pairs of order q and
+// accumulates them in its slots, and adds the sums to L once; L is zeroed
+// before the first launch.  One warp per target.
 // ---------------------------------------------------------------------------
 #define M2LV_R ((FMM_NTMAX + 31) / 32)
-struct PlanVar {
-  Plan p[FMM_PMAX + 1];
-};
 template <typename T>
-__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(PlanVar PV, int ncells, int so, int order,
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(Plan P, int q, int ncells, int so, int order,
                                                             const int *off_, const int *src, const int *cls,
                                                             const unsigned char *ord, const T *clsD,
                                                             const unsigned char *clevel, const T *M, T *L, int mstr,
@@ -267,19 +267,31 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(PlanVar PV, int ncel
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int A = blockIdx.x * FMM_WARPS + w;
   if (A >= ncells) return;
-  const int moff = fmm_nterms(so - 1), lsize = fmm_nterms(order - so);
-  T acc[M2LV_R];
-#pragma unroll
-  for (int r = 0; r < M2LV_R; r++) acc[r] = T(0);
+  const int moff = fmm_nterms(so - 1), nt = fmm_nterms(q), ms = nt - moff, ls = fmm_nterms(q - so);
   const int la = clevel[A];
   const int k0 = off_[A], k1 = off_[A + 1];
+  // the next pair of order q: 32 orders at a time, one ballot each (warp-uniform)
+  int cbase = k0 - 32;
+  unsigned hits = 0;
+  auto next = [&]() -> int {
+    while (!hits) {
+      cbase += 32;
+      if (cbase >= k1) return -1;
+      const int kk = cbase + lane;
+      hits = __ballot_sync(0xffffffffu, kk < k1 && min(max((int)ord[kk], so + 1), order) == q);
+    }
+    const int b = __ffs(hits) - 1;
+    hits &= hits - 1;
+    return cbase + b;
+  };
+  int kn = next();
+  if (kn < 0) return;
   // the operands of the next pair are loaded into registers while the engine
   // runs on the current one
   T dr[M2LV_R], mr[M2LV_R];
-  int qn = 0, dln = 0;
+  int dln = 0;
   auto fetch = [&](int k) {
-    qn = min(max((int)ord[k], so + 1), order);
-    const int B = src[k], nt = fmm_nterms(qn), ms = nt - moff;
+    const int B = src[k];
     const T *D = clsD + (size_t)cls[k] * dstr;
     dln = la - (int)clevel[B];
 #pragma unroll
@@ -289,11 +301,10 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(PlanVar PV, int ncel
       mr[r] = i < ms ? M[(size_t)B * mstr + i] : T(0);
     }
   };
-  if (k0 < k1) fetch(k0);
-  for (int k = k0; k < k1; k++) {
-    const int q = qn, dl = dln;
-    const Plan &P = PV.p[q];
-    const int nt = fmm_nterms(q), ms = nt - moff, ls = fmm_nterms(q - so);
+  fetch(kn);
+  for (int s = lane; s < P.nseg; s += 32) sS[w][s] = T(0);
+  while (kn >= 0) {
+    const int dl = dln;
     __syncwarp();
 #pragma unroll
     for (int r = 0; r < M2LV_R; r++) {
@@ -301,18 +312,13 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(PlanVar PV, int ncel
       if (i < nt) sA[w][i] = dr[r];
       if (i < ms) sB[w][i] = mr[r] * exp2i<T>(dl * (int)c_mi[i + moff][3]);
     }
-    for (int s = lane; s < P.nseg; s += 32) sS[w][s] = T(0);
     __syncwarp();
-    if (k + 1 < k1) fetch(k + 1);
+    kn = next();
+    if (kn >= 0) fetch(kn);
     engine_run<T>(P, sA[w], sB[w], sS[w], lane);
-    __syncwarp();
-#pragma unroll
-    for (int r = 0; r < M2LV_R; r++)
-      if (lane + 32 * r < ls) acc[r] += engine_out<T>(P, sS[w], lane + 32 * r);
   }
-#pragma unroll
-  for (int r = 0; r < M2LV_R; r++)
-    if (lane + 32 * r < lsize) L[(size_t)A * lstr + lane + 32 * r] = acc[r];
+  __syncwarp();
+  for (int n = lane; n < ls; n += 32) L[(size_t)A * lstr + n] += engine_out<T>(P, sS[w], n);
 }
 
 // ---------------------------------------------------------------------------
@@ -564,15 +570,15 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
       fmm_set_error_text("per-pair M2L orders were set for an earlier build");
       return FMM_ERR_STATE;
     }
-    PlanVar PV;
-    for (int q = 0; q <= FMM_PMAX; q++) {
-      const PlanSet *pq = q >= so + 1 && q <= p ? fmm_get_plans(q, so) : nullptr;
-      PV.p[q] = pq ? pq->m2l : Plan();
+    FMM_CUDA_TRY(cudaMemsetAsync(L, 0, sizeof(T) * (size_t)nc * lstr, st));
+    for (int q = so + 1; q <= p; q++) {
+      const PlanSet *pq = fmm_get_plans(q, so);
+      if (!pq) return FMM_ERR_CUDA;
+      fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+          pq->m2l, q, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
+          mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L,
+          mstr, lstr, dstr);
     }
-    fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-        PV, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
-        mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
-        lstr, dstr);
   } else if (mixed && impl == M2L_TC) {
     TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
   } else if (mixed && impl == M2L_GEN) {
