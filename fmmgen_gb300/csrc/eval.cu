@@ -14,6 +14,7 @@
 // displacement conventions are those of example/calculate.cpp:149-151, 182-184,
 // 201-203, 227-229, 243-245.
 #include <algorithm>
+#include <type_traits>
 #include "internal.h"
 #include "mi_table.cuh"
 #include "m2l_gen.cuh"
@@ -322,6 +323,108 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(Plan P, int q, int n
 }
 
 // ---------------------------------------------------------------------------
+// FP32 M2L with two source cells per engine pass.  A and B hold the two
+// pairs' operands side by side (float2), so one task word drives one packed
+// FMA (fma.rn.f32x2) over both: the task-word load and index decoding, which
+// bound the engine's issue rate, are shared by two multiply-adds.  Both halves
+// of the accumulator go to the same output slot.  With `ord` set only the
+// pairs of order q are taken and the sums are added to L (the per-order
+// launches above); with `ord` null every pair is taken at order q and L is
+// written.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ void engine_run2(const Plan &P, const float2 *A, const float2 *B, float *slots,
+                                            int lane) {
+  constexpr uint32_t PAD = 0xffffffffu;
+  const unsigned long long *A2 = reinterpret_cast<const unsigned long long *>(A);
+  const unsigned long long *B2 = reinterpret_cast<const unsigned long long *>(B);
+  unsigned long long acc = 0ull;
+  for (int it = 0; it < P.iters; it += 4) {
+    uint32_t w[4];
+    unsigned long long a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) w[u] = it + u < P.iters ? __ldg(&P.task[(it + u) * 32 + lane]) : PAD;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t x = w[u] == PAD ? 0u : w[u];
+      a[u] = A2[x & 1023u];
+      b[u] = B2[(x >> 10) & 1023u];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (w[u] == PAD) return;
+      acc = ffma2(a[u], b[u], acc);
+      if (w[u] >> 31) {
+        slots[(w[u] >> 20) & 2047u] += __uint_as_float((unsigned)acc) + __uint_as_float((unsigned)(acc >> 32));
+        acc = 0ull;
+      }
+    }
+  }
+}
+__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_f2(Plan P, int q, int ncells, int so, int order,
+                                                           const int *off_, const int *src, const int *cls,
+                                                           const unsigned char *ord, const float *clsD,
+                                                           const unsigned char *clevel, const float *M, float *L,
+                                                           int mstr, int lstr, int dstr) {
+  __shared__ float2 sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX];
+  __shared__ float sS[FMM_WARPS][FMM_NTMAX + 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int A = blockIdx.x * FMM_WARPS + w;
+  if (A >= ncells) return;
+  const int moff = fmm_nterms(so - 1), nt = fmm_nterms(q), ms = nt - moff, ls = fmm_nterms(q - so);
+  const int la = clevel[A];
+  const int k0 = off_[A], k1 = off_[A + 1];
+  int cbase = k0 - 32;
+  unsigned hits = 0;
+  auto next = [&]() -> int {
+    while (!hits) {
+      cbase += 32;
+      if (cbase >= k1) return -1;
+      const int kk = cbase + lane;
+      hits = __ballot_sync(0xffffffffu, kk < k1 && (!ord || min(max((int)ord[kk], so + 1), order) == q));
+    }
+    const int b = __ffs(hits) - 1;
+    hits &= hits - 1;
+    return cbase + b;
+  };
+  int ka = next();
+  if (ka < 0) {
+    if (!ord)
+      for (int n = lane; n < ls; n += 32) L[(size_t)A * lstr + n] = 0.f;
+    return;
+  }
+  for (int s = lane; s < P.nseg; s += 32) sS[w][s] = 0.f;
+  while (ka >= 0) {
+    const int kb = next();
+    const int Ba = src[ka], Bb = kb >= 0 ? src[kb] : Ba;
+    const float *Da = clsD + (size_t)cls[ka] * dstr, *Db = kb >= 0 ? clsD + (size_t)cls[kb] * dstr : Da;
+    const int dla = la - (int)clevel[Ba], dlb = la - (int)clevel[Bb];
+    const float zb = kb >= 0 ? 1.f : 0.f;  // an odd last pair runs beside zeros
+    __syncwarp();
+    for (int i = lane; i < nt; i += 32) sA[w][i] = make_float2(Da[i], Db[i]);
+    for (int j = lane; j < ms; j += 32) {
+      const int dg = (int)c_mi[j + moff][3];
+      sB[w][j] = make_float2(M[(size_t)Ba * mstr + j] * exp2i<float>(dla * dg),
+                             zb * M[(size_t)Bb * mstr + j] * exp2i<float>(dlb * dg));
+    }
+    __syncwarp();
+    engine_run2(P, sA[w], sB[w], sS[w], lane);
+    ka = kb >= 0 ? next() : -1;
+  }
+  __syncwarp();
+  for (int n = lane; n < ls; n += 32) {
+    const float v = engine_out<float>(P, sS[w], n);
+    if (ord) L[(size_t)A * lstr + n] += v;
+    else L[(size_t)A * lstr + n] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // L2L for all cells of one level (example/calculate.cpp:219-234)
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -574,10 +677,15 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
     for (int q = so + 1; q <= p; q++) {
       const PlanSet *pq = fmm_get_plans(q, so);
       if (!pq) return FMM_ERR_CUDA;
-      fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
-          pq->m2l, q, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
-          mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L,
-          mstr, lstr, dstr);
+      if constexpr (std::is_same<T, float>::value)
+        fmm_note_launch(), k_m2l_f2<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+            pq->m2l, q, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p, (const float *)t->cls_Df.p,
+            t->clevel.p, M, L, mstr, lstr, dstr);
+      else
+        fmm_note_launch(), k_m2l_var<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+            pq->m2l, q, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p,
+            mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L,
+            mstr, lstr, dstr);
     }
   } else if (mixed && impl == M2L_TC) {
     TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
@@ -590,6 +698,10 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
           t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
           (const float *)t->cls_Df.p, t->clevel.p,
           (const float *)(const void *)M, (float *)(void *)L);
+  } else if constexpr (std::is_same<T, float>::value) {
+    fmm_note_launch(), k_m2l_f2<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        ps->m2l, p, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, nullptr, (const float *)t->cls_Df.p,
+        t->clevel.p, M, L, mstr, lstr, dstr);
   } else {
     fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
         ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,

@@ -28,8 +28,10 @@ struct HostPlan {
 //
 // Within a (lane, output) segment the order of the terms is free, so each
 // round's terms are chosen to spread the 32 lanes' shared-memory reads of A and
-// of B over distinct banks (4-byte banks; lanes that read the same word share
-// it): lanes are filled in turn, those with the fewest terms left first, each
+// of B over distinct banks -- the 32 4-byte banks across the warp for FP32
+// operands, and the 16 bank pairs within each half-warp for 8-byte ones (FP64,
+// or two FP32 operands side by side); lanes that read the same word share it.
+// Lanes are filled in turn, those with the fewest terms left first, each
 // taking the remaining term of its current segment that collides with the
 // fewest reads already placed in the round.
 // Shared-memory bank conflicts otherwise multiply the engine's load wavefronts
@@ -67,8 +69,10 @@ HostPlan make_plan(const std::vector<std::array<int, 3>> &tasks, int nout) {
     if (!segs[l].empty()) left[l] = segs[l][0].t1 - segs[l][0].t0;
   }
   for (int it = 0; it < P.iters; it++) {
-    int bankA[32], bankB[32];
-    for (int k = 0; k < 32; k++) bankA[k] = bankB[k] = -1;
+    // 4-byte reads: 32 banks over the warp; 8-byte reads (FP64, paired FP32):
+    // 16 bank pairs within each half-warp
+    int bankA[32], bankB[32], pairA[2][16], pairB[2][16];
+    for (int k = 0; k < 32; k++) bankA[k] = bankB[k] = pairA[k >> 4][k & 15] = pairB[k >> 4][k & 15] = -1;
     // lanes with the fewest terms left to choose from go first
     int ord[32];
     for (int k = 0; k < 32; k++) ord[k] = k;
@@ -78,17 +82,22 @@ HostPlan make_plan(const std::vector<std::array<int, 3>> &tasks, int nout) {
       if (cur[l] >= segs[l].size()) continue;
       const Seg &S = segs[l][cur[l]];
       const int base = (int)((long)l * T / 32);
-      int best = -1, bcost = 3;
+      const int h = l >> 4;
+      int best = -1, bcost = 5;
       for (int t = S.t0; t < S.t1 && bcost > 0; t++) {
         if (used[l][t - base]) continue;
         const int a = tasks[t][1], b = tasks[t][2];
-        const int cost = (bankA[a & 31] >= 0 && bankA[a & 31] != a) + (bankB[b & 31] >= 0 && bankB[b & 31] != b);
+        const int cost = (bankA[a & 31] >= 0 && bankA[a & 31] != a) + (bankB[b & 31] >= 0 && bankB[b & 31] != b) +
+                         (pairA[h][a & 15] >= 0 && pairA[h][a & 15] != a) +
+                         (pairB[h][b & 15] >= 0 && pairB[h][b & 15] != b);
         if (cost < bcost) { bcost = cost; best = t; }
       }
       used[l][best - base] = 1;
       const int a = tasks[best][1], b = tasks[best][2];
       if (bankA[a & 31] < 0) bankA[a & 31] = a;
       if (bankB[b & 31] < 0) bankB[b & 31] = b;
+      if (pairA[h][a & 15] < 0) pairA[h][a & 15] = a;
+      if (pairB[h][b & 15] < 0) pairB[h][b & 15] = b;
       const bool end = --left[l] == 0;
       P.task[(size_t)it * 32 + l] =
           (uint32_t)a | ((uint32_t)b << 10) | ((uint32_t)S.id << 20) | ((end ? 1u : 0u) << 31);

@@ -90,3 +90,21 @@ def test_tune_under_graph_replay(fg):
         for _ in range(2):
             t.compute_field_fmm(F, precision="mixed")
             assert np.array_equal(F.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("p,so", [(12, 0), (7, 1), (5, 2)])
+def test_fp32_engine_m2l_vs_fp64(fg, p, so):
+    """The FP32 engine M2L (two source cells per packed-FMA pass, an odd last
+    pair beside zeros) against the FP64 pass, for each source order."""
+    n = 30000
+    rng = np.random.default_rng(40 + p)
+    pos = torch.tensor(rng.uniform(0, 1, (n, 3)), device="cuda")
+    S = torch.tensor(rng.standard_normal((n, {0: 1, 1: 3, 2: 6}[so])), device="cuda")
+    t = fg.build_tree(pos, S, n, 64, p, 0.5, source_order=so)
+    ref = t.compute_field_fmm(precision="fp64").cpu().numpy()
+    t.set_tune(2, 0, 0, 0)
+    F = t.compute_field_fmm(precision="mixed").cpu().numpy()
+    assert rel(F[:, 1:], ref[:, 1:]) < 5e-6
+    assert rel(F[:, 0], ref[:, 0]) < 5e-6
+    again = t.compute_field_fmm(precision="mixed").cpu().numpy()
+    assert np.array_equal(F, again)
