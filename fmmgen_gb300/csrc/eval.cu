@@ -323,14 +323,14 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_var(Plan P, int q, int n
 }
 
 // ---------------------------------------------------------------------------
-// FP32 M2L with two source cells per engine pass.  A and B hold the two
-// pairs' operands side by side (float2), so one task word drives one packed
-// FMA (fma.rn.f32x2) over both: the task-word load and index decoding, which
-// bound the engine's issue rate, are shared by two multiply-adds.  Both halves
-// of the accumulator go to the same output slot.  With `ord` set only the
-// pairs of order q are taken and the sums are added to L (the per-order
-// launches above); with `ord` null every pair is taken at order q and L is
-// written.
+// FP32 M2L with NP (2 or 4) source cells per engine pass.  A and B hold the NP
+// pairs' operands side by side, so one task word drives NP/2 packed FMAs
+// (fma.rn.f32x2): the task-word load and index decoding, which bound the
+// engine's issue rate, are shared by NP multiply-adds.  All lanes of the
+// accumulator go to the same output slot.  With `ord` set only the pairs of
+// order q are taken and the sums are added to L (one launch per order); with
+// `ord` null every pair is taken at order q and L is written.  Missing pairs of
+// a target's last group run beside zeros.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b,
                                                     unsigned long long c) {
@@ -338,15 +338,42 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
   return d;
 }
-__device__ __forceinline__ void engine_run2(const Plan &P, const float2 *A, const float2 *B, float *slots,
-                                            int lane) {
+__device__ __forceinline__ float hsum2(unsigned long long v) {
+  return __uint_as_float((unsigned)v) + __uint_as_float((unsigned)(v >> 32));
+}
+template <int NP> struct PackF;
+template <> struct PackF<2> {
+  using V = unsigned long long;
+  static constexpr int WARPS = 4;
+  struct Acc {
+    unsigned long long a = 0ull;
+    __device__ __forceinline__ void fma(V x, V y) { a = ffma2(x, y, a); }
+    __device__ __forceinline__ float take() { const float r = hsum2(a); a = 0ull; return r; }
+  };
+};
+template <> struct PackF<4> {
+  using V = ulonglong2;
+  static constexpr int WARPS = 2;  // 16.5 KB of operands and slots per warp
+  struct Acc {
+    unsigned long long a = 0ull, b = 0ull;
+    __device__ __forceinline__ void fma(V x, V y) { a = ffma2(x.x, y.x, a); b = ffma2(x.y, y.y, b); }
+    __device__ __forceinline__ float take() {
+      const float r = hsum2(a) + hsum2(b);
+      a = b = 0ull;
+      return r;
+    }
+  };
+};
+template <int NP>
+__device__ __forceinline__ void engine_run_pk(const Plan &P, const float *A, const float *B, float *slots, int lane) {
+  using V = typename PackF<NP>::V;
   constexpr uint32_t PAD = 0xffffffffu;
-  const unsigned long long *A2 = reinterpret_cast<const unsigned long long *>(A);
-  const unsigned long long *B2 = reinterpret_cast<const unsigned long long *>(B);
-  unsigned long long acc = 0ull;
+  const V *A2 = reinterpret_cast<const V *>(A);
+  const V *B2 = reinterpret_cast<const V *>(B);
+  typename PackF<NP>::Acc acc;
   for (int it = 0; it < P.iters; it += 4) {
     uint32_t w[4];
-    unsigned long long a[4], b[4];
+    V a[4], b[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) w[u] = it + u < P.iters ? __ldg(&P.task[(it + u) * 32 + lane]) : PAD;
 #pragma unroll
@@ -358,23 +385,22 @@ __device__ __forceinline__ void engine_run2(const Plan &P, const float2 *A, cons
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       if (w[u] == PAD) return;
-      acc = ffma2(a[u], b[u], acc);
-      if (w[u] >> 31) {
-        slots[(w[u] >> 20) & 2047u] += __uint_as_float((unsigned)acc) + __uint_as_float((unsigned)(acc >> 32));
-        acc = 0ull;
-      }
+      acc.fma(a[u], b[u]);
+      if (w[u] >> 31) slots[(w[u] >> 20) & 2047u] += acc.take();
     }
   }
 }
-__global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_f2(Plan P, int q, int ncells, int so, int order,
-                                                           const int *off_, const int *src, const int *cls,
-                                                           const unsigned char *ord, const float *clsD,
-                                                           const unsigned char *clevel, const float *M, float *L,
-                                                           int mstr, int lstr, int dstr) {
-  __shared__ float2 sA[FMM_WARPS][FMM_NTMAX], sB[FMM_WARPS][FMM_NTMAX];
-  __shared__ float sS[FMM_WARPS][FMM_NTMAX + 32];
+template <int NP>
+__global__ void __launch_bounds__(32 * PackF<NP>::WARPS) k_m2l_pk(Plan P, int q, int ncells, int so, int order,
+                                                                 const int *off_, const int *src, const int *cls,
+                                                                 const unsigned char *ord, const float *clsD,
+                                                                 const unsigned char *clevel, const float *M,
+                                                                 float *L, int mstr, int lstr, int dstr) {
+  constexpr int W = PackF<NP>::WARPS;
+  __shared__ __align__(16) float sA[W][FMM_NTMAX * NP], sB[W][FMM_NTMAX * NP];
+  __shared__ float sS[W][FMM_NTMAX + 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int A = blockIdx.x * FMM_WARPS + w;
+  const int A = blockIdx.x * W + w;
   if (A >= ncells) return;
   const int moff = fmm_nterms(so - 1), nt = fmm_nterms(q), ms = nt - moff, ls = fmm_nterms(q - so);
   const int la = clevel[A];
@@ -392,29 +418,51 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_f2(Plan P, int q, int nc
     hits &= hits - 1;
     return cbase + b;
   };
-  int ka = next();
-  if (ka < 0) {
+  int kc = next();
+  if (kc < 0) {
     if (!ord)
       for (int n = lane; n < ls; n += 32) L[(size_t)A * lstr + n] = 0.f;
     return;
   }
   for (int s = lane; s < P.nseg; s += 32) sS[w][s] = 0.f;
-  while (ka >= 0) {
-    const int kb = next();
-    const int Ba = src[ka], Bb = kb >= 0 ? src[kb] : Ba;
-    const float *Da = clsD + (size_t)cls[ka] * dstr, *Db = kb >= 0 ? clsD + (size_t)cls[kb] * dstr : Da;
-    const int dla = la - (int)clevel[Ba], dlb = la - (int)clevel[Bb];
-    const float zb = kb >= 0 ? 1.f : 0.f;  // an odd last pair runs beside zeros
-    __syncwarp();
-    for (int i = lane; i < nt; i += 32) sA[w][i] = make_float2(Da[i], Db[i]);
-    for (int j = lane; j < ms; j += 32) {
-      const int dg = (int)c_mi[j + moff][3];
-      sB[w][j] = make_float2(M[(size_t)Ba * mstr + j] * exp2i<float>(dla * dg),
-                             zb * M[(size_t)Bb * mstr + j] * exp2i<float>(dlb * dg));
+  while (kc >= 0) {
+    const float *Dp[NP];
+    const float *Mp[NP];
+    int dl[NP];
+    float z[NP];
+    int ks[NP];
+    ks[0] = kc;
+#pragma unroll
+    for (int u = 1; u < NP; u++) ks[u] = next();  // -1 once the pairs run out, and after
+#pragma unroll
+    for (int u = 0; u < NP; u++) {
+      const bool have = ks[u] >= 0;
+      const int kk = have ? ks[u] : kc;  // a missing pair reads the first one's rows, scaled by zero
+      const int B = src[kk];
+      Dp[u] = clsD + (size_t)cls[kk] * dstr;
+      Mp[u] = M + (size_t)B * mstr;
+      dl[u] = la - (int)clevel[B];
+      z[u] = have ? 1.f : 0.f;
     }
     __syncwarp();
-    engine_run2(P, sA[w], sB[w], sS[w], lane);
-    ka = kb >= 0 ? next() : -1;
+    for (int i = lane; i < nt; i += 32) {
+      float v[NP];
+#pragma unroll
+      for (int u = 0; u < NP; u++) v[u] = Dp[u][i];
+#pragma unroll
+      for (int u = 0; u < NP; u++) sA[w][i * NP + u] = v[u];
+    }
+    for (int j = lane; j < ms; j += 32) {
+      const int dg = (int)c_mi[j + moff][3];
+      float v[NP];
+#pragma unroll
+      for (int u = 0; u < NP; u++) v[u] = z[u] * Mp[u][j] * exp2i<float>(dl[u] * dg);
+#pragma unroll
+      for (int u = 0; u < NP; u++) sB[w][j * NP + u] = v[u];
+    }
+    __syncwarp();
+    engine_run_pk<NP>(P, sA[w], sB[w], sS[w], lane);
+    kc = z[NP - 1] != 0.f ? next() : -1;
   }
   __syncwarp();
   for (int n = lane; n < ls; n += 32) {
@@ -423,6 +471,9 @@ __global__ void __launch_bounds__(32 * FMM_WARPS) k_m2l_f2(Plan P, int q, int nc
     else L[(size_t)A * lstr + n] = v;
   }
 }
+// Two pairs per pass: four measured slower (the 16.5 KB per warp halves the
+// warps an SM holds; learned 8e6 step 747 -> 762 ms).
+#define M2L_PACK 2
 
 // ---------------------------------------------------------------------------
 // L2L for all cells of one level (example/calculate.cpp:219-234)
@@ -678,7 +729,7 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
       const PlanSet *pq = fmm_get_plans(q, so);
       if (!pq) return FMM_ERR_CUDA;
       if constexpr (std::is_same<T, float>::value)
-        fmm_note_launch(), k_m2l_f2<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+        fmm_note_launch(), k_m2l_pk<M2L_PACK><<<fmm_blocks(nc, PackF<M2L_PACK>::WARPS), 32 * PackF<M2L_PACK>::WARPS, 0, st>>>(
             pq->m2l, q, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, t->m2l_ord.p, (const float *)t->cls_Df.p,
             t->clevel.p, M, L, mstr, lstr, dstr);
       else
@@ -699,7 +750,7 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
           (const float *)t->cls_Df.p, t->clevel.p,
           (const float *)(const void *)M, (float *)(void *)L);
   } else if constexpr (std::is_same<T, float>::value) {
-    fmm_note_launch(), k_m2l_f2<<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
+    fmm_note_launch(), k_m2l_pk<M2L_PACK><<<fmm_blocks(nc, PackF<M2L_PACK>::WARPS), 32 * PackF<M2L_PACK>::WARPS, 0, st>>>(
         ps->m2l, p, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, nullptr, (const float *)t->cls_Df.p,
         t->clevel.p, M, L, mstr, lstr, dstr);
   } else {
