@@ -371,11 +371,19 @@ __device__ __forceinline__ void engine_run_pk(const Plan &P, const float *A, con
   const V *A2 = reinterpret_cast<const V *>(A);
   const V *B2 = reinterpret_cast<const V *>(B);
   typename PackF<NP>::Acc acc;
+  // the next round's task words are requested while this round's operands are
+  // read and applied (they come from L2 when the plan does not fit in L1)
+  uint32_t wn[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) wn[u] = u < P.iters ? __ldg(&P.task[u * 32 + lane]) : PAD;
   for (int it = 0; it < P.iters; it += 4) {
     uint32_t w[4];
     V a[4], b[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) w[u] = it + u < P.iters ? __ldg(&P.task[(it + u) * 32 + lane]) : PAD;
+    for (int u = 0; u < 4; u++) {
+      w[u] = wn[u];
+      wn[u] = it + 4 + u < P.iters ? __ldg(&P.task[(it + 4 + u) * 32 + lane]) : PAD;
+    }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const uint32_t x = w[u] == PAD ? 0u : w[u];
