@@ -32,11 +32,18 @@ template <typename T>
 __device__ __forceinline__ void engine_run(const Plan &P, const T *A, const T *B, T *slots, int lane) {
   constexpr uint32_t PAD = 0xffffffffu;
   T acc = T(0);
+  // the next round's task words are requested while this round is applied
+  uint32_t wn[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) wn[u] = u < P.iters ? __ldg(&P.task[u * 32 + lane]) : PAD;
   for (int it = 0; it < P.iters; it += 4) {
     uint32_t w[4];
     T a[4], b[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) w[u] = it + u < P.iters ? __ldg(&P.task[(it + u) * 32 + lane]) : PAD;
+    for (int u = 0; u < 4; u++) {
+      w[u] = wn[u];
+      wn[u] = it + 4 + u < P.iters ? __ldg(&P.task[(it + 4 + u) * 32 + lane]) : PAD;
+    }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const uint32_t x = w[u] == PAD ? 0u : w[u];
