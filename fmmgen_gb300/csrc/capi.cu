@@ -168,6 +168,7 @@ void scalar_op(int op, T x, T y, T z, const T *in, int insize, T *out, int outsi
 bool order_ok(int order) {
   return order >= g_cfg.so + (g_cfg.field ? 1 : 0) && order <= g_cfg.maxorder && order <= FMM_PMAX;
 }
+bool fixed_order_ok(int order) { return order >= g_cfg.so + (g_cfg.field ? 1 : 0) && order <= FMM_PMAX; }
 }  // namespace
 
 extern "C" {
@@ -244,6 +245,52 @@ void P2Pf(float x, float y, float z, float *Sv, float *F) {
   scalar_op<float>(5, x, y, z, Sv, fmmgen_sourcesize(g_cfg.so), F, fmmgen_outputsize(g_cfg.potential, g_cfg.field),
                    0);
 }
+
+// Per-order functions of the generated code (P2M_p ... M2P_p, fmmgen/writer.py:142-264,
+// declared in include/operators.h).  The generator emits them for p in
+// [minorder, maxorder); here every p up to 12 exists and applies order p under the
+// configured source order and outputs, whatever the dispatchers' highest order is;
+// p below the minimum order is a no-op.
+#define FMM_PER_ORDER(p)                                                                                         \
+  void P2M_##p(double x, double y, double z, double q, double *M) {                                           \
+    if (fixed_order_ok(p)) scalar_op<double>(0, x, y, z, &q, 1, M, (int)fmmgen_msize(p, g_cfg.so), p);         \
+  }                                                                                                            \
+  void M2M_##p(double x, double y, double z, double *M, double *Ms) {                                         \
+    int ms = (int)fmmgen_msize(p, g_cfg.so);                                                                   \
+    if (fixed_order_ok(p)) scalar_op<double>(1, x, y, z, M, ms, Ms, ms, p);                                    \
+  }                                                                                                            \
+  void M2L_##p(double x, double y, double z, double *M, double *L) {                                          \
+    if (fixed_order_ok(p))                                                                                     \
+      scalar_op<double>(2, x, y, z, M, (int)fmmgen_msize(p, g_cfg.so), L, (int)fmmgen_lsize(p, g_cfg.so), p);  \
+  }                                                                                                            \
+  void L2L_##p(double x, double y, double z, double *L, double *Ls) {                                         \
+    int ls = (int)fmmgen_lsize(p, g_cfg.so);                                                                   \
+    if (fixed_order_ok(p)) scalar_op<double>(3, x, y, z, L, ls, Ls, ls, p);                                    \
+  }                                                                                                            \
+  void L2P_##p(double x, double y, double z, double *L, double *F) {                                          \
+    if (fixed_order_ok(p))                                                                                     \
+      scalar_op<double>(4, x, y, z, L, (int)fmmgen_lsize(p, g_cfg.so), F,                                     \
+                        fmmgen_outputsize(g_cfg.potential, g_cfg.field), p);                                   \
+  }                                                                                                            \
+  void M2P_##p(double x, double y, double z, double *M, double *F) {                                          \
+    if (fixed_order_ok(p))                                                                                     \
+      scalar_op<double>(6, x, y, z, M, (int)fmmgen_msize(p, g_cfg.so), F,                                     \
+                        fmmgen_outputsize(g_cfg.potential, g_cfg.field), p);                                   \
+  }
+FMM_PER_ORDER(0)
+FMM_PER_ORDER(1)
+FMM_PER_ORDER(2)
+FMM_PER_ORDER(3)
+FMM_PER_ORDER(4)
+FMM_PER_ORDER(5)
+FMM_PER_ORDER(6)
+FMM_PER_ORDER(7)
+FMM_PER_ORDER(8)
+FMM_PER_ORDER(9)
+FMM_PER_ORDER(10)
+FMM_PER_ORDER(11)
+FMM_PER_ORDER(12)
+#undef FMM_PER_ORDER
 
 // ---------------------------------------------------------------------------
 // tree API

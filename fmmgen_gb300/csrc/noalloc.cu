@@ -12,11 +12,19 @@
 // and latency-bound callers that cannot afford cudaMalloc's implicit device
 // synchronisation.
 //
-// The array is sized for at most FMMGEN_NOALLOC_MAX_N particles and is part of
-// the library image: every GPU that loads the library holds it until the
-// process exits.  All calls share it and it keeps the last call's contents;
-// what must start at zero (the maxima) is cleared by each call on its own
-// stream.  Calls whose work overlaps on the GPU (different streams, or
+// The array is sized for at most FMMGEN_NOALLOC_MAX_N particles.  CUDA loads
+// a library's device code lazily by default (CUDA_MODULE_LOADING=LAZY): the
+// array, and the kernels this function launches, are placed on a device when
+// the first call on that device looks the array up and launches them, and they
+// stay there until the process exits (or the context is destroyed).  So the
+// first call on each device needs the array's ~11 MiB and the kernels' code to
+// be free on it: make that first call (a tiny input will do) before another
+// allocator takes the GPU's free memory, and before any stream capture; later
+// calls allocate nothing.  The looked-up address is cached per device for the
+// life of the process: do not call this function again on a device after
+// cudaDeviceReset.  All calls share the array and it keeps the last call's
+// contents; what must start at zero (the maxima) is cleared by each call on
+// its own stream.  Calls whose work overlaps on the GPU (different streams, or
 // different host threads) race on the array and give wrong results.
 #include <algorithm>
 #include <mutex>

@@ -172,11 +172,16 @@ int fmmgen_tree_free(fmmgen_tree *tree);
  * device memory: no counterpart in the reference.  For callers that cannot call
  * cudaMalloc where they need the cube (another allocator already holds the
  * GPU's free memory, or cudaMalloc's implicit synchronisation is not
- * acceptable).  Its scratch is one static device array of ~11 MiB held by
- * every GPU that loads the library, enough for N <= FMMGEN_NOALLOC_MAX_N;
- * larger N returns FMMGEN_ERR_ARG.  The first call on a device looks the
- * array's address up (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * acceptable).  Its scratch is one static device array of ~11 MiB, enough
+ * for N <= FMMGEN_NOALLOC_MAX_N; larger N returns FMMGEN_ERR_ARG.  CUDA loads
+ * device code lazily by default, so the first call on a device places the
+ * array and this function's kernels there and looks the array's address up
+ * (cudaGetSymbolAddress): make that first call (a tiny input will do) before
+ * another allocator takes the GPU's free memory and before any stream
+ * capture; later calls allocate nothing, and the device keeps the array until
+ * the process exits.  Not for use on a device after cudaDeviceReset (the
+ * address is cached per device).  All calls share the array: calls that
+ * overlap on the GPU race. */
 #define FMMGEN_NOALLOC_MAX_N 16777216L
 int fmmgen_root_box_noalloc(const double *pos, long N, double *root4, void *stream);
 

@@ -33,7 +33,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-DEFAULT_REF = "/root/reference"
+# the reference checkout: $FMMGEN_REFERENCE_DIR, else where the development container mounts it
+DEFAULT_REF = os.environ.get("FMMGEN_REFERENCE_DIR", "/root/reference")
 
 
 def _generate(args):

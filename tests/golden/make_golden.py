@@ -11,6 +11,7 @@ Barnes-Hut fixtures (compute_field_bh, M2P) keep potentials only: the
 generated M2P's field is not the gradient of its potential.
 `--bh` writes only the Barnes-Hut fixtures; `--so2` only the quadrupole-source
 fixtures (ops_so2.npz, tree_quadrupole_plummer.npz, m2p_potential_so2.npz).
+`--trees a,b` writes only the named tree fixtures.
 `--f32` (after `build_ref.py --float`) writes ops_f32_so{0,1,2}.npz: the outputs
 of the reference's precision="float" operators on the inputs of ops_so*.npz
 rounded to float32 -- the accuracy the FP32 variant is held to.
@@ -148,6 +149,10 @@ CASES = {
     "tiny": (50, 64, 3, 0.5, 0, "uniform"),
     "example_scaled": (2000, 64, 4, 0.5, 0, "example"),
     "quadrupole_plummer": (3000, 32, 4, 0.5, 2, "plummer"),
+    # small enough for a caller that applies every operator through the scalar
+    # operators of include/operators.h (tests/test_gpu_operators_h.py)
+    "small_charges": (400, 16, 3, 0.5, 0, "uniform"),
+    "small_dipoles": (300, 16, 3, 0.5, 1, "plummer"),
 }
 
 
@@ -257,6 +262,8 @@ if __name__ == "__main__":
         make_m2p(((2, (3, 5)),), "m2p_potential_so2.npz", 78)
     elif "--bh" in sys.argv:
         make_bh()
+    elif "--trees" in sys.argv:  # --trees name[,name...]: only these tree fixtures
+        make_trees(only=set(sys.argv[sys.argv.index("--trees") + 1].split(",")))
     else:
         make_ops()
         make_trees()

@@ -1,4 +1,4 @@
-"""Tensor-core M2L (tcgen05, 3xTF32) of the mixed pass against the FP64 pass
+"""Tensor-core M2L (tcgen05 kind::f16, 3 FP16 products per term) of the mixed pass against the FP64 pass
 and the FP32 CUDA-core M2L kernels, on the local expansions every cell ends
 with and on the field."""
 import numpy as np
@@ -49,7 +49,7 @@ def test_tc_m2l_local_expansions(fg, p, so, dist, ncrit):
     assert np.array_equal(Ftc, Ftc2)
     Fs = t.compute_field_fmm(precision="mixed_simt").cpu().numpy()
     _, Ls = t.expansions()
-    # the 3xTF32 products carry ~2^-22 relative error against FP32's 2^-24:
+    # the 3xFP16 products carry ~2^-22 relative error against FP32's 2^-24:
     # the local expansions stay within a few times the CUDA-core FP32 error
     e_tc, e_s = rel(Ltc, L64), rel(Ls, L64)
     assert e_tc < max(8 * e_s, 1e-6), (e_tc, e_s)

@@ -41,6 +41,26 @@ def test_noalloc_root_box_matches_build_twice(fg):
     assert np.array_equal(root_noalloc(fg, a), ra)
 
 
+def test_noalloc_call_allocates_nothing(fg):
+    """After a warm-up call on the device (which places the static array and the
+    kernels there), a call leaves the device's free memory unchanged."""
+    rng = np.random.default_rng(5)
+    a = torch.tensor(rng.uniform(0, 1, (200_003, 3)), device="cuda")
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib = fg.lib()
+    assert lib.fmmgen_root_box_noalloc(C.c_void_p(a.data_ptr()), 1000, C.c_void_p(out.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert lib.fmmgen_root_box_noalloc(C.c_void_p(a.data_ptr()), a.shape[0], C.c_void_p(out.data_ptr()),
+                                           stream) == 0, lib.fmmgen_last_error()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, (free0, free1)
+    assert np.array_equal(out.cpu().numpy(), root_via_build(fg, a))
+
+
 def test_noalloc_rejects_oversize(fg):
     from fmmgen_gb300 import _lib
 
