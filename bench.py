@@ -81,7 +81,8 @@ def args_parse():
     ap.add_argument("--tune", default=None,
                     help="impl,nslots,grouping,overlap: set the M2L choice instead of running the autotuner")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--cpu-stride", type=int, default=32, help="CPU baseline samples every k-th target cell")
+    ap.add_argument("--cpu-stride", type=int, default=1,
+                    help="CPU baseline evaluates every k-th target cell and scales (1: the full pass, the default)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup + timed steps only (no e2e, FP64, direct sum, CPU baseline): for ncu captures")
     a = ap.parse_args()
@@ -296,14 +297,16 @@ def run_reference(a, rank, world):
 
     sp.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
     pos, q = workload(a, a.seed)
-    stride = max(a.cpu_stride, 64)
+    # every step is the whole workload: tree build and the full evaluation
+    # (stride 1, nothing sampled or scaled), timed on the wall clock
     for _ in range(a.warmup):
-        cpu_sample(pos, q, a, stride)
+        cpu_sample(pos, q, a, 1)
     t0 = time.perf_counter()
     est = 0.0
     for _ in range(a.steps):
-        v, t_full, sample, cores = cpu_sample(pos, q, a, stride)
-        est += t_full
+        ts = time.perf_counter()
+        v, t_full, sample, cores = cpu_sample(pos, q, a, 1)
+        est += time.perf_counter() - ts
     wall = time.perf_counter() - t0
     value = a.n * a.steps / est
     line = {"impl": "reference", "metric": metric_name(a), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
