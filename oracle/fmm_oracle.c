@@ -560,7 +560,11 @@ static void or_tree_multipoles(otree_t *t, double *M) { or_tree_multipoles_t(t, 
  * caller's particle order, overwritten.  M/L buffers are returned through
  * Mout/Lout when non-NULL (cells x Msize / Lsize, creation order).
  * sample_stride > 1 restricts the M2L, P2P, L2L-consumer and L2P phases to every
- * sample_stride-th target cell (CPU-baseline sampling); 1 = the full pass.
+ * sample_stride-th target cell (CPU-baseline sampling; fields incomplete);
+ * 1 = the full pass; sample_stride < -1 evaluates the exact fields of the
+ * particles of every |sample_stride|-th leaf cell: M2L into those leaves and
+ * all their ancestors, P2P and L2P at those leaves (a target subset for
+ * checking), other rows of F stay zero.
  * times: [P2M, M2M, M2L, P2P, L2L, L2P] seconds. */
 int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_stride,
                      double *Mout, double *Lout, double *times) {
@@ -571,7 +575,22 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     int ssize = (int)or_sourcesize(so);
     long msize = or_msize(order, so), lsize = or_lsize(order, so);
     long nc = t->ncells, N = t->N, ncrit = t->ncrit;
-    if (sample_stride < 1) sample_stride = 1;
+    /* need[c]: M2L into c; leafsel[c]: P2P and L2P at c */
+    unsigned char *need = (unsigned char *)malloc((size_t)nc), *leafsel = (unsigned char *)malloc((size_t)nc);
+    if (sample_stride < -1) {
+        long k = -sample_stride, nleaves = 0;
+        memset(need, 0, (size_t)nc);
+        memset(leafsel, 0, (size_t)nc);
+        for (long c = 0; c < nc; c++) {
+            if (t->cells[c].nleaf >= ncrit) continue;
+            if (nleaves++ % k) continue;
+            leafsel[c] = 1;
+            for (long a = c; a >= 0 && !need[a]; a = t->cells[a].parent) need[a] = 1;
+        }
+    } else {
+        if (sample_stride < 1) sample_stride = 1;
+        for (long c = 0; c < nc; c++) need[c] = leafsel[c] = (unsigned char)(c % sample_stride == 0);
+    }
     double *M = (double *)calloc((size_t)nc * msize, sizeof(double));
     double *L = (double *)calloc((size_t)nc * lsize, sizeof(double));
     memset(F, 0, sizeof(double) * N * outsize);
@@ -586,7 +605,8 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     csr_by_target(t->np2p, t->p2p, 0, nc, &poff, &psrc, NULL);
     /* M2L (example/calculate.cpp:190-206), grouped by target instead of atomics */
 #pragma omp parallel for schedule(dynamic, 8)
-    for (long A = 0; A < nc; A += sample_stride) {
+    for (long A = 0; A < nc; A++) {
+        if (!need[A]) continue;
         for (long k = moff[A]; k < moff[A + 1]; k++) {
             long B = msrc[k];
             int q = t->m2l_ord ? t->m2l_ord[mpair[k]] : order;
@@ -597,7 +617,8 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     double t3 = now_s();
     /* P2P (example/calculate.cpp:24-40, 208-216) */
 #pragma omp parallel for schedule(dynamic, 8)
-    for (long A = 0; A < nc; A += sample_stride) {
+    for (long A = 0; A < nc; A++) {
+        if (!leafsel[A]) continue;
         const ocell_t *ca = &t->cells[A];
         for (long k = poff[A]; k < poff[A + 1]; k++) {
             const ocell_t *cb = &t->cells[psrc[k]];
@@ -626,7 +647,8 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     double t5 = now_s();
     /* L2P (example/calculate.cpp:236-250) */
 #pragma omp parallel for schedule(dynamic, 16)
-    for (long c = 0; c < nc; c += sample_stride) {
+    for (long c = 0; c < nc; c++) {
+        if (!leafsel[c]) continue;
         const ocell_t *cc = &t->cells[c];
         if (cc->nleaf >= ncrit) continue;
         for (long i = 0; i < cc->nleaf; i++) {
@@ -640,7 +662,7 @@ int or_tree_evaluate(void *h, double *F, int potential, int field, long sample_s
     if (times) memcpy(times, tt, sizeof(tt));
     if (Mout) memcpy(Mout, M, sizeof(double) * nc * msize);
     if (Lout) memcpy(Lout, L, sizeof(double) * nc * lsize);
-    free(M); free(L); free(moff); free(msrc); free(mpair); free(poff); free(psrc);
+    free(M); free(L); free(moff); free(msrc); free(mpair); free(poff); free(psrc); free(need); free(leafsel);
     return 0;
 }
 

@@ -47,8 +47,8 @@ def test_headline_tree_and_fields_vs_oracle(fg, oracle_lib):
     pos, S = bench_inputs("uniform", 1_000_000, 0)
     t, ot = oracle_vs_device(fg, oracle_lib, pos, S, 128, 8, 0.5, 0)
     assert (t.ncells, t.nm2l) == (37449, 15678688)
-    # the restatement's FP64 FMM on every 97th target cell (about 10^4 targets)
-    Fo, _ = ot.evaluate(potential=False, field=True, sample_stride=97)
+    # the restatement's exact FP64 FMM at the particles of every 97th leaf (about 10^4 targets)
+    Fo, _ = ot.evaluate(potential=False, field=True, sample_stride=-97)
     rows = np.flatnonzero(np.any(Fo != 0.0, axis=1))
     assert 5_000 < len(rows) < 20_000
     Fm = t.compute_field_fmm(potential=False, field=True, precision="mixed").cpu().numpy()

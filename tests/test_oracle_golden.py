@@ -166,3 +166,17 @@ def test_oracle_rejects_coincident_points(oracle_lib):
     pos = np.zeros((100, 3))
     with pytest.raises(ValueError):
         oracle_lib.OracleTree(pos, np.ones((100, 1)), 8, 3, 0.5, 0)
+
+
+def test_exact_target_subset_equals_full_pass(oracle_lib):
+    """sample_stride < -1: the fields of every k-th leaf's particles equal the
+    full pass's bit for bit (M2L into their ancestors too), other rows zero."""
+    rng = np.random.default_rng(31)
+    pos = rng.uniform(0, 1, (20000, 3))
+    q = rng.uniform(-1, 1, (20000, 1))
+    ot = oracle_lib.OracleTree(pos, q, 32, 4, 0.5, 0)
+    Ff, _ = ot.evaluate()
+    Fs, _ = ot.evaluate(sample_stride=-7)
+    rows = np.any(Fs != 0.0, axis=1)
+    assert 1000 < rows.sum() < 6000
+    assert np.array_equal(Fs[rows], Ff[rows])
