@@ -368,7 +368,7 @@ def main():
         r = tree.autotune(precision="mixed", reps=3)
         autotune = {"chosen": r["best"], "candidates_ms": [
             [c["impl"], c["nslots"], c["grouping"], c["overlap"], round(c["ms"], 3)] for c in r["table"]],
-            "legend": "impl 0 tensor cores / 1 generated CUDA-core / 2 contraction engine; nslots = tensor-core "
+            "legend": "impl 0 tensor cores (row gather) / 1 generated CUDA-core / 2 contraction engine / 3 tensor cores (level-grid boxes); nslots = tensor-core "
                       "pipeline depth; grouping 0 by octant / 1 Morton; overlap 1 / 2 = M2L and P2P side by side "
                       "(P2P blocks of 4 / 2 warps); "
                       "M2L + P2P median ms"}
@@ -414,7 +414,7 @@ def main():
     with ClockSampler(local) as clk:
         dev_ms, wall = timed(a.steps, step, collect_phases=True)
     launches = L.fmmgen_launch_count() - n0
-    m2l_steps, m2l_mmas, m2l_exec_flops = tree.m2l_work()  # of the last timed (mixed) step
+    m2l_steps, m2l_mmas, m2l_exec_flops, m2l_boxes = tree.m2l_work()  # of the last timed (mixed) step
     m2l_orders = tree.m2l_orders() if model is not None else None
     t_max = max_over_ranks(dev_ms, pg, dev)
     value = job_throughput(a.n, a.steps, world, t_max)

@@ -514,7 +514,8 @@ extern "C" int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, doubl
   return FMM_OK;
 }
 
-extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3) {
+extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out4) {
+  double *out3 = out4;
   if (!tree || !tree->built || !out3) return ret(FMM_ERR_STATE);
   FMM_CUDA_TRY(cudaDeviceSynchronize());
   DevTree &t = tree->t;
@@ -526,6 +527,7 @@ extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3) {
   out3[0] = (double)steps;
   out3[1] = (double)steps * (double)mmas;
   out3[2] = (double)steps * flops;
+  out4[3] = t.tc_boxes_last ? 1.0 : 0.0;
   return FMM_OK;
 }
 
@@ -535,9 +537,9 @@ int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping, 
   g_err.clear();
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   DevTree &t = tree->t;
-  if (impl < -1 || impl > 2 || nslots < 0 || grouping < 0 || grouping > 1 || overlap < 0 || overlap > 2)
+  if (impl < -1 || impl > 3 || nslots < 0 || grouping < 0 || grouping > 1 || overlap < 0 || overlap > 2)
     return ret(FMM_ERR_ARG);
-  if (impl == 0 && !fmm_m2l_tc_supported(t.order, t.so)) {
+  if ((impl == 0 || impl == 3) && !fmm_m2l_tc_supported(t.order, t.so)) {
     fmm_set_error_text("the tensor-core M2L does not support this order / source order");
     return ret(FMM_ERR_ARG);
   }

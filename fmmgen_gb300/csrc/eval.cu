@@ -672,9 +672,12 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
 
 // M2L implementation of a pass: per-pair orders when set; else (mixed pass)
 // the tuned choice or, by default, tensor cores where the order allows
-// (p <= 9, precision "mixed"), else the generated CUDA-core kernels where this
-// order has them, else the warp contraction engine; FP64: the engine.
-enum { M2L_TC = 0, M2L_GEN = 1, M2L_ENGINE = 2 };
+// (p <= 9, precision "mixed": with source rows boxed from level grids when
+// every level is complete, else gathered row by row), else the generated
+// CUDA-core kernels where this order has them, else the warp contraction
+// engine; FP64: the engine.
+enum { M2L_TC = 0, M2L_GEN = 1, M2L_ENGINE = 2, M2L_TCG = 3 };
+static inline bool is_tc(int impl) { return impl == M2L_TC || impl == M2L_TCG; }
 bool fmm_m2l_gen_supported(int p, int so) {
   m2l_reg_kernel kg[4];
   int kt[4];
@@ -684,8 +687,8 @@ static int m2l_impl(const DevTree *t, int precision) {
   if (precision == 0) return M2L_ENGINE;
   const bool tc_ok = fmm_m2l_tc_supported(t->order, t->so), gen_ok = fmm_m2l_gen_supported(t->order, t->so);
   int impl = t->tune.impl;
-  if (impl < 0) impl = precision == 1 ? M2L_TC : M2L_GEN;
-  if (impl == M2L_TC && (!tc_ok || t->nclasses > 262144)) impl = M2L_GEN;  // class bitmap of the tile schedule
+  if (impl < 0) impl = precision == 1 ? M2L_TCG : M2L_GEN;
+  if (is_tc(impl) && (!tc_ok || t->nclasses > 262144)) impl = M2L_GEN;  // class bitmap of the tile schedule
   if (impl == M2L_GEN && !gen_ok) impl = M2L_ENGINE;
   return impl;
 }
@@ -709,7 +712,7 @@ static int side_stream(DevTree *t) {
 template <typename T>
 static int m2l_p2p(DevTree *t, const PlanSet *ps, const double *S, const T *M, T *L, bool mixed, int impl, int mstr,
                    int lstr, int dstr, cudaStream_t st) {
-  if (!(t->tune.overlap && mixed && impl == M2L_TC && t->nm2l > 0)) {
+  if (!(t->tune.overlap && mixed && is_tc(impl) && t->nm2l > 0)) {
     TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, st));
     TRY(rec(t, 3, st));
     TRY(fmm_p2p_launch(t, mixed, S, st));
@@ -731,7 +734,7 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
                      int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so, nc = t->ncells;
   // every M2L but the tensor cores' reads the target lists
-  if (t->ord_mode != 0 || !(mixed && impl == M2L_TC)) TRY(fmm_m2l_csr(t, st));
+  if (t->ord_mode != 0 || !(mixed && is_tc(impl))) TRY(fmm_m2l_csr(t, st));
   if (t->ord_mode != 0) {
     // per-pair orders: predicted now from this pass's multipoles, or given
     if (t->ord_mode == 2) TRY(fmm_learned_orders(t, st));
@@ -753,8 +756,8 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
             mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L,
             mstr, lstr, dstr);
     }
-  } else if (mixed && impl == M2L_TC) {
-    TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st));
+  } else if (mixed && is_tc(impl)) {
+    TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st, impl == M2L_TCG));
   } else if (mixed && impl == M2L_GEN) {
     m2l_reg_kernel kg[4];
     int kthreads[4];
@@ -958,7 +961,7 @@ static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L
   if (!learned) {  // beside the M2L, launched after it
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_s, 0));
-    TRY(fmm_p2p_launch(t, mixed, S, st, mixed && impl == M2L_TC && t->tune.overlap == 2));
+    TRY(fmm_p2p_launch(t, mixed, S, st, mixed && is_tc(impl) && t->tune.overlap == 2));
   }
   FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
   TRY(rec(t, 4, st));

@@ -114,6 +114,8 @@ struct DevTree {
   DevBuf<int> tc_sched_off;               // class-step schedule of the tensor-core M2L tiles
   DevBuf<unsigned> tc_sched_cls, tc_bitmap, tc_rank;
   DevBuf<int> tc_stab, tc_pos;            // per class step: each tile row's source (-1: none); row of each cell
+  void *tcg = nullptr;                    // level-grid tensor-core M2L state (m2l_tc.cu, fmm_tcg_release)
+  int tc_boxes_last = 0;                  // the last tensor-core M2L boxed its source rows from level grids
   uint64_t sched_serial = ~0ull, sched_version = ~0ull;  // ... of this build and cell order
   uint64_t order_version = 0;             // incremented whenever m2l_order is rewritten
   int tc_order = -1, tc_so = -1;          // ... and to this expansion order and source order
@@ -195,7 +197,10 @@ int fmm_mlp_train_step(const float *params, const float *X, const unsigned char 
 int fmm_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, cudaStream_t st);
 int fmm_learned_orders(DevTree *t, cudaStream_t st);
 bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops);
-int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st);
+// boxes: source rows by tensor-map box loads from level grids where every level is complete
+int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st, bool boxes);
+void fmm_tcg_release(DevTree *t);
+bool fmm_m2l_tc_boxes_ok(DevTree *t, cudaStream_t st);  // the level-grid path can run on this build
 // M2M of the parents / L2L into the children of cells [lo, hi), FP32 scaled expansions (shift.cu)
 int fmm_m2m_tab(DevTree *t, int lo, int hi, float *M, int mstr, cudaStream_t st);
 int fmm_l2l_tab(DevTree *t, int lo, int hi, float *L, int lstr, cudaStream_t st);

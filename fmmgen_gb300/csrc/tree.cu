@@ -1128,6 +1128,7 @@ int fmm_m2l_cell_order(DevTree *t, int grouping, cudaStream_t st) {
 void fmm_tree_destroy(DevTree *t) {
   if (!t) return;
   fmm_graph_release(t);
+  fmm_tcg_release(t);
   for (cudaEvent_t *e : {&t->ev_fork, &t->ev_join, &t->ev_m, &t->ev_c, &t->ev_p, &t->ev_s, &t->ev_l}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;

@@ -2,8 +2,10 @@
 // M2L is one OpenMP loop, example/calculate.cpp:190-206).
 //
 // Candidates, for the tree's order and source order:
-//   implementation: tensor cores (p <= 9), generated CUDA-core kernels
-//                   (orders that have them), warp contraction engine;
+//   implementation: tensor cores (p <= 9) with source rows gathered row by row
+//                   or (trees whose levels are all complete) boxed from level
+//                   grids, generated CUDA-core kernels (orders that have them),
+//                   warp contraction engine;
 //   tensor-core pipeline depth: 2 .. the row-gather slots that fit in shared memory;
 //   tensor cores alone, or overlapped with the P2P (in 4- or 2-warp blocks);
 //   grouping of the cells into tiles / warps: by octant within the parent, or Morton.
@@ -28,10 +30,15 @@ int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_c
   std::vector<Cand> cands;
   const int maxs = fmm_m2l_tc_max_slots(t->order, t->so);
   const bool gen = fmm_m2l_gen_supported(t->order, t->so);
+  const bool boxes = precision != 0 && maxs > 0 && fmm_m2l_tc_boxes_ok(t, st);
   for (int g = 0; g < 2; g++) {
     if (precision != 0) {
       for (int ov = 0; ov < 3; ov++)
-        for (int s = 2; s <= maxs; s++) cands.push_back({0, s, g, ov});
+        for (int s = 2; s <= maxs; s++) {
+          cands.push_back({0, s, g, ov});
+          // level-grid boxes (their tiles do not depend on the grouping)
+          if (g == 0 && boxes) cands.push_back({3, s, g, ov});
+        }
       if (gen) cands.push_back({1, 0, g, 0});
     }
     cands.push_back({2, 0, g, 0});
@@ -92,7 +99,7 @@ int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_c
   for (int c = 0; c < std::min(n, max_cand); c++) {
     if (cand4) {
       cand4[4 * c] = cands[c].impl;
-      cand4[4 * c + 1] = cands[c].impl == 0 ? cands[c].nslots : 0;
+      cand4[4 * c + 1] = (cands[c].impl == 0 || cands[c].impl == 3) ? cands[c].nslots : 0;
       cand4[4 * c + 2] = cands[c].grouping;
       cand4[4 * c + 3] = cands[c].overlap;
     }

@@ -227,8 +227,10 @@ class Tree:
     M2L_IMPLS = {-1: "default", 0: "tensor cores", 1: "generated CUDA-core kernels", 2: "contraction engine"}
 
     def set_tune(self, impl=-1, nslots=0, grouping=0, overlap=0):
-        """M2L implementation (-1 default rules, 0 tensor cores, 1 generated
-        CUDA-core kernels, 2 contraction engine), tensor-core pipeline depth
+        """M2L implementation (-1 default rules, 0 tensor cores with source rows
+        gathered row by row, 1 generated CUDA-core kernels, 2 contraction
+        engine, 3 tensor cores with source rows boxed from level grids where
+        every level is complete, else as 0), tensor-core pipeline depth
         (0: as deep as fits), cell grouping (0 by octant, 1 Morton) and
         overlap (1 / 2: tensor-core M2L and P2P side by side on the SMs, the
         P2P in blocks of 4 / 2 warps)."""
@@ -295,8 +297,9 @@ class Tree:
         return o[: self.nm2l]
 
     def m2l_work(self):
-        """Last tensor-core M2L: (class steps, MMA instructions, executed tensor flops)."""
-        w = np.zeros(3)
+        """Last tensor-core M2L: (class steps, MMA instructions, executed tensor
+        flops, 1.0 if its source rows were boxed from level grids else 0.0)."""
+        w = np.zeros(4)
         check(lib().fmmgen_tree_m2l_work(self._h, w.ctypes.data))
         return tuple(float(x) for x in w)
 

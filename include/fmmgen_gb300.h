@@ -230,16 +230,21 @@ int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, double *L);
  * and evaluate ([P2M, M2M, M2L, P2P, L2L, L2P, finalize, total]) in ms. */
 int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8);
 /* Work of the last tensor-core M2L (no counterpart in the reference; for
- * roofline accounting), host out3 = [class steps of 128-row tiles, tcgen05 MMA
- * instructions, executed tensor flops]; zeros if none ran. */
-int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out3);
+ * roofline accounting), host out4 = [class steps of 128-row tiles, tcgen05 MMA
+ * instructions, executed tensor flops, 1 if its source rows were boxed from
+ * level grids (else gathered row by row)]; zeros if none ran. */
+int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out4);
 
 /* ---- M2L choices and their autotuner (no counterpart in the reference) ----
- * impl: -1 the default rules (tensor cores for "mixed" where p <= 9, else the
- * generated CUDA-core kernels where the order has them, else the warp
- * contraction engine), 0 tensor cores, 1 generated CUDA-core kernels,
- * 2 contraction engine (mixed passes; FP64 passes always use the engine).
- * nslots: tensor-core pipeline depth (row-gather slots), 0 = as many as fit.
+ * impl: -1 the default rules (tensor cores for "mixed" where p <= 9 -- as
+ * impl 3 --, else the generated CUDA-core kernels where the order has them,
+ * else the warp contraction engine), 0 tensor cores with the source rows
+ * gathered row by row, 1 generated CUDA-core kernels, 2 contraction engine,
+ * 3 tensor cores with the source rows boxed from dense level grids by
+ * tensor-map copies where every level of the tree is complete (one system,
+ * all 8^l cells of every level), else as 0 (mixed passes; FP64 passes always
+ * use the engine).
+ * nslots: tensor-core pipeline depth (operand slots), 0 = as many as fit.
  * grouping: order of a level's cells in M2L tiles and warps, 0 by octant
  * within the parent, 1 Morton.  overlap: 1 (2) runs the tensor-core M2L on a
  * highest-priority side stream with the P2P beside it on the same SMs, in
