@@ -172,41 +172,159 @@ __device__ __forceinline__ void dipole_one(const float4 &q, const float4 &ql, co
   ez += d.z * r3 - r5 * dz;
 }
 
-// Sources first, first + step, ... < cnt of the staged chunk.  A full chunk
-// with one lane per target (the common case) runs with constant shared-memory
-// offsets, so nothing but the interaction itself sits in the loop body.
+// ---- two sources per instruction (packed FP32x2) ----
+// A full chunk with one lane per target (the common case) runs two sources at a
+// time through add/sub/mul/fma.rn.f32x2: the same operations, in the same
+// precision, as coulomb_one / dipole_one for each source of the pair, with half
+// the instructions (the kernel is issue-bound).  Staged chunks are laid out for
+// this: pair k of sources (2k, 2k+1) is four 16-byte words
+//   X[k] = (xh, xh', yh, yh'), Z[k] = (zh, zh', q, q'),
+//   XL[k] = (xl, xl', yl, yl'), ZL[k] = (zl, zl', index, index'),
+// and for dipoles D[k] = (mx, mx', my, my'), DZ[k] = (mz, mz', -, -)
+// (primes: source 2k + 1).
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 padd(u64 a, u64 b) {
+  u64 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 psub(u64 a, u64 b) {
+  u64 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 pmul(u64 a, u64 b) {
+  u64 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 pfma(u64 a, u64 b, u64 c) {
+  u64 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ u64 pk2(float a, float b) {
+  return ((u64)__float_as_uint(b) << 32) | (u64)__float_as_uint(a);
+}
+__device__ __forceinline__ float plo(u64 v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float phi_(u64 v) { return __uint_as_float((unsigned)(v >> 32)); }
+
+// staged chunk of one warp (32 sources)
+struct P2PStage {
+  ulonglong2 X[16], Z[16], XL[16], ZL[16];
+};
+struct P2PStageD {
+  ulonglong2 D[16], DZ[16];
+};
+__device__ __forceinline__ float *sf(ulonglong2 *a) { return (float *)a; }
+__device__ __forceinline__ const float *sf(const ulonglong2 *a) { return (const float *)a; }
+
+// the target's coordinates (hi, lo) duplicated into both halves
+struct P2PTgt {
+  u64 xh, xl, yh, yl, zh, zl;
+};
+
+template <bool SELF, bool POT>
+__device__ __forceinline__ void coulomb_two(const P2PStage &sg, int k, int i, const P2PTgt &t, u64 &phi, u64 &ex,
+                                            u64 &ey, u64 &ez) {
+  const ulonglong2 X = sg.X[k], Z = sg.Z[k], XL = sg.XL[k], ZL = sg.ZL[k];
+  const u64 dx = padd(psub(t.xh, X.x), psub(t.xl, XL.x));
+  const u64 dy = padd(psub(t.yh, X.y), psub(t.yl, XL.y));
+  const u64 dz = padd(psub(t.zh, Z.x), psub(t.zl, ZL.x));
+  const u64 r2 = pfma(dx, dx, pfma(dy, dy, pmul(dz, dz)));
+  float ra = rsqrt_approx(plo(r2)), rb = rsqrt_approx(phi_(r2));
+  if (SELF) {  // l2 != l1
+    ra = (int)(unsigned)ZL.y == i ? 0.f : ra;
+    rb = (int)(unsigned)(ZL.y >> 32) == i ? 0.f : rb;
+  }
+  const u64 rinv = pk2(ra, rb);
+  const u64 qr = pmul(Z.y, rinv);
+  const u64 qr3 = pmul(qr, pmul(rinv, rinv));
+  if (POT) phi = padd(phi, qr);
+  ex = pfma(qr3, dx, ex);
+  ey = pfma(qr3, dy, ey);
+  ez = pfma(qr3, dz, ez);
+}
+
+template <bool SELF>
+__device__ __forceinline__ void dipole_two(const P2PStage &sg, const P2PStageD &sd, int k, int i, const P2PTgt &t,
+                                           u64 &phi, u64 &ex, u64 &ey, u64 &ez) {
+  const ulonglong2 X = sg.X[k], Z = sg.Z[k], XL = sg.XL[k], ZL = sg.ZL[k], D = sd.D[k];
+  const u64 mz = sd.DZ[k].x;
+  const u64 dx = padd(psub(t.xh, X.x), psub(t.xl, XL.x));
+  const u64 dy = padd(psub(t.yh, X.y), psub(t.yl, XL.y));
+  const u64 dz = padd(psub(t.zh, Z.x), psub(t.zl, ZL.x));
+  const u64 r2 = pfma(dx, dx, pfma(dy, dy, pmul(dz, dz)));
+  float ra = rsqrt_approx(plo(r2)), rb = rsqrt_approx(phi_(r2));
+  if (SELF) {
+    ra = (int)(unsigned)ZL.y == i ? 0.f : ra;
+    rb = (int)(unsigned)(ZL.y >> 32) == i ? 0.f : rb;
+  }
+  const u64 rinv = pk2(ra, rb);
+  const u64 rr = pmul(rinv, rinv);
+  const u64 r3 = pmul(rr, rinv);
+  const u64 sr = pfma(D.x, dx, pfma(D.y, dy, pmul(mz, dz)));
+  const u64 r5 = pmul(pmul(pmul(pk2(3.f, 3.f), sr), r3), rr);
+  phi = psub(phi, pmul(sr, r3));
+  ex = padd(ex, psub(pmul(D.x, r3), pmul(r5, dx)));
+  ey = padd(ey, psub(pmul(D.y, r3), pmul(r5, dy)));
+  ez = padd(ez, psub(pmul(mz, r3), pmul(r5, dz)));
+}
+
+// one source of the packed layout, for partial chunks
+__device__ __forceinline__ void stage_get(const P2PStage &sg, int j, float4 &h, float4 &l) {
+  const int o = 4 * (j >> 1) + (j & 1);
+  const float *x = sf(sg.X) + o, *z = sf(sg.Z) + o, *xl = sf(sg.XL) + o, *zl = sf(sg.ZL) + o;
+  h = make_float4(x[0], x[2], z[0], z[2]);
+  l = make_float4(xl[0], xl[2], zl[0], zl[2]);
+}
+__device__ __forceinline__ float4 stage_getd(const P2PStageD &sd, int j) {
+  const int o = 4 * (j >> 1) + (j & 1);
+  const float *d = sf(sd.D) + o, *dz = sf(sd.DZ) + o;
+  return make_float4(d[0], d[2], dz[0], 0.f);
+}
+
+// Sources first, first + step, ... < cnt of the staged chunk.
 template <bool SELF, bool POT, int SO>
-__device__ __forceinline__ void p2p_chunk(const float4 *sh, const float4 *sl, const float4 *sd, int first, int cnt,
-                                          int step, int i, float txh, float txl, float tyh, float tyl, float tzh,
-                                          float tzl, float &phi, float &ex, float &ey, float &ez) {
+__device__ __forceinline__ void p2p_chunk(const P2PStage &sg, const P2PStageD &sd, int first, int cnt, int step,
+                                          int i, const P2PTgt &t, float txh, float txl, float tyh, float tyl,
+                                          float tzh, float tzl, float &phi, float &ex, float &ey, float &ez) {
   if (step == 1 && cnt == 32) {
-#pragma unroll 8
-    for (int jj = 0; jj < 32; jj++) {
+    u64 p2 = 0, x2 = 0, y2 = 0, z2 = 0;
+#pragma unroll 4
+    for (int k = 0; k < 16; k++) {
       if (SO == 0)
-        coulomb_one<SELF, POT>(sh[jj], sl[jj], i, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+        coulomb_two<SELF, POT>(sg, k, i, t, p2, x2, y2, z2);
       else
-        dipole_one<SELF>(sh[jj], sl[jj], sd[jj], i, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+        dipole_two<SELF>(sg, sd, k, i, t, p2, x2, y2, z2);
     }
+    if (POT || SO) phi += plo(p2) + phi_(p2);
+    ex += plo(x2) + phi_(x2);
+    ey += plo(y2) + phi_(y2);
+    ez += plo(z2) + phi_(z2);
     return;
   }
 #pragma unroll 4
   for (int jj = first; jj < cnt; jj += step) {
+    float4 h, l;
+    stage_get(sg, jj, h, l);
     if (SO == 0)
-      coulomb_one<SELF, POT>(sh[jj], sl[jj], i, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+      coulomb_one<SELF, POT>(h, l, i, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
     else
-      dipole_one<SELF>(sh[jj], sl[jj], sd[jj], i, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
+      dipole_one<SELF>(h, l, stage_getd(sd, jj), i, txh, txl, tyh, tyl, tzh, tzl, phi, ex, ey, ez);
   }
 }
 
-// The near field of target leaf A by one warp (sh, sl, sd: its staging rows).
+// The near field of target leaf A by one warp (sg, sd: its staging area).
 template <bool POT, int SO>
 __device__ __forceinline__ void p2p_leaf(int A, const int *pstart, const int *pcount, const int *off_,
                                          const int *src, const float4 *phi4, const float4 *plo4,
-                                         const float4 *sdip, float4 *shw, float4 *slw, float4 *sdw, double *Fnear) {
+                                         const float4 *sdip, P2PStage &sg, P2PStageD &sd, double *Fnear) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int a0 = pstart[A], na = pcount[A];
   const int k0 = off_[A], k1 = off_[A + 1];
+  const int sk = 4 * (lane >> 1) + (lane & 1);  // this lane's slot when it stages source `lane` of a chunk
   for (int tb = 0; tb < na; tb += 32) {
     const int m = min(32, na - tb);
     int lf = 0;  // f = 2^lf lanes per target
@@ -216,6 +334,8 @@ __device__ __forceinline__ void p2p_leaf(int A, const int *pstart, const int *pc
     const bool ok = tl < m;
     const int i = a0 + tb + (ok ? tl : 0);
     const float4 th = phi4[i], tlo = plo4[i];
+    const P2PTgt tg = {pk2(th.x, th.x), pk2(tlo.x, tlo.x), pk2(th.y, th.y),
+                       pk2(tlo.y, tlo.y), pk2(th.z, th.z), pk2(tlo.z, tlo.z)};
     float s0 = 0, s1 = 0, s2 = 0, s3 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
     for (int kb = k0; kb < k1; kb += 32) {
       // up to 32 source leaves: lane q holds leaf kb + q's particle range and
@@ -252,20 +372,27 @@ __device__ __forceinline__ void p2p_leaf(int A, const int *pstart, const int *pc
         __syncwarp();
         if (s < total) {
           const int j = jb + (s - je);
-          shw[lane] = phi4[j];
-          slw[lane] = plo4[j];
-          if (SO) sdw[lane] = sdip[j];
+          const float4 h = phi4[j], l = plo4[j];
+          sf(sg.X)[sk] = h.x; sf(sg.X)[sk + 2] = h.y;
+          sf(sg.Z)[sk] = h.z; sf(sg.Z)[sk + 2] = h.w;
+          sf(sg.XL)[sk] = l.x; sf(sg.XL)[sk + 2] = l.y;
+          sf(sg.ZL)[sk] = l.z; sf(sg.ZL)[sk + 2] = l.w;
+          if (SO) {
+            const float4 d = sdip[j];
+            sf(sd.D)[sk] = d.x; sf(sd.D)[sk + 2] = d.y;
+            sf(sd.DZ)[sk] = d.z;
+          }
         }
         __syncwarp();
         const int n = min(32, total - cb);
         const bool self = self_lo >= 0 && self_lo < cb + n && self_lo + na > cb;
         float phi = 0, ex = 0, ey = 0, ez = 0;
         if (self)
-          p2p_chunk<true, POT, SO>(shw, slw, sdw, slice, n, f, i, th.x, tlo.x, th.y, tlo.y, th.z, tlo.z, phi, ex, ey,
+          p2p_chunk<true, POT, SO>(sg, sd, slice, n, f, i, tg, th.x, tlo.x, th.y, tlo.y, th.z, tlo.z, phi, ex, ey,
                                    ez);
         else
-          p2p_chunk<false, POT, SO>(shw, slw, sdw, slice, n, f, i, th.x, tlo.x, th.y, tlo.y, th.z, tlo.z, phi, ex,
-                                    ey, ez);
+          p2p_chunk<false, POT, SO>(sg, sd, slice, n, f, i, tg, th.x, tlo.x, th.y, tlo.y, th.z, tlo.z, phi, ex, ey,
+                                    ez);
         if (POT) kahan_add(s0, c0, phi);
         kahan_add(s1, c1, ex); kahan_add(s2, c2, ey); kahan_add(s3, c3, ez);
       }
@@ -293,11 +420,12 @@ __global__ void __launch_bounds__(32 * WARPS) k_p2p32(const int *leaf_cells, int
                                                       const int *pcount, const int *off_, const int *src,
                                                       const float4 *phi4, const float4 *plo4, const float4 *sdip,
                                                       double *Fnear) {
-  __shared__ float4 sh[WARPS][32], sl[WARPS][32], sd[WARPS][SO ? 32 : 1];
+  __shared__ P2PStage sg[WARPS];
+  __shared__ P2PStageD sd[SO ? WARPS : 1];
   const int w = threadIdx.x >> 5;
   const int leaf = blockIdx.x * WARPS + w;
   if (leaf < nleaves)
-    p2p_leaf<POT, SO>(leaf_cells[leaf], pstart, pcount, off_, src, phi4, plo4, sdip, sh[w], sl[w], sd[w], Fnear);
+    p2p_leaf<POT, SO>(leaf_cells[leaf], pstart, pcount, off_, src, phi4, plo4, sdip, sg[w], sd[SO ? w : 0], Fnear);
 }
 
 // ---------------------------------------------------------------------------
