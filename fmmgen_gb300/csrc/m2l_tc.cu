@@ -118,7 +118,7 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   for (uint32_t i = 0; i < TC_WAIT_LIMIT; i++) {
     if (mbar_try(bar, parity)) return true;
-    if (i >= 256) __nanosleep(32);
+    if (i >= 32) __nanosleep(128);
   }
   return false;
 }
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
 // tensor copies and the operator chunks), lane 1 of warp 0 the column scales
 // of every step in order; 4-11 fold; 12 allocates tensor memory and issues
 // MMAs.  Every slot and every barrier has one waiter that moves through its
-// phases in order.
+// phases in order, and every role walks the tile schedule itself.
 constexpr int TCG_MAXLEV = 8;                      // levels 0..7
 constexpr int TCG_PWARPS = 4;                      // producer warps 0-3
 constexpr int TCG_MWARP = TCG_PWARPS + TC_FWARPS;  // warp 12
@@ -710,7 +710,6 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) k_m2l_tcg(const __grid_constan
             const uint32_t use = g / (uint32_t)P.nslots;
             if (!mbar_wait(empty0 + 8 * slot, (use & 1) ^ 1)) { ok = false; break; }
             const uint32_t sa = base + (uint32_t)slot * P.slot_bytes, fb = full0 + 8 * slot;
-            cs->hdr[slot] = kb;
             const unsigned char *rec = P.T + (size_t)c * P.cls_bytes;
             const uint32_t b0 = P.choff[4 * kb], b1 = P.choff[min(4 * kb + 4, P.kch)];
             mbar_arrive_tx(fb, 2u * TC_A_BYTES + (b1 - b0));
@@ -718,17 +717,6 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) k_m2l_tcg(const __grid_constan
             tma_box5(sa + TC_A_BYTES, map, x0, y0, z0, pl0 + 2 * kb + 1, fb);
             bulk_g2s(sa + 2 * TC_A_BYTES, rec + b0, b1 - b0, fb);
           }
-        }
-      }
-      // end of work: one more slot carrying only the end mark
-      if (ok && (int)(g % (uint32_t)P.nslots) == warp) {
-        const int slot = warp;
-        const uint32_t use = g / (uint32_t)P.nslots;
-        if (mbar_wait(empty0 + 8 * slot, (use & 1) ^ 1)) {
-          cs->hdr[slot] = -1;
-          mbar_arrive(full0 + 8 * slot);
-        } else {
-          ok = false;
         }
       }
       if (!ok) atomicOr(P.err, 1u);
@@ -797,15 +785,18 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) k_m2l_tcg(const __grid_constan
       bor[ch] = cs->ch_boff[ch];
       nlr[ch] = cs->ch_nlo[ch];
     }
+    // the thread walks the schedule itself (a shared-memory load issued behind
+    // MMAs that are still reading their operands waits for them)
     const int kch = P.kch;
     uint32_t g = 0, u = 0;
     bool ok = true;
-    while (true) {
+    for (int tile = blockIdx.x; tile < P.ntiles && ok; tile += gridDim.x) {
+    const int nst = P.sched_off[tile + 1] - P.sched_off[tile];
+    for (int st = 0; st < nst && ok; st++) {
+    for (int kb = 0; kb < P.nkb; kb++) {
       const int slot = (int)(g % (uint32_t)P.nslots);
       if (!mbar_wait(full0 + 8 * slot, (g / (uint32_t)P.nslots) & 1)) { ok = false; break; }
       tc_fence_after();
-      const int kb = cs->hdr[slot];
-      if (kb < 0) break;
       const uint32_t b = u & 1;
       if (kb == 0) {
         if (!mbar_wait(accempty0 + 8 * b, ((u >> 1) & 1) ^ 1)) { ok = false; break; }
@@ -842,6 +833,8 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) k_m2l_tcg(const __grid_constan
         u++;
       }
       g++;
+    }
+    }
     }
     mma_commit(drain);
     if (!mbar_wait(drain, 0)) ok = false;
