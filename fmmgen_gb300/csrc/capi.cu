@@ -522,7 +522,7 @@ extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out4) {
   long long mmas = 0;
   double flops = 0;
   unsigned long long steps = 0;
-  if (t.h_pinned && fmm_m2l_tc_step_work(t.order, t.so, &mmas, &flops))
+  if (t.h_pinned && fmm_m2l_tc_step_work(t.order, t.so, t.tc_boxes_last != 0, &mmas, &flops))
     memcpy(&steps, t.h_pinned + FMM_PINNED_TCERR + 2, sizeof(steps));
   out3[0] = (double)steps;
   out3[1] = (double)steps * (double)mmas;

@@ -196,7 +196,7 @@ int fmm_mlp_train_step(const float *params, const float *X, const unsigned char 
                        float *work, cudaStream_t st);
 int fmm_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, cudaStream_t st);
 int fmm_learned_orders(DevTree *t, cudaStream_t st);
-bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops);
+bool fmm_m2l_tc_step_work(int p, int so, bool boxes, long long *mmas, double *flops);
 // boxes: source rows by tensor-map box loads from level grids where every level is complete
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st, bool boxes);
 void fmm_tcg_release(DevTree *t);

@@ -543,6 +543,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const TcParams P) {
 // the fold through a per-step row mask.  The operand scale is one power of
 // two per level (the largest |M~| of the level brought to [2^14, 2^15)), so
 // no per-row scale travels with the rows.
+// Each K chunk's three products are issued as hi x lo, hi x hi, lo x hi, so
+// that consecutive MMAs share an operand; a chunk whose multipole terms all
+// have degree >= TCG_SPLIT_DEG issues hi x hi alone: its part of a local
+// expansion is below (sqrt(3) s / R)^6 ~ 2e-4 of the whole at theta = 0.5, so
+// the two dropped corrections (2^-11 of it) stay near 1e-7 relative, far
+// below the expansion's truncation error (the operand fetch of these narrow
+// MMAs, not their arithmetic, sets the kernel's pace).
 // Warps: lane 0 of warp w < nslots (0-3) issues the fills of slot w (two
 // tensor copies and the operator chunks), lane 1 of warp 0 the column scales
 // of every step in order; 4-11 fold; 12 allocates tensor memory and issues
@@ -552,6 +559,7 @@ constexpr int TCG_MAXLEV = 8;                      // levels 0..7
 constexpr int TCG_PWARPS = 4;                      // producer warps 0-3
 constexpr int TCG_MWARP = TCG_PWARPS + TC_FWARPS;  // warp 12
 constexpr int TCG_THREADS = 32 * (TCG_MWARP + 1);
+constexpr int TCG_SPLIT_DEG = 6;                   // chunks of higher degrees: one product
 static_assert(TC_MAXSLOTS <= TCG_PWARPS, "one producer warp per slot");
 
 struct TcgMaps {
@@ -571,6 +579,7 @@ struct TcgParams {
   const unsigned char *T;
   float *L;
   int lstride, lsize, kch, nkb, nslots, cls_bytes, cls_scale, slot_bytes, nout;
+  int nfull;                  // leading K chunks with all three products (the rest: hi x hi only)
   int nch[TC_MAXCH];
   int choff[TC_MAXCH + 1];
   uint32_t *err;              // as TcParams::err
@@ -787,7 +796,7 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) k_m2l_tcg(const __grid_constan
     }
     // the thread walks the schedule itself (a shared-memory load issued behind
     // MMAs that are still reading their operands waits for them)
-    const int kch = P.kch;
+    const int kch = P.kch, nfull = P.nfull;
     uint32_t g = 0, u = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < P.ntiles && ok; tile += gridDim.x) {
@@ -810,9 +819,13 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) k_m2l_tcg(const __grid_constan
   if (4 * (KB) + (J) < kch) {                                                           \
     const uint64_t bh = b0 + bor[4 * (KB) + (J)], bl = bh + nlr[4 * (KB) + (J)];        \
     const uint64_t ah = ah0 + 2 * (J), al = al0 + 2 * (J); /* 32 bytes along the row */ \
-    mma_f16(d, ah, bh, idr[4 * (KB) + (J)], ((KB) == 0 && (J) == 0) ? 0u : 1u);         \
-    mma_f16(d, ah, bl, idr[4 * (KB) + (J)], 1u);                                        \
-    mma_f16(d, al, bh, idr[4 * (KB) + (J)], 1u);                                        \
+    if (4 * (KB) + (J) < nfull) {                                                       \
+      mma_f16(d, ah, bl, idr[4 * (KB) + (J)], ((KB) == 0 && (J) == 0) ? 0u : 1u);       \
+      mma_f16(d, ah, bh, idr[4 * (KB) + (J)], 1u);                                      \
+      mma_f16(d, al, bh, idr[4 * (KB) + (J)], 1u);                                      \
+    } else {                                                                            \
+      mma_f16(d, ah, bh, idr[4 * (KB) + (J)], 1u);                                      \
+    }                                                                                   \
   }
 #define TC_KBLOCK(KB) \
   TC_CHUNK(KB, 0)     \
@@ -1369,6 +1382,14 @@ int tcg_prepare(DevTree *t, const TcPlan &pl, cudaStream_t st) {
   return FMM_OK;
 }
 
+// leading K chunks whose lowest multipole degree is below TCG_SPLIT_DEG (all three products)
+int tcg_full_chunks(const TcPlan &pl) {
+  const int moff = fmm_nterms(pl.so - 1);
+  int n = 0;
+  while (n < pl.kch && fmm_decode(moff + TC_CH * n).d < TCG_SPLIT_DEG) n++;
+  return n;
+}
+
 template <int NOUT> int tcg_launch(const TcgMaps &maps, const TcgParams &P, int smem, int grid, cudaStream_t st) {
   FMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l_tcg<NOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   fmm_note_launch(), k_m2l_tcg<NOUT><<<grid, TCG_THREADS, smem, st>>>(maps, P);
@@ -1416,6 +1437,7 @@ int tcg_run(DevTree *t, const TcPlan &pl, const float *M, int mstr, float *L, in
   P.cls_scale = pl.cls_scale;
   P.slot_bytes = pl.slot_bytes;
   P.nout = pl.nout;
+  P.nfull = tcg_full_chunks(pl);
   for (int k = 0; k < TC_MAXCH; k++) P.nch[k] = k < pl.kch ? pl.nch[k] : 0;
   for (int k = 0; k <= TC_MAXCH; k++) P.choff[k] = k <= pl.kch ? pl.choff[k] : pl.cls_scale;
   P.err = t->d_tcerr.p;
@@ -1471,14 +1493,22 @@ int fmm_m2l_tc_max_slots(int p, int so) {
 }
 
 // Executed tensor work of one class step of a 128-row tile: MMA instructions
-// and flops (3 products per K chunk, each 2 x 128 x 16 x N).
-bool fmm_m2l_tc_step_work(int p, int so, long long *mmas, double *flops) {
+// and flops (each 2 x 128 x 16 x N): 3 products per K chunk in the row-gather
+// kernel; in the level-grid kernel (boxes) 3 for the leading chunks, 1 for
+// the chunks of degree TCG_SPLIT_DEG and up.
+bool fmm_m2l_tc_step_work(int p, int so, bool boxes, long long *mmas, double *flops) {
   TcPlan pl;
   if (!tc_plan(p, so, pl)) return false;
-  long long n = 0;
-  for (int k = 0; k < pl.kch; k++) n += pl.nch[k];
-  *mmas = 3LL * pl.kch;
-  *flops = 3.0 * 2.0 * TC_ROWS * TC_CH * (double)n;
+  const int nfull = boxes ? tcg_full_chunks(pl) : pl.kch;
+  long long m = 0;
+  double n = 0;
+  for (int k = 0; k < pl.kch; k++) {
+    const int prod = k < nfull ? 3 : 1;
+    m += prod;
+    n += (double)prod * pl.nch[k];
+  }
+  *mmas = m;
+  *flops = 2.0 * TC_ROWS * TC_CH * n;
   return true;
 }
 
