@@ -528,18 +528,23 @@ def main():
     cand = {"P2P": (ph.get("P2P", 0.0), p2p_flops), "M2L": (ph.get("M2L", 0.0), m2l_flops)}
     dom = max(cand, key=lambda k: cand[k][0])
     dom_ms, dom_flops = cand[dom]
-    traffic = None
+    traffic, traffic_current = None, None
     if a.config == "uniform_1m_p8" and a.n == 1_000_000:  # the workload the ncu capture ran
         try:
+            import hashlib
+
             for ln in open(os.path.join(ROOT, "profiles", "dram_traffic_uniform_1m_p8.txt")):
                 f = ln.split()
-                if len(f) == 2 and not ln.startswith("#") and f[0] == dom:
+                if len(f) == 4 and not ln.startswith("#") and f[0] == dom:
                     traffic = float(f[1])
+                    # the capture describes the kernel only while its source is unchanged
+                    with open(os.path.join(ROOT, f[2]), "rb") as src:
+                        traffic_current = hashlib.sha256(src.read()).hexdigest()[:16] == f[3]
         except OSError:
             pass
     achieved = dom_flops / (dom_ms / 1e3) / 1e12 if dom_ms > 0 else 0.0
     roofline = {"kernel": dom, "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp32_peak, "traffic": traffic,
+                "frac": achieved / fp32_peak, "traffic": traffic, "traffic_capture_current": traffic_current,
                 "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json "
                                "(no measured FP32 figure exists)",
                 "work": f"{'20 flop x P2P interactions' if dom == 'P2P' else '2*C(p+6,6) flop x M2L pairs'} "
@@ -554,8 +559,10 @@ def main():
                     "algorithmic_frac": alg_tf / tpeak if tpeak else None,
                     "class_steps": m2l_steps, "mma_instructions": m2l_mmas,
                     "executed_flops_per_launch": m2l_exec_flops, "algorithmic_flops_per_launch": m2l_flops,
-                    "note": "executed = MMA flops issued (3 FP16 products per term, 128-row tiles over the union of "
-                            "the tile's classes, triangular N per 16-term chunk); algorithmic = 2*C(p+6,6) per pair; "
+                    "source_rows": "boxed from level grids (tensor-map copies)" if m2l_boxes else "gathered row by row",
+                    "note": "executed = MMA flops issued (3 FP16 products per 16-term chunk, 1 for the chunks of "
+                            "degree >= 6 in the level-grid kernel; 128-row tiles over the union of the tile's classes, "
+                            "triangular N per chunk); algorithmic = 2*C(p+6,6) per pair; "
                             "peak = measured bf16 dense (MEASURED_PEAKS.json)"}
 
     if dom == "M2L" and m2l_steps and tpeak:
@@ -565,6 +572,7 @@ def main():
         roofline_fp32 = roofline
         roofline = {"kernel": roofline_m2l["kernel"], "bound": "tensor", "achieved": alg_tf, "peak": tpeak,
                     "unit": "TFLOP/s", "frac": alg_tf / tpeak, "traffic": traffic,
+                    "traffic_capture_current": traffic_current,
                     "peak_source": "measured bf16 dense burst (MEASURED_PEAKS.json bf16_tflops)",
                     "work": roofline_fp32["work"], "executed_achieved": exec_tf, "executed_frac": exec_tf / tpeak,
                     "fp32_view": {k: roofline_fp32[k] for k in ("achieved", "peak", "frac", "peak_source")}}
