@@ -436,26 +436,28 @@ def main():
                               "gpu_launches": launches}), flush=True)
         return
 
-    # ---- e2e through the public API from pinned host memory ----
-    pos_h = torch.tensor(pos_np).pin_memory()
-    q_h = torch.tensor(q_np).pin_memory()
-    F_h = torch.empty((a.n, a.outsize), dtype=torch.float64).pin_memory()
-    pos_d = torch.empty_like(pos)
-    q_d = torch.empty_like(q)
+    # ---- e2e through the public API from pinned host memory: a stream of steps
+    # (fmmgen_gb300.stream_compute), every step copying its inputs in and its
+    # outputs out, the copies of one step overlapped with its neighbours' work ----
+    from fmmgen_gb300.pipeline import StepBuffers
 
-    def e2e_step():
-        pos_d.copy_(pos_h, non_blocking=True)
-        q_d.copy_(q_h, non_blocking=True)
-        tree.rebuild_compute(pos_d, F, S=q_d, potential=a.potential, field=a.field, precision="mixed")
-        F_h.copy_(F, non_blocking=True)
-
-    e2e_step()
     k_e2e = max(3, a.steps // 2)
-    e2e_ms, _ = timed(k_e2e, e2e_step)
+    pos_h = [torch.tensor(pos_np).pin_memory() for _ in range(2)]
+    q_h = [torch.tensor(q_np).pin_memory() for _ in range(2)]
+    F_h = [torch.empty((a.n, a.outsize), dtype=torch.float64).pin_memory() for _ in range(2)]
+    bufs = StepBuffers(a.n, q_np.shape[1], a.outsize, dev)
+    seq = lambda xs, k: [xs[i % 2] for i in range(k)]  # noqa: E731  (host arrays reused every other step)
+    fg.stream_compute(tree, seq(pos_h, 2), seq(q_h, 2), seq(F_h, 2), a.potential, a.field, "mixed", bufs)
+    flush.fill_(0.0)
+    barrier()
+    e2e_ms = fg.stream_compute(tree, seq(pos_h, k_e2e), seq(q_h, k_e2e), seq(F_h, k_e2e), a.potential, a.field,
+                               "mixed", bufs, timing=True)
+    barrier()
     e2e_max = max_over_ranks(e2e_ms, pg, dev)
     e2e_value = job_throughput(a.n, k_e2e, world, e2e_max)
-    h2d = pos_h.numel() * 8 + q_h.numel() * 8
-    d2h = F_h.numel() * 8
+    h2d = pos_h[0].numel() * 8 + q_h[0].numel() * 8
+    d2h = F_h[0].numel() * 8
+    del bufs
     tree.rebuild(pos)
     tree.S = q
 

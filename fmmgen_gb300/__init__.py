@@ -8,5 +8,7 @@ from ._lib import FMMError, lib  # noqa: F401
 from .tree import Tree, build_forest, build_tree, direct  # noqa: F401
 from . import operators  # noqa: F401
 from .demag import DemagFMM  # noqa: F401
+from .pipeline import stream_compute  # noqa: F401
 
-__all__ = ["Tree", "build_forest", "build_tree", "direct", "operators", "DemagFMM", "FMMError", "lib"]
+__all__ = ["Tree", "build_forest", "build_tree", "direct", "operators", "DemagFMM", "FMMError", "lib",
+           "stream_compute"]
