@@ -29,12 +29,17 @@ def _headers():
 
 
 def _generate():
-    """(Re)write csrc/m2l_gen.cuh when its generator is newer."""
-    from . import gen_m2l
+    """(Re)write the generated kernels (csrc/m2l_gen.cuh, csrc/m2l_cm*) when
+    their generator is newer."""
+    from . import gen_m2l, gen_m2l_cm
 
     out, src = gen_m2l.OUT, os.path.abspath(gen_m2l.__file__)
     if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
         gen_m2l.generate()
+    src = os.path.abspath(gen_m2l_cm.__file__)
+    outs = [os.path.join(CSRC, "m2l_cm.cuh")] + [os.path.join(CSRC, f"m2l_cm_s{so}.cu") for so, _ in gen_m2l_cm.FAMILIES]
+    if any(not os.path.exists(o) or os.path.getmtime(o) < os.path.getmtime(src) for o in outs):
+        gen_m2l_cm.generate()
 
 
 def build(verbose=False, ptxas_verbose=False):

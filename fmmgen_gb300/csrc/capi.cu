@@ -537,7 +537,7 @@ int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping, 
   g_err.clear();
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   DevTree &t = tree->t;
-  if (impl < -1 || impl > 3 || nslots < 0 || grouping < 0 || grouping > 1 || overlap < 0 || overlap > 2)
+  if (impl < -1 || impl > 5 || nslots < 0 || grouping < 0 || grouping > 1 || overlap < 0 || overlap > 2)
     return ret(FMM_ERR_ARG);
   if ((impl == 0 || impl == 3) && !fmm_m2l_tc_supported(t.order, t.so)) {
     fmm_set_error_text("the tensor-core M2L does not support this order / source order");
@@ -545,6 +545,10 @@ int fmmgen_tree_set_tune(fmmgen_tree *tree, int impl, int nslots, int grouping, 
   }
   if (impl == 1 && !fmm_m2l_gen_supported(t.order, t.so)) {
     fmm_set_error_text("no generated CUDA-core M2L kernels for this order / source order");
+    return ret(FMM_ERR_ARG);
+  }
+  if ((impl == 4 || impl == 5) && !fmm_m2l_cm_supported(t.order, t.so)) {
+    fmm_set_error_text("no class-major CUDA-core M2L kernels for this order / source order");
     return ret(FMM_ERR_ARG);
   }
   fmm_graph_release(&t);  // a recorded pass holds the old choice

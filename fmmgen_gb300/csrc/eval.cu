@@ -676,7 +676,7 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
 // every level is complete, else gathered row by row), else the generated
 // CUDA-core kernels where this order has them, else the warp contraction
 // engine; FP64: the engine.
-enum { M2L_TC = 0, M2L_GEN = 1, M2L_ENGINE = 2, M2L_TCG = 3 };
+enum { M2L_TC = 0, M2L_GEN = 1, M2L_ENGINE = 2, M2L_TCG = 3, M2L_CM = 4, M2L_TP = 5 };
 static inline bool is_tc(int impl) { return impl == M2L_TC || impl == M2L_TCG; }
 bool fmm_m2l_gen_supported(int p, int so) {
   m2l_reg_kernel kg[4];
@@ -689,6 +689,8 @@ static int m2l_impl(const DevTree *t, int precision) {
   int impl = t->tune.impl;
   if (impl < 0) impl = precision == 1 ? M2L_TCG : M2L_GEN;
   if (is_tc(impl) && (!tc_ok || t->nclasses > 262144)) impl = M2L_GEN;  // class bitmap of the tile schedule
+  if (impl == M2L_CM && (!fmm_m2l_cm_supported(t->order, t->so) || t->nclasses > 262144)) impl = M2L_GEN;
+  if (impl == M2L_TP && !fmm_m2l_cm_supported(t->order, t->so)) impl = M2L_GEN;
   if (impl == M2L_GEN && !gen_ok) impl = M2L_ENGINE;
   return impl;
 }
@@ -734,13 +736,22 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
                      int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so, nc = t->ncells;
   // every M2L but the tensor cores' reads the target lists
-  if (t->ord_mode != 0 || !(mixed && is_tc(impl))) TRY(fmm_m2l_csr(t, st));
+  if (t->ord_mode != 0 || !(mixed && (is_tc(impl) || impl == M2L_CM))) TRY(fmm_m2l_csr(t, st));
+  // a tuned choice pins the per-pair-order kernels: 2 the engine, 4 class-major, else target-major
+  const int timpl = t->tune.impl;
   if (t->ord_mode != 0) {
     // per-pair orders: predicted now from this pass's multipoles, or given
     if (t->ord_mode == 2) TRY(fmm_learned_orders(t, st));
     else if (t->ord_serial != t->build_serial) {
       fmm_set_error_text("per-pair M2L orders were set for an earlier build");
       return FMM_ERR_STATE;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+      // mixed: the generated kernels, each lane truncating at its pair's order
+      const int rc = timpl == M2L_ENGINE ? FMM_ERR_STATE
+                     : timpl == M2L_CM   ? fmm_m2l_cm(t, M, mstr, L, lstr, t->m2l_ord.p, st)
+                                         : fmm_m2l_tp(t, M, mstr, L, lstr, t->m2l_ord.p, st);
+      if (rc != FMM_ERR_STATE) return rc;
     }
     FMM_CUDA_TRY(cudaMemsetAsync(L, 0, sizeof(T) * (size_t)nc * lstr, st));
     for (int q = so + 1; q <= p; q++) {
@@ -758,6 +769,10 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
     }
   } else if (mixed && is_tc(impl)) {
     TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st, impl == M2L_TCG));
+  } else if (mixed && impl == M2L_CM) {
+    TRY(fmm_m2l_cm(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, nullptr, st));
+  } else if (mixed && impl == M2L_TP) {
+    TRY(fmm_m2l_tp(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, nullptr, st));
   } else if (mixed && impl == M2L_GEN) {
     m2l_reg_kernel kg[4];
     int kthreads[4];

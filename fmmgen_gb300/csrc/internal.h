@@ -114,6 +114,12 @@ struct DevTree {
   DevBuf<int> tc_sched_off;               // class-step schedule of the tensor-core M2L tiles
   DevBuf<unsigned> tc_sched_cls, tc_bitmap, tc_rank;
   DevBuf<int> tc_stab, tc_pos;            // per class step: each tile row's source (-1: none); row of each cell
+  int tc_nsteps = 0;                      // class steps of the schedule
+  DevBuf<unsigned char> cm_otab;          // per class step: each tile row's per-pair M2L order
+  DevBuf<int> cm_woff, cm_wstep;          // per (tile, warp of 32 rows): its steps with a pair
+  uint64_t cm_wserial = ~0ull, cm_wversion = ~0ull;  // ... of this schedule (build, cell order)
+  DevBuf<int> tp_perm;                    // per target list: pair indices by descending per-pair order
+  DevBuf<int> tp_tgt;                     // targets by level, then by their count of high-order pairs
   void *tcg = nullptr;                    // level-grid tensor-core M2L state (m2l_tc.cu, fmm_tcg_release)
   int tc_boxes_last = 0;                  // the last tensor-core M2L boxed its source rows from level grids
   uint64_t sched_serial = ~0ull, sched_version = ~0ull;  // ... of this build and cell order
@@ -200,6 +206,14 @@ bool fmm_m2l_tc_step_work(int p, int so, bool boxes, long long *mmas, double *fl
 // boxes: source rows by tensor-map box loads from level grids where every level is complete
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st, bool boxes);
 void fmm_tcg_release(DevTree *t);
+// the tiles' class-step schedule (tc_sched_off / tc_sched_cls / tc_stab), once per build and cell order
+int fmm_tc_schedule(DevTree *t, cudaStream_t st);
+// class-major generated CUDA-core M2L over that schedule (m2l_cm_s*.cu); ord: per-pair orders in target-list
+// order or null; FMM_ERR_STATE when no family covers (order, source order) or the schedule cannot be built
+int fmm_m2l_cm(DevTree *t, const float *M, int mstr, float *L, int lstr, const unsigned char *ord, cudaStream_t st);
+// the same kernel bodies, one thread per target cell over its target list (m2l_cm_s*.cu)
+int fmm_m2l_tp(DevTree *t, const float *M, int mstr, float *L, int lstr, const unsigned char *ord, cudaStream_t st);
+bool fmm_m2l_cm_supported(int p, int so);
 bool fmm_m2l_tc_boxes_ok(DevTree *t, cudaStream_t st);  // the level-grid path can run on this build
 // M2M of the parents / L2L into the children of cells [lo, hi), FP32 scaled expansions (shift.cu)
 int fmm_m2m_tab(DevTree *t, int lo, int hi, float *M, int mstr, cudaStream_t st);

@@ -1515,6 +1515,59 @@ bool fmm_m2l_tc_step_work(int p, int so, bool boxes, long long *mmas, double *fl
 // M2L of the mixed-precision pass on the tensor cores: reads the FP32 scaled
 // multipoles M (row stride mstr) and writes every cell's FP32 scaled local
 // expansion L (row stride lstr).
+// The class-step schedule of the tiles (tiles of TC_ROWS rows in M2L processing
+// order): once per build and cell order.  FMM_ERR_RANGE when the classes
+// exceed the bitmap's words.
+int fmm_tc_schedule(DevTree *t, cudaStream_t st) {
+  if (t->sched_serial == t->build_serial && t->sched_version == t->order_version) return FMM_OK;
+  const int nc = t->ncells;
+  const int ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
+  const int nwords = (t->nclasses + 31) / 32;
+  if (nwords > TC_SCHED_MAXW) return FMM_ERR_RANGE;
+  const size_t nbm = (size_t)ntiles * nwords;
+  if (fmm_reserve(t->tc_sched_off, ntiles + 1) || fmm_reserve(t->tc_pos, nc) || fmm_reserve(t->tc_bitmap, nbm) ||
+      fmm_reserve(t->tc_rank, nbm) || fmm_reserve(t->tmp, sizeof(int) * (ntiles + 1 + fmm_scan_tmp_elems<int>(ntiles))))
+    return FMM_ERR_CUDA;
+  int *cnt = (int *)t->tmp.p, *stmp = cnt + ntiles + 1;
+  const long n = t->nm2l;
+  fmm_note_launch(), k_tc_pos<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->m2l_order.p, nc, t->tc_pos.p);
+  const int nparts = 2 * tc_sm_count();
+  if (nbm * sizeof(unsigned) <= 160 * 1024 && n >= 64L * nparts) {
+    const int sbytes = (int)(nbm * sizeof(unsigned));
+    if (fmm_reserve(t->tc_stab, (size_t)nparts * nbm)) return FMM_ERR_CUDA;  // scratch until the table
+    if (sbytes > 48 * 1024)
+      FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_bitmap_part, cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes));
+    unsigned *part = (unsigned *)t->tc_stab.p;
+    fmm_note_launch(), k_tc_bitmap_part<<<nparts, 512, sbytes, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
+                                                                      t->tc_pos.p, nwords, (int)nbm, part);
+    fmm_note_launch(), k_tc_bitmap_or<<<fmm_blocks(nbm, 256), 256, 0, st>>>(part, nparts, (int)nbm,
+                                                                            t->tc_bitmap.p);
+  } else {
+    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_bitmap.p, 0, sizeof(unsigned) * nbm, st));
+    fmm_note_launch(), k_tc_bitmap<<<fmm_blocks(n, 256), 256, 0, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
+                                                                        t->tc_pos.p, nwords, t->tc_bitmap.p);
+  }
+  fmm_note_launch(), k_tc_rank<<<ntiles, 256, 0, st>>>(t->tc_bitmap.p, nwords, t->tc_rank.p, cnt);
+  if (int rc = fmm_scan<int>(cnt, t->tc_sched_off.p, ntiles, t->tc_sched_off.p + ntiles, stmp, st)) return rc;
+  FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_SCRATCH, t->tc_sched_off.p + ntiles, sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+  FMM_CUDA_TRY(cudaStreamSynchronize(st));
+  const int nsteps = (int)t->h_pinned[FMM_PINNED_SCRATCH];
+  const size_t ntab = (size_t)(nsteps > 0 ? nsteps : 1) * TC_ROWS;
+  if (fmm_reserve(t->tc_sched_cls, nsteps > 0 ? nsteps : 1) || fmm_reserve(t->tc_stab, ntab)) return FMM_ERR_CUDA;
+  fmm_note_launch(), k_tc_steps<<<ntiles, 128, 0, st>>>(t->tc_bitmap.p, t->tc_rank.p, nwords, t->tc_sched_off.p,
+                                                        t->tc_sched_cls.p);
+  FMM_CUDA_TRY(cudaMemsetAsync(t->tc_stab.p, 0xff, sizeof(int) * ntab, st));
+  fmm_note_launch(), k_tc_scatter<<<fmm_blocks(n, 256), 256, 0, st>>>(
+      t->m2l_tgt_raw.p, t->m2l_src_raw.p, t->m2l_cls_raw.p, n, t->tc_pos.p, t->tc_bitmap.p, t->tc_rank.p, nwords,
+      t->tc_sched_off.p, t->tc_stab.p);
+  FMM_CUDA_TRY(cudaGetLastError());
+  t->sched_serial = t->build_serial;
+  t->sched_version = t->order_version;
+  t->tc_nsteps = nsteps;
+  return FMM_OK;
+}
+
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st, bool boxes) {
   TcPlan pl;
   if (!tc_plan(t->order, t->so, pl)) return FMM_ERR_ARG;
@@ -1548,50 +1601,7 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   }
   // class-step schedule of the tiles: once per build and cell order
   const int ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
-  if (t->sched_serial != t->build_serial || t->sched_version != t->order_version) {
-    const int nwords = (t->nclasses + 31) / 32;
-    if (nwords > TC_SCHED_MAXW) return FMM_ERR_RANGE;
-    const size_t nbm = (size_t)ntiles * nwords;
-    if (fmm_reserve(t->tc_sched_off, ntiles + 1) || fmm_reserve(t->tc_pos, nc) || fmm_reserve(t->tc_bitmap, nbm) ||
-        fmm_reserve(t->tc_rank, nbm) || fmm_reserve(t->tmp, sizeof(int) * (ntiles + 1 + fmm_scan_tmp_elems<int>(ntiles))))
-      return FMM_ERR_CUDA;
-    int *cnt = (int *)t->tmp.p, *stmp = cnt + ntiles + 1;
-    const long n = t->nm2l;
-    fmm_note_launch(), k_tc_pos<<<fmm_blocks(nc, 256), 256, 0, st>>>(t->m2l_order.p, nc, t->tc_pos.p);
-    const int nparts = 2 * tc_sm_count();
-    if (nbm * sizeof(unsigned) <= 160 * 1024 && n >= 64L * nparts) {
-      const int sbytes = (int)(nbm * sizeof(unsigned));
-      if (fmm_reserve(t->tc_stab, (size_t)nparts * nbm)) return FMM_ERR_CUDA;  // scratch until the table
-      if (sbytes > 48 * 1024)
-        FMM_CUDA_TRY(cudaFuncSetAttribute(k_tc_bitmap_part, cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes));
-      unsigned *part = (unsigned *)t->tc_stab.p;
-      fmm_note_launch(), k_tc_bitmap_part<<<nparts, 512, sbytes, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
-                                                                        t->tc_pos.p, nwords, (int)nbm, part);
-      fmm_note_launch(), k_tc_bitmap_or<<<fmm_blocks(nbm, 256), 256, 0, st>>>(part, nparts, (int)nbm,
-                                                                              t->tc_bitmap.p);
-    } else {
-      FMM_CUDA_TRY(cudaMemsetAsync(t->tc_bitmap.p, 0, sizeof(unsigned) * nbm, st));
-      fmm_note_launch(), k_tc_bitmap<<<fmm_blocks(n, 256), 256, 0, st>>>(t->m2l_tgt_raw.p, t->m2l_cls_raw.p, n,
-                                                                          t->tc_pos.p, nwords, t->tc_bitmap.p);
-    }
-    fmm_note_launch(), k_tc_rank<<<ntiles, 256, 0, st>>>(t->tc_bitmap.p, nwords, t->tc_rank.p, cnt);
-    if (int rc = fmm_scan<int>(cnt, t->tc_sched_off.p, ntiles, t->tc_sched_off.p + ntiles, stmp, st)) return rc;
-    FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_SCRATCH, t->tc_sched_off.p + ntiles, sizeof(int),
-                                 cudaMemcpyDeviceToHost, st));
-    FMM_CUDA_TRY(cudaStreamSynchronize(st));
-    const int nsteps = (int)t->h_pinned[FMM_PINNED_SCRATCH];
-    const size_t ntab = (size_t)(nsteps > 0 ? nsteps : 1) * TC_ROWS;
-    if (fmm_reserve(t->tc_sched_cls, nsteps > 0 ? nsteps : 1) || fmm_reserve(t->tc_stab, ntab)) return FMM_ERR_CUDA;
-    fmm_note_launch(), k_tc_steps<<<ntiles, 128, 0, st>>>(t->tc_bitmap.p, t->tc_rank.p, nwords, t->tc_sched_off.p,
-                                                          t->tc_sched_cls.p);
-    FMM_CUDA_TRY(cudaMemsetAsync(t->tc_stab.p, 0xff, sizeof(int) * ntab, st));
-    fmm_note_launch(), k_tc_scatter<<<fmm_blocks(n, 256), 256, 0, st>>>(
-        t->m2l_tgt_raw.p, t->m2l_src_raw.p, t->m2l_cls_raw.p, n, t->tc_pos.p, t->tc_bitmap.p, t->tc_rank.p, nwords,
-        t->tc_sched_off.p, t->tc_stab.p);
-    FMM_CUDA_TRY(cudaGetLastError());
-    t->sched_serial = t->build_serial;
-    t->sched_version = t->order_version;
-  }
+  if (int rc = fmm_tc_schedule(t, st)) return rc;
   const size_t nm = (size_t)nc * pl.kpad;
   if (fmm_reserve(t->tc_Mh, nm) || fmm_reserve(t->tc_Ml, nm) || fmm_reserve(t->tc_mexp, nc) ||
       fmm_reserve(t->d_tcerr, 4))
@@ -1646,4 +1656,198 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, 4 * sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, st));
   return FMM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// class-major CUDA-core M2L (generated kernels in m2l_cm_s*.cu) over the same
+// class-step schedule: a block per tile, a thread per row, a step gives a warp
+// pairs of one class
+// ---------------------------------------------------------------------------
+namespace {
+
+// Per-pair orders (target-list order) into the schedule's (step, row) slots:
+// a warp per target cell, lanes over its pairs.
+__global__ void k_cm_otab(const int *off, const int *cls, const unsigned char *ord, int nc, const int *pos,
+                          const unsigned *bm, const unsigned *rank, int nwords, const int *sched_off,
+                          unsigned char *otab) {
+  const int A = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (A >= nc) return;
+  const int row = pos[A], tile = row / TC_ROWS;
+  const size_t rb = (size_t)tile * nwords;
+  const unsigned sb = (unsigned)sched_off[tile];
+  for (int k = off[A] + lane; k < off[A + 1]; k += 32) {
+    const unsigned c = (unsigned)cls[k];
+    const size_t w = rb + (c >> 5);
+    const unsigned st = sb + rank[w] + __popc(bm[w] & ((1u << (c & 31)) - 1u));
+    otab[(size_t)st * TC_ROWS + row % TC_ROWS] = ord[k];
+  }
+}
+
+// Per (tile, warp of 32 rows): how many of the tile's steps have a pair in the
+// warp's rows, then their list (a block per tile).
+__global__ void k_cm_wcount(const int *sched_off, const int *stab, int *cnt) {
+  const int tile = blockIdx.x, w = threadIdx.x >> 5;
+  int n = 0;
+  for (int s = sched_off[tile]; s < sched_off[tile + 1]; s++)
+    n += __any_sync(0xffffffffu, stab[(size_t)s * TC_ROWS + threadIdx.x] >= 0) ? 1 : 0;
+  if ((threadIdx.x & 31) == 0) cnt[tile * 4 + w] = n;
+}
+__global__ void k_cm_wlist(const int *sched_off, const int *stab, const int *woff, int *wstep) {
+  const int tile = blockIdx.x, w = threadIdx.x >> 5;
+  int o = woff[tile * 4 + w];
+  for (int s = sched_off[tile]; s < sched_off[tile + 1]; s++)
+    if (__any_sync(0xffffffffu, stab[(size_t)s * TC_ROWS + threadIdx.x] >= 0)) {
+      if ((threadIdx.x & 31) == 0) wstep[o] = s;
+      o++;
+    }
+}
+
+// Each target list's pair indices by descending per-pair order (orders clamped
+// to [qlo, qhi], at most 32 of them), stable within an order: a warp per
+// target (row r of the M2L processing order), lane b counting the pairs of
+// order qhi - b.  Also the target's sort key: its level, then its number of
+// pairs of order >= qhi - 2, descending (warps of targets alike in their
+// high-order pairs spend less time on lanes that have none).
+__global__ void k_tp_perm(const int *off, const unsigned char *ord, const int *order, const unsigned char *clevel,
+                          int nc, int qlo, int qhi, int *perm, unsigned *key, unsigned *val) {
+  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= nc) return;
+  const int A = order[r];
+  const int k0 = off[A], k1 = off[A + 1], nb = qhi - qlo + 1;
+  int cnt = 0;
+  for (int k = k0; k < k1; k += 32) {
+    const int kk = k + lane;
+    const int q = kk < k1 ? min(max((int)ord[kk], qlo), qhi) : -1;
+    for (int b = 0; b < nb; b++) {
+      const unsigned m = __ballot_sync(0xffffffffu, q == qhi - b);
+      if (lane == b) cnt += __popc(m);
+    }
+  }
+  int pos = cnt;  // exclusive prefix over the lanes: the first slot of each order
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, pos, o);
+    if (lane >= o) pos += v;
+  }
+  pos -= cnt;
+  const int hi = __shfl_sync(0xffffffffu, pos, min(3, nb));  // pairs of the 3 highest orders
+  if (lane == 0) {
+    key[r] = ((unsigned)clevel[A] << 24) | (0xffffffu - (unsigned)min(hi, 0xffffff));
+    val[r] = (unsigned)A;
+  }
+  for (int k = k0; k < k1; k += 32) {
+    const int kk = k + lane;
+    const int q = kk < k1 ? min(max((int)ord[kk], qlo), qhi) : -1;
+    const unsigned same = __match_any_sync(0xffffffffu, q);
+    const int first = __shfl_sync(0xffffffffu, pos, q >= 0 ? qhi - q : 0);
+    if (q >= 0) perm[k0 + first + __popc(same & ((1u << lane) - 1u))] = kk;
+    for (int b = 0; b < nb; b++) {
+      const unsigned m = __ballot_sync(0xffffffffu, q == qhi - b);
+      if (lane == b) pos += __popc(m);
+    }
+  }
+}
+
+}  // namespace
+
+#include "m2l_cm.cuh"
+
+bool fmm_m2l_cm_supported(int p, int so) { return p >= so + 1 && p <= fmm_m2l_cm_pmax(so); }
+
+int fmm_m2l_cm(DevTree *t, const float *M, int mstr, float *L, int lstr, const unsigned char *ord, cudaStream_t st) {
+  static_assert(TC_ROWS == 128, "the generated kernels take tiles of 128 rows");
+  const int p = t->order, so = t->so, nc = t->ncells;
+  if (!fmm_m2l_cm_supported(p, so) || (mstr & 3) || t->nclasses > TC_SCHED_MAXW * 32) return FMM_ERR_STATE;
+  const int lsize = fmm_nterms(p - so);
+  if (t->nm2l == 0) {
+    FMM_CUDA_TRY(cudaMemset2DAsync(L, sizeof(float) * lstr, 0, sizeof(float) * lsize, nc, st));
+    return FMM_OK;
+  }
+  if (int rc = fmm_tc_schedule(t, st)) return rc == FMM_ERR_RANGE ? FMM_ERR_STATE : rc;
+  const int ntiles = (nc + TC_ROWS - 1) / TC_ROWS;
+  if (t->cm_wserial != t->sched_serial || t->cm_wversion != t->sched_version) {
+    const int nw = 4 * ntiles;
+    if (fmm_reserve(t->cm_woff, (size_t)nw + 1) ||
+        fmm_reserve(t->cm_wstep, (size_t)4 * (t->tc_nsteps > 0 ? t->tc_nsteps : 1)) ||
+        fmm_reserve(t->tmp, sizeof(int) * (nw + fmm_scan_tmp_elems<int>(nw))))
+      return FMM_ERR_CUDA;
+    int *cnt = (int *)t->tmp.p, *stmp = cnt + nw;
+    fmm_note_launch(), k_cm_wcount<<<ntiles, TC_ROWS, 0, st>>>(t->tc_sched_off.p, t->tc_stab.p, cnt);
+    if (int rc = fmm_scan<int>(cnt, t->cm_woff.p, nw, t->cm_woff.p + nw, stmp, st)) return rc;
+    fmm_note_launch(), k_cm_wlist<<<ntiles, TC_ROWS, 0, st>>>(t->tc_sched_off.p, t->tc_stab.p, t->cm_woff.p,
+                                                              t->cm_wstep.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    t->cm_wserial = t->sched_serial;
+    t->cm_wversion = t->sched_version;
+  }
+  if (ord) {
+    if (int rc = fmm_m2l_csr(t, st)) return rc;
+    if (fmm_reserve(t->cm_otab, (size_t)(t->tc_nsteps > 0 ? t->tc_nsteps : 1) * TC_ROWS)) return FMM_ERR_CUDA;
+    fmm_note_launch(), k_cm_otab<<<fmm_blocks((size_t)nc * 32, 256), 256, 0, st>>>(
+        t->m2l_off.p, t->m2l_cls.p, ord, nc, t->tc_pos.p, t->tc_bitmap.p, t->tc_rank.p, (t->nclasses + 31) / 32,
+        t->tc_sched_off.p, t->cm_otab.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+  }
+  CmParams P;
+  P.woff = t->cm_woff.p;
+  P.wstep = t->cm_wstep.p;
+  P.sched_cls = t->tc_sched_cls.p;
+  P.stab = t->tc_stab.p;
+  P.otab = ord ? t->cm_otab.p : nullptr;
+  P.order = t->m2l_order.p;
+  P.ncells = nc;
+  P.p = p;
+  P.D = (const float *)t->cls_Df.p;
+  P.dstr = fmm_stride4(fmm_nterms(p));
+  P.clevel = t->clevel.p;
+  P.M = M;
+  P.mstr = mstr;
+  P.L = L;
+  P.lstr = lstr;
+  P.lsize = lsize;
+  return fmm_m2l_cm_launch(so, P, st);
+}
+
+int fmm_m2l_tp(DevTree *t, const float *M, int mstr, float *L, int lstr, const unsigned char *ord, cudaStream_t st) {
+  const int p = t->order, so = t->so, nc = t->ncells;
+  if (!fmm_m2l_cm_supported(p, so) || (mstr & 3) || p - so > 32) return FMM_ERR_STATE;
+  const int lsize = fmm_nterms(p - so);
+  if (t->nm2l == 0) {
+    FMM_CUDA_TRY(cudaMemset2DAsync(L, sizeof(float) * lstr, 0, sizeof(float) * lsize, nc, st));
+    return FMM_OK;
+  }
+  if (int rc = fmm_m2l_csr(t, st)) return rc;
+  if (ord) {
+    const size_t nbh = fmm_rs_nblocks(nc), hist_n = 256 * nbh;
+    if (fmm_reserve(t->tp_perm, (size_t)t->nm2l) || fmm_reserve(t->tp_tgt, nc) ||
+        fmm_reserve(t->tmp, (size_t)nc * 12 + hist_n * 4 + fmm_scan_tmp_elems<uint32_t>(hist_n) * 4 + 256))
+      return FMM_ERR_CUDA;
+    char *q = t->tmp.p;
+    unsigned *k1 = (unsigned *)q; q += (size_t)nc * 4;
+    unsigned *k2 = (unsigned *)q; q += (size_t)nc * 4;
+    uint32_t *v2 = (uint32_t *)q; q += (size_t)nc * 4;
+    uint32_t *hist = (uint32_t *)q; q += hist_n * 4;
+    uint32_t *stmp = (uint32_t *)q;
+    fmm_note_launch(), k_tp_perm<<<fmm_blocks((size_t)nc * 32, 256), 256, 0, st>>>(
+        t->m2l_off.p, ord, t->m2l_order.p, t->clevel.p, nc, so + 1, p, t->tp_perm.p, k1, (unsigned *)t->tp_tgt.p);
+    FMM_CUDA_TRY(cudaGetLastError());
+    if (int rc = fmm_radix_sort<unsigned>(k1, (uint32_t *)t->tp_tgt.p, k2, v2, nc, 0, 32, hist, stmp, st)) return rc;
+  }
+  TpParams P;
+  P.tgt = ord ? t->tp_tgt.p : t->m2l_order.p;
+  P.ntgt = nc;
+  P.off = t->m2l_off.p;
+  P.src = t->m2l_src.p;
+  P.cls = t->m2l_cls.p;
+  P.perm = ord ? t->tp_perm.p : nullptr;
+  P.ord = ord;
+  P.p = p;
+  P.D = (const float *)t->cls_Df.p;
+  P.dstr = fmm_stride4(fmm_nterms(p));
+  P.clevel = t->clevel.p;
+  P.M = M;
+  P.mstr = mstr;
+  P.L = L;
+  P.lstr = lstr;
+  P.lsize = lsize;
+  return fmm_m2l_tp_launch(so, P, st);
 }

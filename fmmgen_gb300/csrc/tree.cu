@@ -1160,7 +1160,9 @@ void fmm_tree_destroy(DevTree *t) {
   fmm_release(t->tc_T); fmm_release(t->tc_Mh); fmm_release(t->tc_Ml); fmm_release(t->tc_mexp);
   fmm_release(t->d_tcerr);
   fmm_release(t->tc_sched_off); fmm_release(t->tc_sched_cls); fmm_release(t->tc_bitmap); fmm_release(t->tc_rank);
-  fmm_release(t->tc_stab); fmm_release(t->tc_pos);
+  fmm_release(t->tc_stab); fmm_release(t->tc_pos); fmm_release(t->cm_otab);
+  fmm_release(t->cm_woff); fmm_release(t->cm_wstep); fmm_release(t->tp_perm); fmm_release(t->tp_tgt);
+  t->cm_wserial = ~0ull;
   t->sched_serial = ~0ull;
   t->tc_serial = ~0ull;
   fmm_release(t->wdec);

@@ -5,7 +5,8 @@
 //   implementation: tensor cores (p <= 9) with source rows gathered row by row
 //                   or (trees whose levels are all complete) boxed from level
 //                   grids, generated CUDA-core kernels (orders that have them),
-//                   warp contraction engine;
+//                   class-major and target-major generated CUDA-core kernels
+//                   (every order up to 12), warp contraction engine;
 //   tensor-core pipeline depth: 2 .. the row-gather slots that fit in shared memory;
 //   tensor cores alone, or overlapped with the P2P (in 4- or 2-warp blocks);
 //   grouping of the cells into tiles / warps: by octant within the parent, or Morton.
@@ -30,6 +31,8 @@ int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_c
   std::vector<Cand> cands;
   const int maxs = fmm_m2l_tc_max_slots(t->order, t->so);
   const bool gen = fmm_m2l_gen_supported(t->order, t->so);
+  const bool cm = fmm_m2l_cm_supported(t->order, t->so) && t->nclasses <= 262144;
+  const bool tp = fmm_m2l_cm_supported(t->order, t->so);
   const bool boxes = precision != 0 && maxs > 0 && fmm_m2l_tc_boxes_ok(t, st);
   for (int g = 0; g < 2; g++) {
     if (precision != 0) {
@@ -40,6 +43,8 @@ int fmm_autotune(DevTree *t, const double *S, int precision, int reps, int max_c
           if (g == 0 && boxes) cands.push_back({3, s, g, ov});
         }
       if (gen) cands.push_back({1, 0, g, 0});
+      if (cm) cands.push_back({4, 0, g, 0});
+      if (tp) cands.push_back({5, 0, g, 0});
     }
     cands.push_back({2, 0, g, 0});
   }

@@ -230,7 +230,9 @@ class Tree:
         """M2L implementation (-1 default rules, 0 tensor cores with source rows
         gathered row by row, 1 generated CUDA-core kernels, 2 contraction
         engine, 3 tensor cores with source rows boxed from level grids where
-        every level is complete, else as 0), tensor-core pipeline depth
+        every level is complete, else as 0, 4 class-major and 5 target-major
+        CUDA-core kernels; per-pair orders run on 5 unless 2 or 4 is chosen),
+        tensor-core pipeline depth
         (0: as deep as fits), cell grouping (0 by octant, 1 Morton) and
         overlap (1 / 2: tensor-core M2L and P2P side by side on the SMs, the
         P2P in blocks of 4 / 2 warps)."""

@@ -242,8 +242,14 @@ int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out4);
  * gathered row by row, 1 generated CUDA-core kernels, 2 contraction engine,
  * 3 tensor cores with the source rows boxed from dense level grids by
  * tensor-map copies where every level of the tree is complete (one system,
- * all 8^l cells of every level), else as 0 (mixed passes; FP64 passes always
- * use the engine).
+ * all 8^l cells of every level), else as 0, 4 class-major CUDA-core kernels
+ * (a warp takes 32 target cells' pairs of one translation class per step),
+ * 5 target-major CUDA-core kernels (a thread per target cell over its list);
+ * 4 and 5 cover orders up to 12 for charges, 8 for dipoles (mixed passes;
+ * FP64 passes always use the engine).  Per-pair M2L orders
+ * (fmmgen_tree_set_m2l_orders, an order model) run in mixed passes on the
+ * target-major kernels, on the class-major ones with impl 4, on the engine
+ * with impl 2 or where the kernels do not cover the order.
  * nslots: tensor-core pipeline depth (operand slots), 0 = as many as fit.
  * grouping: order of a level's cells in M2L tiles and warps, 0 by octant
  * within the parent, 1 Morton.  overlap: 1 (2) runs the tensor-core M2L on a
