@@ -315,28 +315,109 @@ __device__ __forceinline__ void mlp_forward(const float *P, const float *x, floa
 
 // Order of each pair: the lowest q whose cumulative predicted probability
 // P(q* <= q) reaches 1 - delta (delta trades M2L work against the risk of a
-// too-low order), clamped to [2, qmax].  The weights sit in shared memory.
+// too-low order), clamped to [2, qmax].
+__device__ __forceinline__ unsigned char mlp_order(const float *z, float delta, int qmax) {
+  float zm = z[0];
+  for (int i = 1; i < MLP_OUT; i++) zm = fmaxf(zm, z[i]);
+  float s = 0;
+  for (int i = 0; i < MLP_OUT; i++) s += __expf(z[i] - zm);
+  float cum = 0;
+  int q = MLP_QMIN + MLP_OUT - 1;
+  for (int i = 0; i < MLP_OUT; i++) {
+    cum += __expf(z[i] - zm) / s;
+    if (cum >= 1.f - delta) {
+      q = MLP_QMIN + i;
+      break;
+    }
+  }
+  return (unsigned char)min(max(q, MLP_QMIN), qmax);
+}
+
+// The forward pass of R pairs per thread with the weights in shared memory
+// (float4 broadcasts, each used for the R pairs); the second layer computes
+// four hidden units at once (4 R independent FMA chains) and feeds each into
+// the logits as soon as it is done, so no second hidden layer is kept.  Every
+// output is summed in the order of mlp_forward (bias first, inputs
+// ascending): the same bits.
+template <int R>
 __global__ void __launch_bounds__(128) k_mlp_predict(const float *params, const float *X, long n, float delta,
                                                      int qmax, unsigned char *orders) {
-  __shared__ float P[MLP_NPARAM];
+  __shared__ __align__(16) float P[MLP_NPARAM];
+  __shared__ __align__(16) float W3T[MLP_H][12];  // W3 by hidden unit: the 11 logits' weights (+ 1 pad)
   for (int i = threadIdx.x; i < MLP_NPARAM; i += blockDim.x) P[i] = params[i];
+  for (int i = threadIdx.x; i < MLP_H * 12; i += blockDim.x) {
+    const int h = i / 12, o = i - 12 * h;
+    W3T[h][o] = o < MLP_OUT ? params[OFF_W3 + o * MLP_H + h] : 0.f;
+  }
   __syncthreads();
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-    float x[MLP_IN], h1[MLP_H], h2[MLP_H], z[MLP_OUT];
+  const long stride = (long)R * gridDim.x * blockDim.x;
+  for (long k = R * (blockIdx.x * (long)blockDim.x + threadIdx.x); k < n; k += stride) {
+    float h[R][MLP_H];
 #pragma unroll
-    for (int j = 0; j < MLP_IN; j++) x[j] = X[k * MLP_IN + j];
-    mlp_forward(P, x, h1, h2, z);
-    float zm = z[0];
-    for (int i = 1; i < MLP_OUT; i++) zm = fmaxf(zm, z[i]);
-    float s = 0;
-    for (int i = 0; i < MLP_OUT; i++) s += __expf(z[i] - zm);
-    float cum = 0;
-    int q = MLP_QMIN + MLP_OUT - 1;
-    for (int i = 0; i < MLP_OUT; i++) {
-      cum += __expf(z[i] - zm) / s;
-      if (cum >= 1.f - delta) { q = MLP_QMIN + i; break; }
+    for (int r = 0; r < R; r++) {
+      const float4 *x4 = (const float4 *)(X + min(k + r, n - 1) * MLP_IN);
+      float x[MLP_IN];
+#pragma unroll
+      for (int j = 0; j < MLP_IN / 4; j++) {
+        const float4 u = x4[j];
+        x[4 * j] = u.x, x[4 * j + 1] = u.y, x[4 * j + 2] = u.z, x[4 * j + 3] = u.w;
+      }
+#pragma unroll
+      for (int i = 0; i < MLP_H; i++) {
+        float a = P[OFF_B1 + i];
+#pragma unroll
+        for (int j = 0; j < MLP_IN; j += 4) {
+          const float4 w = *(const float4 *)&P[OFF_W1 + i * MLP_IN + j];
+          a = fmaf(w.x, x[j], a);
+          a = fmaf(w.y, x[j + 1], a);
+          a = fmaf(w.z, x[j + 2], a);
+          a = fmaf(w.w, x[j + 3], a);
+        }
+        h[r][i] = fmaxf(a, 0.f);
+      }
     }
-    orders[k] = (unsigned char)min(max(q, MLP_QMIN), qmax);
+    float z[R][MLP_OUT];
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+      for (int o = 0; o < MLP_OUT; o++) z[r][o] = P[OFF_B3 + o];
+#pragma unroll 4
+    for (int i = 0; i < MLP_H; i += 4) {
+      float a[4][R];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int r = 0; r < R; r++) a[u][r] = P[OFF_B2 + i + u];
+#pragma unroll
+      for (int j = 0; j < MLP_H; j += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const float4 w = *(const float4 *)&P[OFF_W2 + (i + u) * MLP_H + j];
+#pragma unroll
+          for (int r = 0; r < R; r++) {
+            a[u][r] = fmaf(w.x, h[r][j], a[u][r]);
+            a[u][r] = fmaf(w.y, h[r][j + 1], a[u][r]);
+            a[u][r] = fmaf(w.z, h[r][j + 2], a[u][r]);
+            a[u][r] = fmaf(w.w, h[r][j + 3], a[u][r]);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float4 t0 = *(const float4 *)&W3T[i + u][0], t1 = *(const float4 *)&W3T[i + u][4],
+                     t2 = *(const float4 *)&W3T[i + u][8];
+        const float t[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const float g = fmaxf(a[u][r], 0.f);
+#pragma unroll
+          for (int o = 0; o < MLP_OUT; o++) z[r][o] = fmaf(t[o], g, z[r][o]);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+      if (k + r < n) orders[k + r] = mlp_order(z[r], delta, qmax);
   }
 }
 
@@ -500,8 +581,8 @@ int fmm_order_labels(DevTree *t, double eps, unsigned char *label, float *errq, 
 int fmm_mlp_predict(const float *params, const float *X, long n, float delta, int qmax, unsigned char *orders,
                     cudaStream_t st) {
   if (n <= 0) return FMM_OK;
-  const unsigned nb = (unsigned)std::min<long>((n + 127) / 128, 152L * 16);
-  fmm_note_launch(), k_mlp_predict<<<nb, 128, 0, st>>>(params, X, n, delta, qmax, orders);
+  const unsigned nb = (unsigned)std::min<long>((n + 255) / 256, 152L * 16);
+  fmm_note_launch(), k_mlp_predict<2><<<nb, 128, 0, st>>>(params, X, n, delta, qmax, orders);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }
