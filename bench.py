@@ -368,7 +368,8 @@ def main():
         r = tree.autotune(precision="mixed", reps=3)
         autotune = {"chosen": r["best"], "candidates_ms": [
             [c["impl"], c["nslots"], c["grouping"], c["overlap"], round(c["ms"], 3)] for c in r["table"]],
-            "legend": "impl 0 tensor cores (row gather) / 1 generated CUDA-core / 2 contraction engine / 3 tensor cores (level-grid boxes); nslots = tensor-core "
+            "legend": "impl 0 tensor cores (row gather) / 1 generated CUDA-core / 2 contraction engine / 3 tensor cores "
+                      "(level-grid boxes) / 4 generated class-major / 5 generated target-major; nslots = tensor-core "
                       "pipeline depth; grouping 0 by octant / 1 Morton; overlap 1 / 2 = M2L and P2P side by side "
                       "(P2P blocks of 4 / 2 warps); "
                       "M2L + P2P median ms"}
@@ -555,7 +556,19 @@ def main():
     tpeak = peaks.get("bf16_tflops")  # dense 16-bit tensor peak (FP16 runs at the bf16 rate)
     exec_tf = m2l_exec_flops / (m2l_ms / 1e3) / 1e12 if m2l_ms > 0 else 0.0
     alg_tf = m2l_flops / (m2l_ms / 1e3) / 1e12 if m2l_ms > 0 else 0.0
-    roofline_m2l = {"kernel": "M2L (k_m2l_tc, tcgen05 kind::f16)" if m2l_steps else "M2L (CUDA cores)",
+    tuned = tree.get_tune()["impl"]
+    if m2l_steps:
+        m2l_kernel = ("M2L (k_m2l_tcg, tcgen05 kind::f16, source rows boxed from level grids)" if m2l_boxes
+                      else "M2L (k_m2l_tc, tcgen05 kind::f16)")
+    elif learned_info:
+        m2l_kernel = ("M2L (k_m2l_tp_*, generated FP32, a thread per target, each pair at its own order; the phase "
+                      "includes the pairs' features and the order model's inference)")
+    else:
+        m2l_kernel = {1: "M2L (k_m2l_reg_*, generated FP32, a thread per target)",
+                      4: "M2L (k_m2l_cm_*, generated FP32, class-major)",
+                      5: "M2L (k_m2l_tp_*, generated FP32, a thread per target)",
+                      2: "M2L (k_m2l_pk, FP32 contraction engine)"}.get(tuned, "M2L (CUDA cores)")
+    roofline_m2l = {"kernel": m2l_kernel,
                     "bound": "tensor", "achieved": exec_tf, "algorithmic_tflops": alg_tf, "peak": tpeak,
                     "unit": "TFLOP/s", "frac": exec_tf / tpeak if tpeak else None,
                     "algorithmic_frac": alg_tf / tpeak if tpeak else None,
@@ -567,6 +580,8 @@ def main():
                             "triangular N per chunk); algorithmic = 2*C(p+6,6) per pair; "
                             "peak = measured bf16 dense (MEASURED_PEAKS.json)"}
 
+    if dom == "M2L":
+        roofline["kernel"] = m2l_kernel
     if dom == "M2L" and m2l_steps and tpeak:
         # the dominant M2L ran on the tensor cores: its roofline is the measured
         # dense 16-bit tensor peak (algorithmic flops, as for every bound); the

@@ -333,91 +333,102 @@ __device__ __forceinline__ unsigned char mlp_order(const float *z, float delta, 
   return (unsigned char)min(max(q, MLP_QMIN), qmax);
 }
 
-// The forward pass of R pairs per thread with the weights in shared memory
-// (float4 broadcasts, each used for the R pairs); the second layer computes
-// four hidden units at once (4 R independent FMA chains) and feeds each into
-// the logits as soon as it is done, so no second hidden layer is kept.  Every
+// The forward pass of two pairs per thread.  The weights sit in shared memory
+// (float4 broadcasts, each used for both pairs) and so do the first hidden
+// layers (a row per pair, padded so the lanes' float4 reads are conflict
+// free): both layers loop at run time over short unrolled bodies -- a fully
+// unrolled network (two pairs x 5,824 multiply-adds) outgrows the instruction
+// cache.  Units are computed MLP_U at a time (2 MLP_U independent FMA chains),
+// and each second-layer unit feeds the logits as soon as it is done.  Every
 // output is summed in the order of mlp_forward (bias first, inputs
 // ascending): the same bits.
-template <int R>
+#define MLP_U 8
+#define MLP_HS (MLP_H + 4)  // padded row of a first hidden layer
+constexpr int MLP_PREDICT_SMEM = (MLP_NPARAM + 3) / 4 * 16 + MLP_H * 12 * 4 + 128 * 2 * MLP_HS * 4;
 __global__ void __launch_bounds__(128) k_mlp_predict(const float *params, const float *X, long n, float delta,
                                                      int qmax, unsigned char *orders) {
-  __shared__ __align__(16) float P[MLP_NPARAM];
-  __shared__ __align__(16) float W3T[MLP_H][12];  // W3 by hidden unit: the 11 logits' weights (+ 1 pad)
+  extern __shared__ float4 mlp_smem[];
+  float *P = (float *)mlp_smem;
+  float(*W3T)[12] = (float(*)[12])(P + (MLP_NPARAM + 3) / 4 * 4);  // W3 by hidden unit (11 logits + 1 pad)
+  float *H = (float *)(W3T + MLP_H) + threadIdx.x * 2 * MLP_HS;     // this thread's two first hidden layers
   for (int i = threadIdx.x; i < MLP_NPARAM; i += blockDim.x) P[i] = params[i];
   for (int i = threadIdx.x; i < MLP_H * 12; i += blockDim.x) {
     const int h = i / 12, o = i - 12 * h;
     W3T[h][o] = o < MLP_OUT ? params[OFF_W3 + o * MLP_H + h] : 0.f;
   }
   __syncthreads();
-  const long stride = (long)R * gridDim.x * blockDim.x;
-  for (long k = R * (blockIdx.x * (long)blockDim.x + threadIdx.x); k < n; k += stride) {
-    float h[R][MLP_H];
+  const long stride = 2L * gridDim.x * blockDim.x;
+  for (long k = 2L * (blockIdx.x * (long)blockDim.x + threadIdx.x); k < n; k += stride) {
+    float x[2][MLP_IN];
 #pragma unroll
-    for (int r = 0; r < R; r++) {
+    for (int r = 0; r < 2; r++) {
       const float4 *x4 = (const float4 *)(X + min(k + r, n - 1) * MLP_IN);
-      float x[MLP_IN];
 #pragma unroll
       for (int j = 0; j < MLP_IN / 4; j++) {
         const float4 u = x4[j];
-        x[4 * j] = u.x, x[4 * j + 1] = u.y, x[4 * j + 2] = u.z, x[4 * j + 3] = u.w;
-      }
-#pragma unroll
-      for (int i = 0; i < MLP_H; i++) {
-        float a = P[OFF_B1 + i];
-#pragma unroll
-        for (int j = 0; j < MLP_IN; j += 4) {
-          const float4 w = *(const float4 *)&P[OFF_W1 + i * MLP_IN + j];
-          a = fmaf(w.x, x[j], a);
-          a = fmaf(w.y, x[j + 1], a);
-          a = fmaf(w.z, x[j + 2], a);
-          a = fmaf(w.w, x[j + 3], a);
-        }
-        h[r][i] = fmaxf(a, 0.f);
+        x[r][4 * j] = u.x, x[r][4 * j + 1] = u.y, x[r][4 * j + 2] = u.z, x[r][4 * j + 3] = u.w;
       }
     }
-    float z[R][MLP_OUT];
-#pragma unroll
-    for (int r = 0; r < R; r++)
-#pragma unroll
-      for (int o = 0; o < MLP_OUT; o++) z[r][o] = P[OFF_B3 + o];
-#pragma unroll 4
+#pragma unroll 1
     for (int i = 0; i < MLP_H; i += 4) {
-      float a[4][R];
+      float a[4][2];
 #pragma unroll
-      for (int u = 0; u < 4; u++)
+      for (int u = 0; u < 4; u++) {
+        a[u][0] = a[u][1] = P[OFF_B1 + i + u];
 #pragma unroll
-        for (int r = 0; r < R; r++) a[u][r] = P[OFF_B2 + i + u];
+        for (int j = 0; j < MLP_IN; j += 4) {
+          const float4 w = *(const float4 *)&P[OFF_W1 + (i + u) * MLP_IN + j];
 #pragma unroll
-      for (int j = 0; j < MLP_H; j += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const float4 w = *(const float4 *)&P[OFF_W2 + (i + u) * MLP_H + j];
-#pragma unroll
-          for (int r = 0; r < R; r++) {
-            a[u][r] = fmaf(w.x, h[r][j], a[u][r]);
-            a[u][r] = fmaf(w.y, h[r][j + 1], a[u][r]);
-            a[u][r] = fmaf(w.z, h[r][j + 2], a[u][r]);
-            a[u][r] = fmaf(w.w, h[r][j + 3], a[u][r]);
+          for (int r = 0; r < 2; r++) {
+            a[u][r] = fmaf(w.x, x[r][j], a[u][r]);
+            a[u][r] = fmaf(w.y, x[r][j + 1], a[u][r]);
+            a[u][r] = fmaf(w.z, x[r][j + 2], a[u][r]);
+            a[u][r] = fmaf(w.w, x[r][j + 3], a[u][r]);
           }
         }
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int r = 0; r < 2; r++)
+        *(float4 *)&H[r * MLP_HS + i] =
+            make_float4(fmaxf(a[0][r], 0.f), fmaxf(a[1][r], 0.f), fmaxf(a[2][r], 0.f), fmaxf(a[3][r], 0.f));
+    }
+    float z[2][MLP_OUT];
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int o = 0; o < MLP_OUT; o++) z[r][o] = P[OFF_B3 + o];
+#pragma unroll 1
+    for (int i = 0; i < MLP_H; i += MLP_U) {
+      float a[MLP_U][2];
+#pragma unroll
+      for (int u = 0; u < MLP_U; u++) a[u][0] = a[u][1] = P[OFF_B2 + i + u];
+#pragma unroll 2
+      for (int j = 0; j < MLP_H; j += 4) {
+        const float4 h0 = *(const float4 *)&H[j], h1 = *(const float4 *)&H[MLP_HS + j];
+#pragma unroll
+        for (int u = 0; u < MLP_U; u++) {
+          const float4 w = *(const float4 *)&P[OFF_W2 + (i + u) * MLP_H + j];
+          a[u][0] = fmaf(w.x, h0.x, a[u][0]), a[u][1] = fmaf(w.x, h1.x, a[u][1]);
+          a[u][0] = fmaf(w.y, h0.y, a[u][0]), a[u][1] = fmaf(w.y, h1.y, a[u][1]);
+          a[u][0] = fmaf(w.z, h0.z, a[u][0]), a[u][1] = fmaf(w.z, h1.z, a[u][1]);
+          a[u][0] = fmaf(w.w, h0.w, a[u][0]), a[u][1] = fmaf(w.w, h1.w, a[u][1]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < MLP_U; u++) {
         const float4 t0 = *(const float4 *)&W3T[i + u][0], t1 = *(const float4 *)&W3T[i + u][4],
                      t2 = *(const float4 *)&W3T[i + u][8];
         const float t[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
 #pragma unroll
-        for (int r = 0; r < R; r++) {
+        for (int r = 0; r < 2; r++) {
           const float g = fmaxf(a[u][r], 0.f);
 #pragma unroll
           for (int o = 0; o < MLP_OUT; o++) z[r][o] = fmaf(t[o], g, z[r][o]);
         }
       }
     }
-#pragma unroll
-    for (int r = 0; r < R; r++)
-      if (k + r < n) orders[k + r] = mlp_order(z[r], delta, qmax);
+    orders[k] = mlp_order(z[0], delta, qmax);
+    if (k + 1 < n) orders[k + 1] = mlp_order(z[1], delta, qmax);
   }
 }
 
@@ -582,7 +593,8 @@ int fmm_mlp_predict(const float *params, const float *X, long n, float delta, in
                     cudaStream_t st) {
   if (n <= 0) return FMM_OK;
   const unsigned nb = (unsigned)std::min<long>((n + 255) / 256, 152L * 16);
-  fmm_note_launch(), k_mlp_predict<2><<<nb, 128, 0, st>>>(params, X, n, delta, qmax, orders);
+  FMM_CUDA_TRY(cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, MLP_PREDICT_SMEM));
+  fmm_note_launch(), k_mlp_predict<<<nb, 128, MLP_PREDICT_SMEM, st>>>(params, X, n, delta, qmax, orders);
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
 }

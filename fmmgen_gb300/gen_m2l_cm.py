@@ -53,6 +53,7 @@ RMAX = 208              # register estimate per thread an output group may reach
 OVERHEAD = 32           # registers besides accumulators, temporaries and the chunk
 PARTIAL_MIN_TERMS = 21  # outputs with at least this many terms per pair (in a kernel) sum per pair first
 ROWS = 128              # threads of a block (class-major: rows of a schedule tile)
+MIN_BLOCKS = 2          # resident blocks per SM the register allocation must allow
 
 
 def nterms(p):
@@ -240,7 +241,7 @@ def header_lines(kern, name, so, pmax, params, extra_smem_comment):
     return [f"// outputs {outs[0]}..{outs[-1]} (degree {kern['lo']}..{sum(mono[outs[-1]])}), multipole terms "
             f"{c0['mb']}..{c1['me'] - 1}: {len(outs)} accumulators, {len(kern['temps'])} per-pair sums, "
             f"{nf} multiply-adds per pair at order {pmax}; {'stores' if kern['first'] else 'adds to'} the outputs",
-            f"__global__ void __launch_bounds__({ROWS}, 2) {name}(const {params} P) {{",
+            f"__global__ void __launch_bounds__({ROWS}, {MIN_BLOCKS}) {name}(const {params} P) {{",
             f"  // per warp: 2 source-chunk buffers [32 rows][{CH // 4 + 1}] (float4){extra_smem_comment}",
             "  extern __shared__ float4 cm_smem[];",
             "  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;"]
