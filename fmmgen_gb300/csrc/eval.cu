@@ -674,8 +674,9 @@ static int run_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L, 
 // the tuned choice or, by default, tensor cores where the order allows
 // (p <= 9, precision "mixed": with source rows boxed from level grids when
 // every level is complete, else gathered row by row), else the generated
-// CUDA-core kernels where this order has them, else the warp contraction
-// engine; FP64: the engine.
+// CUDA-core kernels where this order has them (register-resident, p <= 8;
+// then the target-major kernels of every order up to 12), else the warp
+// contraction engine; FP64: the engine.
 enum { M2L_TC = 0, M2L_GEN = 1, M2L_ENGINE = 2, M2L_TCG = 3, M2L_CM = 4, M2L_TP = 5 };
 static inline bool is_tc(int impl) { return impl == M2L_TC || impl == M2L_TCG; }
 bool fmm_m2l_gen_supported(int p, int so) {
@@ -691,7 +692,7 @@ static int m2l_impl(const DevTree *t, int precision) {
   if (is_tc(impl) && (!tc_ok || t->nclasses > 262144)) impl = M2L_GEN;  // class bitmap of the tile schedule
   if (impl == M2L_CM && (!fmm_m2l_cm_supported(t->order, t->so) || t->nclasses > 262144)) impl = M2L_GEN;
   if (impl == M2L_TP && !fmm_m2l_cm_supported(t->order, t->so)) impl = M2L_GEN;
-  if (impl == M2L_GEN && !gen_ok) impl = M2L_ENGINE;
+  if (impl == M2L_GEN && !gen_ok) impl = fmm_m2l_cm_supported(t->order, t->so) ? M2L_TP : M2L_ENGINE;
   return impl;
 }
 

@@ -237,8 +237,8 @@ int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out4);
 
 /* ---- M2L choices and their autotuner (no counterpart in the reference) ----
  * impl: -1 the default rules (tensor cores for "mixed" where p <= 9 -- as
- * impl 3 --, else the generated CUDA-core kernels where the order has them,
- * else the warp contraction engine), 0 tensor cores with the source rows
+ * impl 3 --, else the generated CUDA-core kernels where the order has them:
+ * impl 1, then impl 5, else the warp contraction engine), 0 tensor cores with the source rows
  * gathered row by row, 1 generated CUDA-core kernels, 2 contraction engine,
  * 3 tensor cores with the source rows boxed from dense level grids by
  * tensor-map copies where every level of the tree is complete (one system,
