@@ -60,7 +60,8 @@ def test_set_tune_rejects_unsupported(fg):
     with pytest.raises(fg.FMMError):
         t.set_tune(1)  # no generated kernels at p = 12
     with pytest.raises(fg.FMMError):
-        t.set_tune(5)
+        t.set_tune(6)  # no such implementation
+    t.set_tune(5)  # the target-major generated kernels cover p = 12
     t.set_tune(2, 0, 1)
     assert t.get_tune() == {"impl": 2, "nslots": 0, "grouping": 1, "overlap": 0}
 
