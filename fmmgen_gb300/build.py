@@ -37,7 +37,8 @@ def _generate():
     if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
         gen_m2l.generate()
     src = os.path.abspath(gen_m2l_cm.__file__)
-    outs = [os.path.join(CSRC, "m2l_cm.cuh")] + [os.path.join(CSRC, f"m2l_cm_s{so}.cu") for so, _ in gen_m2l_cm.FAMILIES]
+    outs = [os.path.join(CSRC, "m2l_cm.cuh")] + [os.path.join(CSRC, gen_m2l_cm.family_file(so, pm))
+                                                  for so, pm in gen_m2l_cm.FAMILIES]
     if any(not os.path.exists(o) or os.path.getmtime(o) < os.path.getmtime(src) for o in outs):
         gen_m2l_cm.generate()
 

@@ -48,24 +48,37 @@ template <int N> static __device__ __forceinline__ void cm_cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" :: "n"(N) : "memory");
 }
 
-int fmm_m2l_cm_s0(const CmParams &P, cudaStream_t st);  // orders 1..12
-int fmm_m2l_tp_s0(const TpParams &P, cudaStream_t st);
-int fmm_m2l_cm_s1(const CmParams &P, cudaStream_t st);  // orders 2..8
-int fmm_m2l_tp_s1(const TpParams &P, cudaStream_t st);
-// largest order of the family of each source order (0: none)
+int fmm_m2l_cm_s0_p6(const CmParams &P, cudaStream_t st);  // orders 1..6
+int fmm_m2l_tp_s0_p6(const TpParams &P, cudaStream_t st);
+int fmm_m2l_cm_s0_p8(const CmParams &P, cudaStream_t st);  // orders 1..8
+int fmm_m2l_tp_s0_p8(const TpParams &P, cudaStream_t st);
+int fmm_m2l_cm_s0_p12(const CmParams &P, cudaStream_t st);  // orders 1..12
+int fmm_m2l_tp_s0_p12(const TpParams &P, cudaStream_t st);
+int fmm_m2l_cm_s1_p6(const CmParams &P, cudaStream_t st);  // orders 2..6
+int fmm_m2l_tp_s1_p6(const TpParams &P, cudaStream_t st);
+int fmm_m2l_cm_s1_p8(const CmParams &P, cudaStream_t st);  // orders 2..8
+int fmm_m2l_tp_s1_p8(const TpParams &P, cudaStream_t st);
+// largest order of the families of each source order (0: none)
 static inline int fmm_m2l_cm_pmax(int so) {
   if (so == 0) return 12;
   if (so == 1) return 8;
   return 0;
 }
-// launch the family of source order so (FMM_ERR_STATE: none)
+// launch the family of source order so with the smallest largest order >= P.p (FMM_ERR_STATE: none)
 static inline int fmm_m2l_cm_launch(int so, const CmParams &P, cudaStream_t st) {
-  if (so == 0) return fmm_m2l_cm_s0(P, st);
-  if (so == 1) return fmm_m2l_cm_s1(P, st);
+  if (so == 0 && P.p <= 6) return fmm_m2l_cm_s0_p6(P, st);
+  if (so == 0 && P.p <= 8) return fmm_m2l_cm_s0_p8(P, st);
+  if (so == 0 && P.p <= 12) return fmm_m2l_cm_s0_p12(P, st);
+  if (so == 1 && P.p <= 6) return fmm_m2l_cm_s1_p6(P, st);
+  if (so == 1 && P.p <= 8) return fmm_m2l_cm_s1_p8(P, st);
   return FMM_ERR_STATE;
 }
+// launch the family of source order so with the smallest largest order >= P.p (FMM_ERR_STATE: none)
 static inline int fmm_m2l_tp_launch(int so, const TpParams &P, cudaStream_t st) {
-  if (so == 0) return fmm_m2l_tp_s0(P, st);
-  if (so == 1) return fmm_m2l_tp_s1(P, st);
+  if (so == 0 && P.p <= 6) return fmm_m2l_tp_s0_p6(P, st);
+  if (so == 0 && P.p <= 8) return fmm_m2l_tp_s0_p8(P, st);
+  if (so == 0 && P.p <= 12) return fmm_m2l_tp_s0_p12(P, st);
+  if (so == 1 && P.p <= 6) return fmm_m2l_tp_s1_p6(P, st);
+  if (so == 1 && P.p <= 8) return fmm_m2l_tp_s1_p8(P, st);
   return FMM_ERR_STATE;
 }

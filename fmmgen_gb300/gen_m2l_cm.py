@@ -45,8 +45,15 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 
-# (source order, largest order) of the generated families
-FAMILIES = [(0, 12), (1, 8)]
+# (source order, largest order) of the generated families; a pass of order p
+# runs the family of its source order with the smallest largest order >= p (a
+# family's kernels are split for its largest order: at lower orders a smaller
+# family packs more of its terms into fewer kernels)
+FAMILIES = [(0, 6), (0, 8), (0, 12), (1, 6), (1, 8)]
+
+
+def family_file(so, pmax):
+    return f"m2l_cm_s{so}_p{pmax}.cu"
 CH = 48                 # multipole terms per staged chunk (a multiple of 4)
 KERNEL_FMAS = 3000      # multiply-adds per pair in one kernel's body at most (unless one chunk exceeds it)
 RMAX = 208              # register estimate per thread an output group may reach
@@ -471,8 +478,8 @@ def launcher(fname, params, so, pmax, table, grid):
 
 def generate_family(so, pmax):
     kernels = plan(so, pmax)
-    out = os.path.join(CSRC, f"m2l_cm_s{so}.cu")
-    parts = [f"// m2l_cm_s{so}.cu -- generated by fmmgen_gb300/gen_m2l_cm.py; do not edit.",
+    out = os.path.join(CSRC, family_file(so, pmax))
+    parts = [f"// {family_file(so, pmax)} -- generated by fmmgen_gb300/gen_m2l_cm.py; do not edit.",
              f"// FP32 M2L kernels, source order {so}, orders {so + 1}..{pmax}: class-major (k_m2l_cm_*) and",
              "// target-major (k_m2l_tp_*) schedules of the same kernel bodies.",
              '#include "m2l_cm.cuh"', ""]
@@ -484,8 +491,8 @@ def generate_family(so, pmax):
         name, dmin, smem, code = emit_tp(so, pmax, ki, kern)
         parts += [code, ""]
         ttp.append((name, dmin, smem))
-    parts += launcher(f"fmm_m2l_cm_s{so}", "CmParams", so, pmax, tcm, "P.ncells") + [""]
-    parts += launcher(f"fmm_m2l_tp_s{so}", "TpParams", so, pmax, ttp, "P.ntgt")
+    parts += launcher(f"fmm_m2l_cm_s{so}_p{pmax}", "CmParams", so, pmax, tcm, "P.ncells") + [""]
+    parts += launcher(f"fmm_m2l_tp_s{so}_p{pmax}", "TpParams", so, pmax, ttp, "P.ntgt")
     with open(out, "w") as f:
         f.write("\n".join(parts) + "\n")
     return out
@@ -549,25 +556,29 @@ def generate():
     decl = []
     for so, pmax in FAMILIES:
         outs.append(generate_family(so, pmax))
-        decl.append(f"int fmm_m2l_cm_s{so}(const CmParams &P, cudaStream_t st);  // orders {so + 1}..{pmax}")
-        decl.append(f"int fmm_m2l_tp_s{so}(const TpParams &P, cudaStream_t st);")
-    table = ["// largest order of the family of each source order (0: none)",
+        decl.append(f"int fmm_m2l_cm_s{so}_p{pmax}(const CmParams &P, cudaStream_t st);  // orders {so + 1}..{pmax}")
+        decl.append(f"int fmm_m2l_tp_s{so}_p{pmax}(const TpParams &P, cudaStream_t st);")
+    fams = sorted(FAMILIES, key=lambda f: (f[0], f[1]))
+    table = ["// largest order of the families of each source order (0: none)",
              "static inline int fmm_m2l_cm_pmax(int so) {"]
-    for so, pmax in FAMILIES:
-        table.append(f"  if (so == {so}) return {pmax};")
-    table += ["  return 0;", "}", "// launch the family of source order so (FMM_ERR_STATE: none)",
-              "static inline int fmm_m2l_cm_launch(int so, const CmParams &P, cudaStream_t st) {"]
-    for so, pmax in FAMILIES:
-        table.append(f"  if (so == {so}) return fmm_m2l_cm_s{so}(P, st);")
-    table += ["  return FMM_ERR_STATE;", "}",
-              "static inline int fmm_m2l_tp_launch(int so, const TpParams &P, cudaStream_t st) {"]
-    for so, pmax in FAMILIES:
-        table.append(f"  if (so == {so}) return fmm_m2l_tp_s{so}(P, st);")
-    table += ["  return FMM_ERR_STATE;", "}"]
+    for so in sorted({f[0] for f in fams}):
+        table.append(f"  if (so == {so}) return {max(pm for s_, pm in fams if s_ == so)};")
+    table += ["  return 0;", "}"]
+    for kind, params in (("cm", "CmParams"), ("tp", "TpParams")):
+        table += [f"// launch the family of source order so with the smallest largest order >= P.p (FMM_ERR_STATE: none)",
+                  f"static inline int fmm_m2l_{kind}_launch(int so, const {params} &P, cudaStream_t st) {{"]
+        for so, pmax in fams:
+            table.append(f"  if (so == {so} && P.p <= {pmax}) return fmm_m2l_{kind}_s{so}_p{pmax}(P, st);")
+        table += ["  return FMM_ERR_STATE;", "}"]
     hdr = os.path.join(CSRC, "m2l_cm.cuh")
     with open(hdr, "w") as f:
         f.write(HEADER + "\n".join(decl) + "\n" + "\n".join(table) + "\n")
     outs.append(hdr)
+    # generated files of families no longer listed
+    keep = {family_file(so, pm) for so, pm in FAMILIES}
+    for fn in os.listdir(CSRC):
+        if fn.startswith("m2l_cm_s") and fn.endswith(".cu") and fn not in keep:
+            os.remove(os.path.join(CSRC, fn))
     return outs
 
 
