@@ -375,7 +375,9 @@ __global__ void k_ss_chain(const double *__restrict__ pos, long N, long nchunks,
             if (lane >= d) mp = compose(o, mp);
           }
           long long Sj = S + ((S & 1) ? mp.i1 : mp.i0);
-          bool leaves = el.bad || !(S > 0 ? (Sj >= LO && Sj < HI) : (Sj <= -LO && Sj > -HI));
+          // strictly inside the binade: a result of exactly 2^52 ulps may be the rounding of a sum
+          // just below the power of two, whose true rounding is on the finer grid below it
+          bool leaves = el.bad || !(S > 0 ? (Sj > LO && Sj < HI) : (Sj < -LO && Sj > -HI));
           unsigned bal = __ballot_sync(FULL, act && leaves);
           if (bal == 0) {
             S = __shfl_sync(FULL, Sj, cnt - 1);
