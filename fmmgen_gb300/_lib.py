@@ -84,6 +84,7 @@ _SIGS = {
     "fmmgen_tree_export_lists": (C.c_int, [_vp, _lp, _lp]),
     "fmmgen_tree_export_expansions": (C.c_int, [_vp, _dp, _dp]),
     "fmmgen_tree_times": (C.c_int, [_vp, _vp, _vp]),
+    "fmmgen_tree_kernel_ms": (C.c_int, [_vp, _vp]),
     "fmmgen_tree_m2l_work": (C.c_int, [_vp, _dp]),
     "fmmgen_tree_set_tune": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
     "fmmgen_tree_get_tune": (C.c_int, [_vp, _vp]),

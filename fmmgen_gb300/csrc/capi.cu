@@ -671,6 +671,18 @@ int fmmgen_mlp_adam(float *params, const float *grad, float *m, float *v, int st
 }
 }  // extern "C"
 
+extern "C" int fmmgen_tree_kernel_ms(fmmgen_tree *tree, float *ms2) {
+  if (!tree || !tree->built || !ms2) return ret(FMM_ERR_STATE);
+  FMM_CUDA_TRY(cudaDeviceSynchronize());
+  ms2[0] = ms2[1] = -1.f;
+  if (tree->last_precision >= 0) {
+    fmm_eval_times(&tree->t);
+    ms2[0] = tree->t.kernel_ms[0];
+    ms2[1] = tree->t.kernel_ms[1];
+  }
+  return FMM_OK;
+}
+
 extern "C" int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8) {
   if (!tree || !tree->built) return ret(FMM_ERR_STATE);
   FMM_CUDA_TRY(cudaDeviceSynchronize());

@@ -605,6 +605,16 @@ static int rec(DevTree *t, int i, cudaStream_t st) {
   return FMM_OK;
 }
 
+int fmm_mark_kernel(DevTree *t, int which, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FMM_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusActive)
+    FMM_CUDA_TRY(cudaEventRecordWithFlags(t->ev_mk[which], st, cudaEventRecordExternal));
+  else
+    FMM_CUDA_TRY(cudaEventRecord(t->ev_mk[which], st));
+  return FMM_OK;
+}
+
 template <typename T>
 static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed, int impl, int mstr, int lstr,
                      int dstr, cudaStream_t st);
@@ -755,6 +765,7 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
       if (rc != FMM_ERR_STATE) return rc;
     }
     FMM_CUDA_TRY(cudaMemsetAsync(L, 0, sizeof(T) * (size_t)nc * lstr, st));
+    TRY(fmm_mark_kernel(t, 0, st));
     for (int q = so + 1; q <= p; q++) {
       const PlanSet *pq = fmm_get_plans(q, so);
       if (!pq) return FMM_ERR_CUDA;
@@ -768,6 +779,7 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
             mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L,
             mstr, lstr, dstr);
     }
+    TRY(fmm_mark_kernel(t, 1, st));
   } else if (mixed && is_tc(impl)) {
     TRY(fmm_m2l_tc(t, (const float *)(const void *)M, mstr, (float *)(void *)L, lstr, st, impl == M2L_TCG));
   } else if (mixed && impl == M2L_CM) {
@@ -778,20 +790,26 @@ static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed
     m2l_reg_kernel kg[4];
     int kthreads[4];
     const int ng = m2l_reg_kernels(p, so, kg, kthreads);
+    TRY(fmm_mark_kernel(t, 0, st));
     for (int g = 0; g < ng; g++)
       fmm_note_launch(), kg[g]<<<(nc + kthreads[g] - 1) / kthreads[g], kthreads[g], 0, st>>>(
           t->nm2l > 0 ? t->m2l_order.p : nullptr, nc, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
           (const float *)t->cls_Df.p, t->clevel.p,
           (const float *)(const void *)M, (float *)(void *)L);
+    TRY(fmm_mark_kernel(t, 1, st));
   } else if constexpr (std::is_same<T, float>::value) {
+    TRY(fmm_mark_kernel(t, 0, st));
     fmm_note_launch(), k_m2l_pk<M2L_PACK><<<fmm_blocks(nc, PackF<M2L_PACK>::WARPS), 32 * PackF<M2L_PACK>::WARPS, 0, st>>>(
         ps->m2l, p, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p, nullptr, (const float *)t->cls_Df.p,
         t->clevel.p, M, L, mstr, lstr, dstr);
+    TRY(fmm_mark_kernel(t, 1, st));
   } else {
+    TRY(fmm_mark_kernel(t, 0, st));
     fmm_note_launch(), k_m2l<T><<<fmm_blocks(nc, FMM_WARPS), 32 * FMM_WARPS, 0, st>>>(
         ps->m2l, nc, so, p, t->m2l_off.p, t->m2l_src.p, t->m2l_cls.p,
         mixed ? (const T *)(const void *)t->cls_Df.p : (const T *)(const void *)t->cls_D.p, t->clevel.p, M, L, mstr,
         lstr, dstr);
+    TRY(fmm_mark_kernel(t, 1, st));
   }
   FMM_CUDA_TRY(cudaGetLastError());
   return FMM_OK;
@@ -1245,6 +1263,13 @@ void fmm_eval_times(DevTree *t) {
     t->phase_ms[i] = ms;
   }
   if (t->p2p_first) std::swap(t->phase_ms[2], t->phase_ms[3]);  // the pass ran P2P, then M2L
+  for (int k = 0; k < 2; k++) {
+    if (cudaEventElapsedTime(&ms, t->ev_mk[2 * k], t->ev_mk[2 * k + 1]) != cudaSuccess) {
+      ms = -1.f;
+      cudaGetLastError();
+    }
+    t->kernel_ms[k] = ms;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -133,6 +133,8 @@ struct DevTree {
   float phase_ms[8] = {0};
   float build_ms[6] = {0};                // root, keys+sort, levels, lists, classes, total
   cudaEvent_t ev[16];
+  cudaEvent_t ev_mk[4];                   // around the last pass's M2L kernels (not their preparation), P2P kernel
+  float kernel_ms[2] = {-1.f, -1.f};      // ... their device times: M2L, P2P
   bool ev_ready = false;
   // evaluation pass as a CUDA graph (fmmgen_tree_set_graph): replayed while
   // the build, the arrays and the switches are those it was captured with
@@ -206,6 +208,9 @@ bool fmm_m2l_tc_step_work(int p, int so, bool boxes, long long *mmas, double *fl
 // boxes: source rows by tensor-map box loads from level grids where every level is complete
 int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStream_t st, bool boxes);
 void fmm_tcg_release(DevTree *t);
+// marks the start (which 0) / end (1) of the pass's M2L kernels, the start (2) / end (3) of its
+// P2P kernel, on their streams
+int fmm_mark_kernel(DevTree *t, int which, cudaStream_t st);
 // the tiles' class-step schedule (tc_sched_off / tc_sched_cls / tc_stab), once per build and cell order
 int fmm_tc_schedule(DevTree *t, cudaStream_t st);
 // class-major generated CUDA-core M2L over that schedule (m2l_cm_s*.cu); ord: per-pair orders in target-list

@@ -1443,6 +1443,7 @@ int tcg_run(DevTree *t, const TcPlan &pl, const float *M, int mstr, float *L, in
   P.err = t->d_tcerr.p;
   const int grid = std::min(P.ntiles, tc_sm_count());
   int rc;
+  if ((rc = fmm_mark_kernel(t, 0, st))) return rc;
   switch (pl.nout) {
     case 16: rc = tcg_launch<16>(s->maps, P, smem, grid, st); break;
     case 32: rc = tcg_launch<32>(s->maps, P, smem, grid, st); break;
@@ -1454,7 +1455,7 @@ int tcg_run(DevTree *t, const TcPlan &pl, const float *M, int mstr, float *L, in
     case 224: rc = tcg_launch<224>(s->maps, P, smem, grid, st); break;
     default: return FMM_ERR_ARG;
   }
-  if (rc) return rc;
+  if (rc || (rc = fmm_mark_kernel(t, 1, st))) return rc;
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, 4 * sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, st));
   return FMM_OK;
@@ -1640,6 +1641,7 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
   P.err = t->d_tcerr.p;
   const int grid = std::min(P.ntiles, tc_sm_count());
   int rc;
+  if ((rc = fmm_mark_kernel(t, 0, st))) return rc;
   switch (pl.nout) {
     case 16: rc = tc_launch<16>(P, smem, grid, st); break;
     case 32: rc = tc_launch<32>(P, smem, grid, st); break;
@@ -1651,7 +1653,7 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
     case 224: rc = tc_launch<224>(P, smem, grid, st); break;
     default: return FMM_ERR_ARG;
   }
-  if (rc) return rc;
+  if (rc || (rc = fmm_mark_kernel(t, 1, st))) return rc;
   // timeout flags reach the host with the stream (read by fmmgen_tree_times)
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, 4 * sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, st));
@@ -1804,7 +1806,9 @@ int fmm_m2l_cm(DevTree *t, const float *M, int mstr, float *L, int lstr, const u
   P.L = L;
   P.lstr = lstr;
   P.lsize = lsize;
-  return fmm_m2l_cm_launch(so, P, st);
+  int rc = fmm_mark_kernel(t, 0, st);
+  if (!rc) rc = fmm_m2l_cm_launch(so, P, st);
+  return rc ? rc : fmm_mark_kernel(t, 1, st);
 }
 
 int fmm_m2l_tp(DevTree *t, const float *M, int mstr, float *L, int lstr, const unsigned char *ord, cudaStream_t st) {
@@ -1849,5 +1853,7 @@ int fmm_m2l_tp(DevTree *t, const float *M, int mstr, float *L, int lstr, const u
   P.L = L;
   P.lstr = lstr;
   P.lsize = lsize;
-  return fmm_m2l_tp_launch(so, P, st);
+  int rc = fmm_mark_kernel(t, 0, st);
+  if (!rc) rc = fmm_m2l_tp_launch(so, P, st);
+  return rc ? rc : fmm_mark_kernel(t, 1, st);
 }

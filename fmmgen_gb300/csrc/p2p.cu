@@ -445,15 +445,17 @@ int fmm_p2p_launch(DevTree *t, bool mixed, const double *S, cudaStream_t st, boo
       k = narrow ? (pot ? k_p2p32<true, 2, 0> : k_p2p32<false, 2, 0>)
                  : (pot ? k_p2p32<true, P2P_WARPS, 0> : k_p2p32<false, P2P_WARPS, 0>);
     const unsigned grid = fmm_blocks(nl, wp);
+    if (int rc = fmm_mark_kernel(t, 2, st)) return rc;
     fmm_note_launch(), k<<<grid, 32 * wp, 0, st>>>(t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p,
                                                    t->p2p_src.p, t->phi4.p, t->plo4.p, t->sdip.p, t->Fnear.p);
   } else {
+    if (int rc = fmm_mark_kernel(t, 2, st)) return rc;
     fmm_note_launch(), k_p2p64<<<fmm_blocks(nl, P2P_WARPS), 32 * P2P_WARPS, 0, st>>>(
         t->leaf_cells.p, nl, t->pstart.p, t->pcount.p, t->p2p_off.p, t->p2p_src.p, t->px.p, t->py.p, t->pz.p,
         t->perm.p, S, so, t->Fnear.p);
   }
   FMM_CUDA_TRY(cudaGetLastError());
-  return FMM_OK;
+  return fmm_mark_kernel(t, 3, st);
 }
 
 int fmm_stage_particles(DevTree *t, const double *S, cudaStream_t st) {

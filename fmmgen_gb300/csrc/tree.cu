@@ -648,6 +648,7 @@ int fmm_tree_build(DevTree *t, const double *pos, long N, long ncrit, int order,
   FMM_CUDA_TRY(cudaGetDevice(&t->dev));
   if (!t->ev_ready) {
     for (int i = 0; i < 16; i++) FMM_CUDA_TRY(cudaEventCreate(&t->ev[i]));
+    for (int i = 0; i < 4; i++) FMM_CUDA_TRY(cudaEventCreate(&t->ev_mk[i]));
     t->ev_ready = true;
   }
   if (!t->h_pinned) {
@@ -1177,5 +1178,7 @@ void fmm_tree_destroy(DevTree *t) {
   t->h_pinned = nullptr;
   if (t->ev_ready)
     for (int i = 0; i < 16; i++) cudaEventDestroy(t->ev[i]);
+  if (t->ev_ready)
+    for (int i = 0; i < 4; i++) cudaEventDestroy(t->ev_mk[i]);
   t->ev_ready = false;
 }

@@ -305,6 +305,14 @@ class Tree:
         check(lib().fmmgen_tree_m2l_work(self._h, w.ctypes.data))
         return tuple(float(x) for x in w)
 
+    def kernel_ms(self):
+        """Device times (ms) of the last evaluate's M2L kernels and P2P kernel
+        alone (events on their streams around the launches, preparation
+        excluded): {"M2L": ms, "P2P": ms}, -1 where none ran."""
+        v = np.zeros(2, np.float32)
+        check(lib().fmmgen_tree_kernel_ms(self._h, v.ctypes.data))
+        return {"M2L": float(v[0]), "P2P": float(v[1])}
+
     def times(self):
         b = np.zeros(6, np.float32)
         e = np.zeros(8, np.float32)

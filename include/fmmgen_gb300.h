@@ -229,6 +229,12 @@ int fmmgen_tree_export_expansions(fmmgen_tree *tree, double *M, double *L);
 /* Phase times of the last build ([root, keys+sort, cells, lists, classes, total])
  * and evaluate ([P2M, M2M, M2L, P2P, L2L, L2P, finalize, total]) in ms. */
 int fmmgen_tree_times(fmmgen_tree *tree, float *build_ms6, float *eval_ms8);
+/* Device times (ms) of the last evaluate's M2L kernels and P2P kernel alone,
+ * host ms2 = [M2L, P2P], from events on their streams around the launches (no
+ * counterpart in the reference; for roofline accounting): the M2L phase of
+ * fmmgen_tree_times also holds its preparation (schedules, operand packing),
+ * and the two kernels may run side by side; -1 where none ran. */
+int fmmgen_tree_kernel_ms(fmmgen_tree *tree, float *ms2);
 /* Work of the last tensor-core M2L (no counterpart in the reference; for
  * roofline accounting), host out4 = [class steps of 128-row tiles, tcgen05 MMA
  * instructions, executed tensor flops, 1 if its source rows were boxed from

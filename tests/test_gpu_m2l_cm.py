@@ -94,3 +94,17 @@ def test_no_pairs(fg, impl):
     F = t.compute_field_fmm(precision="mixed").cpu().numpy()
     F64 = t.compute_field_fmm(precision="fp64").cpu().numpy()
     assert rel(F, F64) < 1e-6
+
+
+@pytest.mark.parametrize("impl", [3, 0, 1, 2, 4, 5])
+def test_kernel_times(fg, impl):
+    """Every M2L implementation brackets its kernels with events: the kernel
+    time is positive and within the M2L phase of the pass."""
+    pos, S = system("uniform", 40000, 0, 9)
+    t = fg.build_tree(pos, S, pos.shape[0], 64, 6, 0.5)
+    t.set_tune(impl=impl)
+    t.compute_field_fmm(precision="mixed")
+    k = t.kernel_ms()
+    ph = t.times()[1]
+    assert k["M2L"] > 0 and k["P2P"] > 0, k
+    assert k["M2L"] <= ph["M2L"] + 1e-3, (k, ph)
