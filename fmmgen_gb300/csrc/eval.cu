@@ -992,9 +992,10 @@ static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L
   TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, t->s_hi));
   TRY(rec(t, 3, t->s_hi));
   FMM_CUDA_TRY(cudaEventRecord(t->ev_join, t->s_hi));
-  if (!learned) {  // beside the M2L, launched after it
+  if (!learned) {  // launched after the M2L: beside it with the overlap switch, else behind it
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_s, 0));
+    if (!t->tune.overlap) FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
     TRY(fmm_p2p_launch(t, mixed, S, st, mixed && is_tc(impl) && t->tune.overlap == 2));
   }
   FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));

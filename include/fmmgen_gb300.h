@@ -267,7 +267,8 @@ int fmmgen_tree_get_tune(fmmgen_tree *tree, int *tune4);
 /* Autotuner: one pass over S at `precision` (for the multipoles and the staged
  * particles), then the M2L and P2P phases alone timed `reps` times per
  * candidate (implementation x pipeline depth x overlap x grouping that this
- * order supports); the handle keeps the candidate with the lowest median.
+ * order supports); the handle keeps the candidate with the lowest median, or
+ * its serial twin (overlap 0) when that is within 2 % of it.
  * cand4 [max_cand][4] (impl, nslots, grouping, overlap) and cand_ms [max_cand]
  * receive the table (either may be NULL), *ncand its size. */
 int fmmgen_tree_autotune(fmmgen_tree *tree, const double *S, int precision, int reps, int max_cand, int *cand4,

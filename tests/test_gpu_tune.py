@@ -32,7 +32,12 @@ def test_autotune_candidates(fg, p, so):
     assert (0 in impls) == (p <= 9)  # tensor cores where the order allows
     assert all(c["ms"] > 0 for c in table)
     best = min(table, key=lambda c: c["ms"])
-    assert r["best"] == {k: best[k] for k in ("impl", "nslots", "grouping", "overlap")}
+    key = ("impl", "nslots", "grouping", "overlap")
+    if r["best"] != {k: best[k] for k in key}:
+        # the serial twin of an overlapped fastest candidate, within 2 % of it
+        assert best["overlap"] and r["best"]["overlap"] == 0, (r["best"], best)
+        twin = [c for c in table if {k: c[k] for k in key} == r["best"]]
+        assert twin and all(r["best"][k] == best[k] for k in key[:3]) and twin[0]["ms"] <= 1.02 * best["ms"]
     F = t.compute_field_fmm(precision="mixed").cpu().numpy()
     assert rel(F, ref) < 2e-6
     for c in table:
