@@ -60,6 +60,7 @@ RMAX = 208              # register estimate per thread an output group may reach
 OVERHEAD = 32           # registers besides accumulators, temporaries and the chunk
 PARTIAL_MIN_TERMS = 21  # outputs with at least this many terms per pair (in a kernel) sum per pair first
 ROWS = 128              # threads of a block (class-major: rows of a schedule tile)
+TP_PREFETCH_QUADS = 2   # target-major: operator quads of the next degree block loaded a block ahead
 MIN_BLOCKS = 2          # resident blocks per SM the register allocation must allow
 
 
@@ -151,9 +152,12 @@ def plan(so, pmax):
 COMP = "xyzw"
 
 
-def chunk_body(so, pmax, c, kern, srcexpr, dload, ind):
+def chunk_body(so, pmax, c, kern, srcexpr, dload, ind, prefetch_quads=0):
     """Multiply one staged chunk: its multipole terms from shared memory
-    (scaled by the level difference), the terms nested by degree."""
+    (scaled by the level difference), the terms nested by degree; with
+    prefetch_quads, each degree block first loads that many of the next
+    block's operator quads (global loads, whose latency the block's own
+    multiply-adds then cover)."""
     mono = monomials(pmax)
     moff = nterms(so - 1)
     i0 = kern["outs"][0]
@@ -179,12 +183,38 @@ def chunk_body(so, pmax, c, kern, srcexpr, dload, ind):
     by_d = {}
     for t in c["terms"]:
         by_d.setdefault(t[0], []).append(t)
+    dlo, dhi = min(by_d), max(by_d)
+    # the quads each degree block loads first, in order of use
+    first = {}
+    seen = set()
+    for d in range(dlo, dhi + 1):
+        first[d] = []
+        for (_, k, i, jj) in by_d.get(d, []):
+            if k // 4 not in seen:
+                seen.add(k // 4)
+                first[d].append(k // 4)
     depth = 0
     loaded = set()
-    for d in range(min(by_d), max(by_d) + 1):
+
+    def prefetch(d, ii, guard):
+        # the first quads of block d, loaded a block ahead (warp-uniform: d <= qmax <= the pass's order,
+        # so every load stays inside the class's row)
+        for kq in first.get(d, [])[:prefetch_quads]:
+            if guard:
+                L.append(ii + f"float4 dq{kq} = make_float4(0.f, 0.f, 0.f, 0.f);")
+                L.append(ii + f"if (qmax >= {d}) dq{kq} = {dload(kq)};")
+            else:
+                L.append(ii + f"const float4 dq{kq} = {dload(kq)};")
+            loaded.add(kq)
+
+    if prefetch_quads:
+        prefetch(dlo, ind, False)  # the chunk runs only when qmax reaches its lowest degree
+    for d in range(dlo, dhi + 1):
         L.append(ind + "  " * depth + f"if (ql >= {d}) {{")
         depth += 1
         ii = ind + "  " * depth
+        if prefetch_quads and d < dhi:
+            prefetch(d + 1, ii, True)
         for (_, k, i, jj) in by_d.get(d, []):
             kq = k // 4
             if kq not in loaded:
@@ -215,7 +245,7 @@ def stage_chunk(c, chq, chb, bufexpr, bvar, ind):
             ind + "}"]
 
 
-def pipeline(so, pmax, kern, chq, chb, dload, prefetch_next, ind):
+def pipeline(so, pmax, kern, chq, chb, dload, prefetch_next, ind, prefetch_quads=0):
     """The chunks of one pair (or step): chunk j+1 staged while j is multiplied;
     after the last, prefetch_next(ind) stages the next pair's first chunk."""
     chunks = kern["chunks"]
@@ -234,7 +264,7 @@ def pipeline(so, pmax, kern, chq, chb, dload, prefetch_next, ind):
         L.append(ind + "  }")
         L.append(ind + "  __syncwarp();")
         L.extend(chunk_body(so, pmax, c, kern, f"sbuf + ((base + {ci}) & 1) * {chb} + lane * {chq + 1}", dload,
-                            ind + "  "))
+                            ind + "  ", prefetch_quads))
         L.append(ind + "  __syncwarp();  // the buffer is refilled two chunks on")
         L.append(ind + "}")
     return L
@@ -438,7 +468,7 @@ def emit_tp(so, pmax, ki, kern):
              ind + "}"]
 
     L.extend(pipeline(so, pmax, kern, chq, chb, lambda kq: f"__ldg((const float4 *)(Dp + {4 * kq}))",
-                      prefetch_next, "    "))
+                      prefetch_next, "    ", TP_PREFETCH_QUADS))
     for i in kern["outs"]:
         if i in temps:
             L.append(f"    a{i - i0} += t{i - i0};")
