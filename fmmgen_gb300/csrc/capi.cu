@@ -522,12 +522,12 @@ extern "C" int fmmgen_tree_m2l_work(fmmgen_tree *tree, double *out4) {
   long long mmas = 0;
   double flops = 0;
   unsigned long long steps = 0;
-  if (t.h_pinned && fmm_m2l_tc_step_work(t.order, t.so, t.tc_boxes_last != 0, &mmas, &flops))
+  if (t.h_pinned && t.tc_ran && fmm_m2l_tc_step_work(t.order, t.so, t.tc_boxes_last != 0, &mmas, &flops))
     memcpy(&steps, t.h_pinned + FMM_PINNED_TCERR + 2, sizeof(steps));
   out3[0] = (double)steps;
   out3[1] = (double)steps * (double)mmas;
   out3[2] = (double)steps * flops;
-  out4[3] = t.tc_boxes_last ? 1.0 : 0.0;
+  out4[3] = t.tc_ran && t.tc_boxes_last ? 1.0 : 0.0;
   return FMM_OK;
 }
 

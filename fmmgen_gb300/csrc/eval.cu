@@ -746,6 +746,7 @@ template <typename T>
 static int m2l_phase(DevTree *t, const PlanSet *ps, const T *M, T *L, bool mixed, int impl, int mstr, int lstr,
                      int dstr, cudaStream_t st) {
   const int p = t->order, so = t->so, nc = t->ncells;
+  t->tc_ran = 0;
   // every M2L but the tensor cores' reads the target lists
   if (t->ord_mode != 0 || !(mixed && (is_tc(impl) || impl == M2L_CM))) TRY(fmm_m2l_csr(t, st));
   // a tuned choice pins the per-pair-order kernels: 2 the engine, 4 class-major, else target-major
@@ -992,10 +993,11 @@ static int fused_pass(DevTree *t, const PlanSet *ps, const double *S, T *M, T *L
   TRY(m2l_phase<T>(t, ps, M, L, mixed, impl, mstr, lstr, dstr, t->s_hi));
   TRY(rec(t, 3, t->s_hi));
   FMM_CUDA_TRY(cudaEventRecord(t->ev_join, t->s_hi));
-  if (!learned) {  // launched after the M2L: beside it with the overlap switch, else behind it
+  if (!learned) {  // launched after the M2L, beside it; behind the tensor-core M2L without the overlap
+                   // switch (its CTA leaves room for one P2P block per SM: side by side gains nothing there)
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_c, 0));
     FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_s, 0));
-    if (!t->tune.overlap) FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
+    if (!t->tune.overlap && mixed && is_tc(impl)) FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));
     TRY(fmm_p2p_launch(t, mixed, S, st, mixed && is_tc(impl) && t->tune.overlap == 2));
   }
   FMM_CUDA_TRY(cudaStreamWaitEvent(st, t->ev_join, 0));

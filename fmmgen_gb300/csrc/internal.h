@@ -122,6 +122,7 @@ struct DevTree {
   DevBuf<int> tp_tgt;                     // targets by level, then by their count of high-order pairs
   void *tcg = nullptr;                    // level-grid tensor-core M2L state (m2l_tc.cu, fmm_tcg_release)
   int tc_boxes_last = 0;                  // the last tensor-core M2L boxed its source rows from level grids
+  int tc_ran = 0;                         // the last pass's M2L ran on the tensor cores
   uint64_t sched_serial = ~0ull, sched_version = ~0ull;  // ... of this build and cell order
   uint64_t order_version = 0;             // incremented whenever m2l_order is rewritten
   int tc_order = -1, tc_so = -1;          // ... and to this expansion order and source order

@@ -1456,6 +1456,7 @@ int tcg_run(DevTree *t, const TcPlan &pl, const float *M, int mstr, float *L, in
     default: return FMM_ERR_ARG;
   }
   if (rc || (rc = fmm_mark_kernel(t, 1, st))) return rc;
+  t->tc_ran = 1;
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, 4 * sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, st));
   return FMM_OK;
@@ -1654,6 +1655,7 @@ int fmm_m2l_tc(DevTree *t, const float *M, int mstr, float *L, int lstr, cudaStr
     default: return FMM_ERR_ARG;
   }
   if (rc || (rc = fmm_mark_kernel(t, 1, st))) return rc;
+  t->tc_ran = 1;
   // timeout flags reach the host with the stream (read by fmmgen_tree_times)
   FMM_CUDA_TRY(cudaMemcpyAsync(t->h_pinned + FMM_PINNED_TCERR, t->d_tcerr.p, 4 * sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, st));
